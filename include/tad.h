@@ -1,0 +1,260 @@
+/*
+ * tad.h -- C ABI of the GB300 sparse per-element derivative library.
+ *
+ * One opaque problem object stands for one TinyAD ScalarFunction: a set of
+ * d-dimensional variable handles plus a list of objective terms, each a set
+ * of elements of fixed valence N evaluated by a per-element energy.  All
+ * entry points take plain pointers and sizes; "_h" buffers are host memory,
+ * "_d" buffers are device memory of the current CUDA device.
+ *
+ * Reference interface each entry point replaces (TinyAD, MIT licence):
+ *   tad_problem_create        ScalarFunction ctor / scalar_function<d>(range)
+ *                             include/TinyAD/Detail/ScalarFunctionImpl.hh:47-61, :418-442
+ *   tad_add_elements          ScalarFunction::add_elements<N>(range, lambda)
+ *                             include/TinyAD/Detail/ScalarFunctionImpl.hh:63-100
+ *   tad_add_elements_custom   the same, for a user functor compiled by the C++
+ *                             front end (include/tad/ScalarFunction.cuh)
+ *   tad_eval                  ScalarFunction::eval / operator()
+ *                             include/TinyAD/Detail/ScalarFunctionImpl.hh:256-282
+ *   tad_eval_with_gradient    ScalarFunction::eval_with_gradient
+ *                             include/TinyAD/Detail/ScalarFunctionImpl.hh:284-314
+ *   tad_eval_with_derivatives ScalarFunction::eval_with_derivatives / eval_hessian
+ *                             include/TinyAD/Detail/ScalarFunctionImpl.hh:316-376
+ *   tad_eval_with_hessian_proj ScalarFunction::eval_with_hessian_proj
+ *                             include/TinyAD/Detail/ScalarFunctionImpl.hh:378-416
+ *   tad_hessian_pattern       the index arrays of the returned Eigen::SparseMatrix
+ *                             (outerIndexPtr/innerIndexPtr; H is symmetric so the
+ *                             CSR arrays here equal Eigen's CSC arrays)
+ *   tad_newton_direction      newton_direction(g, H, solver)
+ *                             include/TinyAD/Utils/NewtonDirection.hh:25-65
+ *   tad_line_search           line_search(x, d, f, g, func)
+ *                             include/TinyAD/Utils/LineSearch.hh:26-65
+ *   tad_newton_solve          the Projected-Newton loop users write around the
+ *                             three calls above (tests/NewtonTest.cc:69-75)
+ *   tad_adjoint_rest_gradient no reference counterpart (adjoint extension)
+ *   tad_batch_*               no reference counterpart (batched extension)
+ *
+ * Errors: every entry point returns a tad_status; tad_last_error_message()
+ * gives the text for the calling thread.  The reference throws
+ * std::runtime_error (include/TinyAD/Utils/Out.hh:73-79); the C++ front end
+ * turns a non-OK status back into that exception.  A problem stays usable
+ * after an error (tests/ExceptionTest.cc:8-53).
+ */
+#ifndef TAD_H
+#define TAD_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define TAD_API __declspec(dllexport)
+#else
+#define TAD_API __attribute__((visibility("default")))
+#endif
+
+typedef enum tad_status {
+    TAD_OK = 0,
+    TAD_ERR_ARG = 1,          /* invalid argument (sizes, handles, null pointers) */
+    TAD_ERR_NONFINITE = 2,    /* non-finite input or non-finite derivative */
+    TAD_ERR_PCG_NOCONV = 3,   /* linear solve did not reach its tolerance */
+    TAD_ERR_LS_FAIL = 4,      /* warning: line search found no decrease, x kept */
+    TAD_ERR_TIMEOUT = 5,      /* a bounded device-side wait gave up */
+    TAD_ERR_CUDA = 6,         /* CUDA runtime error */
+    TAD_ERR_STATE = 7,        /* call not valid in the problem's current state */
+    TAD_ERR_TOO_MANY_VARS = 8 /* element accessed more handles than its valence */
+} tad_status;
+
+/* Built-in per-element energies (params are per element, doubles). */
+typedef enum tad_energy {
+    /* d=2, N=3: params [Mr00 Mr10 Mr01 Mr11 w] (Mr column-major = rest edge
+       matrix [b-a, c-a]).  E = w * (|M Mr^-1|_F^2 + |Mr M^-1|_F^2), +inf if
+       det M <= 0.  Same lambda as tests/NewtonTest.cc:28-44. */
+    TAD_ENERGY_SYMMETRIC_DIRICHLET_TRI = 0,
+    /* d=3, N=4: params [Mr (3x3 column-major) w], 3D analogue. */
+    TAD_ENERGY_SYMMETRIC_DIRICHLET_TET = 1,
+    /* any d, N=1: params [target(d) w].  E = w * |target - p|^2
+       (tests/NewtonTest.cc:48-55). */
+    TAD_ENERGY_POSITION_PENALTY = 2,
+    /* any d, N: params [A (k*k, row-major) b (k) c], k = d*N.
+       E = sum_ij A_ij x_i x_j + sum_i b_i x_i + c over the element's
+       variables in access order (the quadratics of tests/ScalarFunctionTest.cc). */
+    TAD_ENERGY_QUADRATIC = 3,
+    /* any d, N=3: params [w].  E = w * (|b-a|^2 + |c-b|^2 + |a-c|^2)
+       (the Laplacian test of tests/DynamicElementsTest.cc:60-91 with w=1/4). */
+    TAD_ENERGY_DIRICHLET_TRI = 4,
+    TAD_ENERGY_COUNT_ = 5
+} tad_energy;
+
+typedef enum tad_precision {
+    TAD_PREC_FP64 = 0,   /* plain drop-in: everything in double */
+    TAD_PREC_MIXED = 1   /* FP32 element Hessians, projection and PCG; FP64
+                            determinant/inverse, line-search energy and
+                            iterative-refinement residuals */
+} tad_precision;
+
+typedef struct tad_settings {
+    int precision;            /* tad_precision */
+    int pcg_max_iters;        /* per linear solve (default 1000) */
+    double pcg_rel_tol;       /* relative residual target (default 1e-10) */
+    int refine_max_iters;     /* mixed mode: iterative-refinement passes (default 4) */
+    double refine_rel_tol;    /* mixed mode: FP64 residual target (default 1e-10) */
+    int ls_max_iters;         /* line search trials (reference default 64) */
+    double ls_shrink;         /* 0.8 */
+    double ls_armijo;         /* 1e-4 */
+    int verbose;
+} tad_settings;
+
+typedef struct tad_problem tad_problem;
+
+/* Fill *s with the defaults above. */
+TAD_API void tad_settings_default(tad_settings* s);
+
+TAD_API const char* tad_last_error_message(void);
+TAD_API const char* tad_version(void);
+
+/* Create a problem with n_handles variable handles of dimension var_dim
+   (n_vars = var_dim * n_handles, interleaved x[d*v + i]).  Uses the current
+   CUDA device. */
+TAD_API tad_status tad_problem_create(int var_dim, int64_t n_handles,
+                                      const tad_settings* settings,
+                                      tad_problem** out);
+TAD_API tad_status tad_problem_destroy(tad_problem* p);
+TAD_API tad_status tad_problem_set_settings(tad_problem* p, const tad_settings* s);
+TAD_API int64_t tad_n_vars(const tad_problem* p);
+
+/* Add n_elem elements of valence N, each naming N variable handles in the
+   order its energy accesses them (handles_h: n_elem*N int32, host), with
+   n_params doubles per element (params_h: n_elem*n_params, host). */
+TAD_API tad_status tad_add_elements(tad_problem* p, int energy, int valence,
+                                    int64_t n_elem, const int32_t* handles_h,
+                                    const double* params_h, int n_params);
+
+/* User-functor terms (the C++ front end).  The callback evaluates all
+   elements of the term on the library's stream and writes per-element
+   outputs into library-owned device buffers; see tad_term_eval_args. */
+typedef struct tad_term_eval_args {
+    int mode;                 /* tad_eval_mode */
+    int precision;            /* tad_precision of the outputs */
+    int64_t n_elem;
+    int valence;
+    int var_dim;
+    const double* x_d;        /* current x (device, n_vars) */
+    const double* dir_d;      /* line search: direction (device) */
+    const double* steps_d;    /* line search: n_steps trial step sizes */
+    int n_steps;
+    int64_t f_row_stride;     /* line search: trial j writes out_f_d + j*f_row_stride */
+    double proj_eps;
+    const int32_t* handles_d; /* recorded access order, n_elem*N, -1 = unused slot */
+    void* out_f_d;            /* double[n_elem] (or [n_steps][n_elem]) */
+    void* out_g_d;            /* [n_elem][N*d] in output precision */
+    void* out_H_d;            /* [n_elem][N(N+1)/2 slot pairs][d][d] */
+    int32_t* record_d;        /* TAD_MODE_RECORD: write accessed handles here */
+    int32_t* error_d;         /* device error word (OR in TAD_DEVERR_* bits) */
+    void* stream;             /* cudaStream_t */
+} tad_term_eval_args;
+
+typedef enum tad_eval_mode {
+    TAD_MODE_VALUE = 0,       /* f only */
+    TAD_MODE_GRADIENT = 1,    /* f, g */
+    TAD_MODE_HESSIAN = 2,     /* f, g, H */
+    TAD_MODE_HESSIAN_PROJ = 3,/* f, g, PSD-projected H */
+    TAD_MODE_LINESEARCH = 4,  /* f at x + s_j * dir for j < n_steps */
+    TAD_MODE_RECORD = 5       /* record first-access handle order */
+} tad_eval_mode;
+
+typedef int (*tad_term_eval_fn)(void* user, const tad_term_eval_args* args);
+
+/* element_handles_h: n_elem int32 element handles (passed to the functor).
+   The library records each element's access order with one TAD_MODE_RECORD
+   call when the sparsity pattern is built. */
+TAD_API tad_status tad_add_elements_custom(tad_problem* p, int valence,
+                                           int64_t n_elem,
+                                           tad_term_eval_fn fn, void* user);
+
+/* Build the sparsity pattern now (otherwise done by the first eval). */
+TAD_API tad_status tad_finalize(tad_problem* p);
+
+/* Number of non-zeros of the assembled Hessian (explicit zeros kept, so
+   nnz = union of the element blocks, as Eigen's setFromTriplets keeps them). */
+TAD_API tad_status tad_hessian_nnz(tad_problem* p, int64_t* nnz);
+/* CSR arrays of the pattern: outer (n_vars+1) and inner (nnz), int32, host. */
+TAD_API tad_status tad_hessian_pattern(tad_problem* p, int32_t* outer_h, int32_t* inner_h);
+
+/* Evaluations (host buffers).  g_h: n_vars doubles.  H_values_h: nnz doubles
+   in the order of tad_hessian_pattern (may be NULL to skip the copy). */
+TAD_API tad_status tad_eval(tad_problem* p, const double* x_h, double* f);
+TAD_API tad_status tad_eval_with_gradient(tad_problem* p, const double* x_h,
+                                          double* f, double* g_h);
+TAD_API tad_status tad_eval_with_derivatives(tad_problem* p, const double* x_h,
+                                             double* f, double* g_h, double* H_values_h);
+TAD_API tad_status tad_eval_with_hessian_proj(tad_problem* p, const double* x_h,
+                                              double proj_eps, double* f,
+                                              double* g_h, double* H_values_h);
+/* Device-pointer variants (zero copy). */
+TAD_API tad_status tad_eval_d(tad_problem* p, const double* x_d, double* f);
+TAD_API tad_status tad_eval_with_hessian_proj_d(tad_problem* p, const double* x_d,
+                                                double proj_eps, double* f,
+                                                double* g_d, double* H_values_d);
+
+/* d = -(H + w I)^-1 g with H the PSD-projected Hessian at x (block-Jacobi PCG
+   on the device).  Returns TAD_ERR_PCG_NOCONV if the tolerance is not met
+   (d then holds the last iterate). */
+TAD_API tad_status tad_newton_direction(tad_problem* p, const double* x_h,
+                                        double proj_eps, double w_identity,
+                                        double* d_h, double* f, double* g_h);
+
+/* Armijo backtracking from x along d: s = s_max, s *= shrink, at most
+   max_iters trials; x_out = x + s d for the first s meeting
+   f(x+sd) <= f + c s d.g, else x_out = x and TAD_ERR_LS_FAIL. */
+TAD_API tad_status tad_line_search(tad_problem* p, const double* x_h,
+                                   const double* d_h, double f, const double* g_h,
+                                   double s_max, double* x_out_h, double* f_out);
+
+/* Run n_iters Projected-Newton iterations in place on x_h (host):
+   eval_with_hessian_proj -> PCG -> Armijo line search, all on the device.
+   f_hist_h (optional, n_iters+1): energy before each iteration and at the end.
+   Stops early when the Newton decrement -d.g/2 < stop_decrement (if > 0). */
+TAD_API tad_status tad_newton_solve(tad_problem* p, double* x_h, int n_iters,
+                                    double proj_eps, double stop_decrement,
+                                    double* f_hist_h, int* iters_done);
+/* The same on a device-resident x (no host copies). */
+TAD_API tad_status tad_newton_solve_d(tad_problem* p, double* x_d, int n_iters,
+                                      double proj_eps, double stop_decrement,
+                                      double* f_hist_h, int* iters_done);
+
+/* The CUDA stream (cudaStream_t) all work of the problem is issued on. */
+TAD_API tad_status tad_get_stream(tad_problem* p, void** stream);
+
+/* Per-stage timing of the last tad_newton_solve[_d] call (milliseconds,
+   CUDA events): [eval+project, assemble, pcg, line search], plus PCG
+   iteration total.  Any pointer may be NULL. */
+TAD_API tad_status tad_last_solve_stats(tad_problem* p, double* ms_stages4,
+                                        int64_t* pcg_iters_total,
+                                        int64_t* ls_trials_total);
+
+/* Diagnostics: apply one operator of the device scalar tad::Scalar<1>
+   (precision TAD_PREC_FP64: Double<1>; TAD_PREC_MIXED: Mixed<1>) to
+   a = (val, grad, hess) and b, writing (val, grad, hess).  Op codes:
+   0 -a, 1 sqrt, 2 sqr, 3 pow(a, int b.val), 4 pow(a, b.val), 5 exp, 6 log,
+   7 sin, 8 cos, 9 tan, 10 asin, 11 acos, 12 atan, 13 sinh, 14 cosh, 15 tanh,
+   16 fabs, 17 a+b, 18 a-b, 19 a*b, 20 a/b, 21 atan2(a,b), 22 hypot(a,b),
+   23 b.val/a, 24 log2, 25 log10, 26 asinh, 27 acosh, 28 atanh, 29 a+b.val,
+   30 a*b.val, 31 b.val-a, 32 a/b.val.  Replaces the operator known-answer
+   tests of tests/ScalarTestUnaryOperators.cc / ScalarTestBinaryOperators.cc. */
+TAD_API tad_status tad_debug_scalar_op(int op, int precision, const double* a3,
+                                       const double* b3, double* out3);
+
+/* Measured CUDA-core FMA throughput of the current device in TFLOP/s
+   (precision TAD_PREC_FP64: double, TAD_PREC_MIXED: float); the roofline
+   denominator of the element kernels. */
+TAD_API tad_status tad_measure_fma_peak(int precision, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TAD_H */

@@ -1,0 +1,153 @@
+/*
+ * tad/Element.cuh -- what an element functor receives: `element.handle` and
+ * `element.variables(vh)` (include/TinyAD/Detail/Element.hh:93-144).
+ *
+ * The reference builds each element's local index map on every call, in
+ * first-access order with de-duplication (Element.hh:208-260).  Here the map
+ * is recorded once, when the sparsity pattern is built (RecordElement), and
+ * every later evaluation looks the handle up in the element's recorded list
+ * of at most N handles held in registers: the local index of handle vh is
+ * d * (its position in that list) + i, exactly the reference's order.
+ *
+ * Element kinds:
+ *   ActiveElement<d, N, S>   seeds tad::Scalar variables (gradient/Hessian)
+ *   PassiveElement<d, N, T>  returns plain values (energy only)
+ *   LineSearchElement<d, N>  returns x + s * dir (passive, line search)
+ *   RecordElement<d, N>      records the first-access order
+ */
+#pragma once
+#include <stdint.h>
+#include "Mat.cuh"
+
+namespace tad {
+
+/* device error word bits */
+enum : int32_t {
+    DEVERR_UNRECORDED_ACCESS = 1,   /* handle not in the recorded access list */
+    DEVERR_TOO_MANY_VARS = 2,       /* more distinct handles than the valence */
+    DEVERR_NONFINITE = 4,           /* non-finite gradient/Hessian entry */
+    DEVERR_TIMEOUT = 8              /* bounded wait gave up */
+};
+
+#if defined(__CUDACC__)
+__device__ __forceinline__ void report_error(int32_t* err, int32_t bit)
+{
+    if (err) atomicOr(err, bit);
+}
+#endif
+
+template <int d, int N, typename S>
+struct ActiveElement
+{
+    using scalar_type = S;
+    using passive_type = typename S::passive_type;
+    static constexpr bool active_mode = true;
+    int64_t handle;
+    int32_t vh[N];
+    const double* x;
+    int32_t* err;
+
+    TAD_HD int slot_of(int v) const
+    {
+        int slot = -1;
+#pragma unroll
+        for (int i = N - 1; i >= 0; --i)
+            if (vh[i] == v) slot = i;
+        return slot;
+    }
+
+#if defined(__CUDACC__)
+    __device__ Vec<S, d> variables(int v) const
+    {
+        int slot = slot_of(v);
+        if (slot < 0) { report_error(err, DEVERR_UNRECORDED_ACCESS); slot = 0; }
+        Vec<S, d> r;
+#pragma unroll
+        for (int i = 0; i < d; ++i) r[i] = S((passive_type)x[(int64_t)d * v + i], slot * d + i);
+        return r;
+    }
+    __device__ S variable(int v) const
+    {
+        static_assert(d == 1, "element.variable(vh) needs variable dimension 1; use element.variables(vh)");
+        return variables(v)[0];
+    }
+#endif
+};
+
+template <int d, int N, typename T>
+struct PassiveElement
+{
+    using scalar_type = T;
+    using passive_type = T;
+    static constexpr bool active_mode = false;
+    int64_t handle;
+    const double* x;
+
+    TAD_HD Vec<T, d> variables(int v) const
+    {
+        Vec<T, d> r;
+#pragma unroll
+        for (int i = 0; i < d; ++i) r[i] = (T)x[(int64_t)d * v + i];
+        return r;
+    }
+    TAD_HD T variable(int v) const { return variables(v)[0]; }
+};
+
+template <int d, int N>
+struct LineSearchElement
+{
+    using scalar_type = double;
+    using passive_type = double;
+    static constexpr bool active_mode = false;
+    int64_t handle;
+    const double* x;
+    const double* dir;
+    double s;
+
+    TAD_HD Vec<double, d> variables(int v) const
+    {
+        Vec<double, d> r;
+#pragma unroll
+        for (int i = 0; i < d; ++i) r[i] = x[(int64_t)d * v + i] + s * dir[(int64_t)d * v + i];
+        return r;
+    }
+    TAD_HD double variable(int v) const { return variables(v)[0]; }
+};
+
+template <int d, int N>
+struct RecordElement
+{
+    using scalar_type = double;
+    using passive_type = double;
+    static constexpr bool active_mode = false;
+    int64_t handle;
+    const double* x;
+    int32_t vh[N];
+    int n = 0;
+    bool overflow = false;
+
+    TAD_HD Vec<double, d> variables(int v)
+    {
+        bool seen = false;
+#pragma unroll
+        for (int i = 0; i < N; ++i)
+            if (i < n && vh[i] == v) seen = true;
+        if (!seen)
+        {
+            if (n < N) vh[n++] = v;
+            else overflow = true;
+        }
+        Vec<double, d> r;
+#pragma unroll
+        for (int i = 0; i < d; ++i) r[i] = x[(int64_t)d * v + i];
+        return r;
+    }
+    TAD_HD double variable(int v) { return variables(v)[0]; }
+};
+
+/* TINYAD_SCALAR_TYPE(element) of the reference (Element.hh:300-331) */
+#define TAD_SCALAR_TYPE(element) typename std::decay_t<decltype(element)>::scalar_type
+#define TAD_PASSIVE_TYPE(element) typename std::decay_t<decltype(element)>::passive_type
+#define TAD_ACTIVE_MODE(element) (std::decay_t<decltype(element)>::active_mode)
+
+} // namespace tad

@@ -1,0 +1,195 @@
+/*
+ * tad/ElementKernels.cuh -- element evaluation kernels, templated on the
+ * variable dimension d, the valence N and the element functor.  Included by
+ * the library for its built-in energies and by the C++ front end for user
+ * functors, so both run the same code.
+ *
+ * One element per thread.  The functor runs with an element whose
+ * variables() seed tad::Scalar<k> values (k = d*N) held in registers; the
+ * result (value, gradient, packed Hessian) is optionally PSD-projected in the
+ * same thread (project_positive_definite, tad/Projection.cuh) and written as
+ *   f:  double  out_f[e]
+ *   g:  Tg      out_g[e][N*d]                         (slot-major)
+ *   H:  Th      out_H[e][N(N+1)/2 slot pairs a<=b][d][d]
+ * which the assembly kernels gather per global block in element order.  This
+ * replaces the per-element std::vector results and the serial triplet
+ * scatter of ScalarObjectiveTerm::eval_with_derivatives_add
+ * (include/TinyAD/Detail/ScalarObjectiveTerm.hh:224-278).
+ */
+#pragma once
+#include <stdint.h>
+#include "Scalar.cuh"
+#include "Element.cuh"
+#include "Projection.cuh"
+#include "../tad.h"
+
+namespace tad {
+
+template <typename T> __device__ __forceinline__ bool finite_val(T v) { return ::isfinite(v); }
+
+struct ElemLaunch
+{
+    int64_t n_elem;
+    const int32_t* rec;      /* recorded access order, n_elem * N, -1 = unused */
+    const double* x;
+    const double* dir;
+    const double* steps;     /* device, n_steps */
+    int n_steps;
+    int64_t f_stride;        /* line search: row stride of out_f */
+    double eps;
+    int project;
+    double* out_f;
+    void* out_g;
+    void* out_H;
+    int32_t* record;         /* record mode output */
+    int32_t* err;
+};
+
+template <int d, int N, typename Energy>
+__global__ void __launch_bounds__(128) k_elem_value(ElemLaunch L, Energy energy)
+{
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= L.n_elem) return;
+    PassiveElement<d, N, double> el{e, L.x};
+    L.out_f[e] = (double)energy(el);
+}
+
+/* f at x + s_j dir for the n_steps trial step sizes */
+template <int d, int N, typename Energy>
+__global__ void __launch_bounds__(128) k_elem_linesearch(ElemLaunch L, Energy energy)
+{
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= L.n_elem) return;
+    for (int j = 0; j < L.n_steps; ++j)
+    {
+        LineSearchElement<d, N> el{e, L.x, L.dir, L.steps[j]};
+        L.out_f[(int64_t)j * L.f_stride + e] = (double)energy(el);
+    }
+}
+
+template <int d, int N, typename Energy>
+__global__ void __launch_bounds__(128) k_elem_record(ElemLaunch L, Energy energy)
+{
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= L.n_elem) return;
+    RecordElement<d, N> el;
+    el.handle = e;
+    el.x = L.x;
+#pragma unroll
+    for (int i = 0; i < N; ++i) el.vh[i] = -1;
+    (void)energy(el);
+    if (el.overflow) report_error(L.err, DEVERR_TOO_MANY_VARS);
+#pragma unroll
+    for (int i = 0; i < N; ++i) L.record[e * N + i] = (i < el.n) ? el.vh[i] : -1;
+}
+
+template <int d, int N, typename Energy>
+__global__ void __launch_bounds__(128) k_elem_gradient(ElemLaunch L, Energy energy)
+{
+    constexpr int k = d * N;
+    using S = Scalar<k, double, false>;
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= L.n_elem) return;
+    ActiveElement<d, N, S> el;
+    el.handle = e;
+    el.x = L.x;
+    el.err = L.err;
+#pragma unroll
+    for (int i = 0; i < N; ++i) el.vh[i] = L.rec[e * N + i];
+    const S r = energy(el);
+    L.out_f[e] = r.val;
+    double* g = (double*)L.out_g + e * k;
+    bool fin = true;
+#pragma unroll
+    for (int i = 0; i < k; ++i) { g[i] = r.grad[i]; fin = fin && finite_val(r.grad[i]); }
+    if (!fin) report_error(L.err, DEVERR_NONFINITE);
+}
+
+/* second-order evaluation with the Hessian in T: double (plain Double<k>), or
+   float with FP64 value and gradient (mixed, tad::Mixed<k>). */
+template <int d, int N, typename T, typename Energy>
+__global__ void __launch_bounds__(128) k_elem_hessian(ElemLaunch L, Energy energy)
+{
+    constexpr int k = d * N;
+    constexpr int NP = N * (N + 1) / 2;
+    using S = Scalar<k, T, true, double, double>;
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= L.n_elem) return;
+    ActiveElement<d, N, S> el;
+    el.handle = e;
+    el.x = L.x;
+    el.err = L.err;
+#pragma unroll
+    for (int i = 0; i < N; ++i) el.vh[i] = L.rec[e * N + i];
+    S r = energy(el);
+    if (L.project) project_positive_definite<k, T>(r.hess, (T)L.eps);
+    L.out_f[e] = (double)r.val;
+    bool fin = true;
+    double* g = (double*)L.out_g + e * k;
+#pragma unroll
+    for (int i = 0; i < k; ++i) { g[i] = (double)r.grad[i]; fin = fin && finite_val(r.grad[i]); }
+    T* Hb = (T*)L.out_H + e * (NP * d * d);
+#pragma unroll
+    for (int a = 0; a < N; ++a)
+#pragma unroll
+        for (int b = a; b < N; ++b)
+        {
+            const int pr = packed_index(a, b, N);
+#pragma unroll
+            for (int p = 0; p < d; ++p)
+#pragma unroll
+                for (int q = 0; q < d; ++q)
+                {
+                    const int i = a * d + p, j = b * d + q;
+                    const T v = (i <= j) ? r.hess[packed_index(i, j, k)] : r.hess[packed_index(j, i, k)];
+                    fin = fin && finite_val(v);
+                    Hb[pr * d * d + p * d + q] = v;
+                }
+        }
+    if (!fin) report_error(L.err, DEVERR_NONFINITE);
+}
+
+inline unsigned elem_grid(int64_t n) { return (unsigned)((n + 127) / 128); }
+
+/* ElemLaunch from the C-ABI callback arguments */
+inline ElemLaunch make_launch(const tad_term_eval_args& a)
+{
+    ElemLaunch L{};
+    L.n_elem = a.n_elem;
+    L.rec = a.handles_d;
+    L.x = a.x_d;
+    L.dir = a.dir_d;
+    L.steps = a.steps_d;
+    L.n_steps = a.n_steps;
+    L.f_stride = a.f_row_stride;
+    L.eps = a.proj_eps;
+    L.project = a.mode == 3;
+    L.out_f = (double*)a.out_f_d;
+    L.out_g = a.out_g_d;
+    L.out_H = a.out_H_d;
+    L.record = a.record_d;
+    L.err = a.error_d;
+    return L;
+}
+
+/* Launch the kernel for `mode` (tad_eval_mode values) on stream s. */
+template <int d, int N, typename Energy>
+inline void launch_elements(int mode, int precision, const ElemLaunch& L, const Energy& energy, cudaStream_t s)
+{
+    if (L.n_elem <= 0) return;
+    const unsigned g = elem_grid(L.n_elem);
+    switch (mode)
+    {
+    case 0: k_elem_value<d, N, Energy><<<g, 128, 0, s>>>(L, energy); break;
+    case 1: k_elem_gradient<d, N, Energy><<<g, 128, 0, s>>>(L, energy); break;
+    case 2:
+    case 3:
+        if (precision == 1) k_elem_hessian<d, N, float, Energy><<<g, 128, 0, s>>>(L, energy);
+        else k_elem_hessian<d, N, double, Energy><<<g, 128, 0, s>>>(L, energy);
+        break;
+    case 4: k_elem_linesearch<d, N, Energy><<<g, 128, 0, s>>>(L, energy); break;
+    case 5: k_elem_record<d, N, Energy><<<g, 128, 0, s>>>(L, energy); break;
+    }
+}
+
+} // namespace tad

@@ -1,0 +1,152 @@
+/*
+ * tad/Energies.cuh -- the library's built-in element functors (tad_energy in
+ * tad.h).  They are ordinary element functors, written like the reference's
+ * test lambdas, and run through the same kernels as user functors.
+ *
+ *   SymmetricDirichletTri  tests/NewtonTest.cc:28-44 (weight per element)
+ *   SymmetricDirichletTet  its 3D analogue (k = 12)
+ *   PositionPenalty        tests/NewtonTest.cc:48-55 (weight per element)
+ *   Quadratic              the quadratics of tests/ScalarFunctionTest.cc
+ *   DirichletTri           the Laplacian energy of tests/DynamicElementsTest.cc:60-91
+ *
+ * Each functor reads its element's vertex handles (`vtx`, n_elem x N) and
+ * parameters (`prm`, n_elem x P) through element.handle, the way the
+ * reference lambdas read F(element.handle, i).
+ */
+#pragma once
+#include <math.h>
+#include <stdint.h>
+#include "Mat.cuh"
+#include "Element.cuh"
+
+namespace tad {
+
+struct SymmetricDirichletTri
+{
+    static constexpr int d = 2, N = 3, n_params = 5;
+    const int32_t* vtx;
+    const double* prm;
+
+    template <typename El>
+    TAD_HD auto operator()(El& element) const -> TAD_SCALAR_TYPE(element)
+    {
+        using T = TAD_SCALAR_TYPE(element);
+        using P = TAD_PASSIVE_TYPE(element);
+        const int64_t e = element.handle;
+        const double* p = prm + e * n_params;
+        Mat<P, 2, 2> Mr;
+        Mr.m[0] = P(p[0]); Mr.m[1] = P(p[1]); Mr.m[2] = P(p[2]); Mr.m[3] = P(p[3]);
+        const Vec<T, 2> a = element.variables(vtx[e * 3 + 0]);
+        const Vec<T, 2> b = element.variables(vtx[e * 3 + 1]);
+        const Vec<T, 2> c = element.variables(vtx[e * 3 + 2]);
+        const Mat<T, 2, 2> M = col_mat(b - a, c - a);
+        if (determinant(M) <= 0.0) return T(INFINITY);
+        return ((M * inverse(Mr)).squaredNorm() + (Mr * inverse(M)).squaredNorm()) * P(p[4]);
+    }
+};
+
+struct SymmetricDirichletTet
+{
+    static constexpr int d = 3, N = 4, n_params = 10;
+    const int32_t* vtx;
+    const double* prm;
+
+    template <typename El>
+    TAD_HD auto operator()(El& element) const -> TAD_SCALAR_TYPE(element)
+    {
+        using T = TAD_SCALAR_TYPE(element);
+        using P = TAD_PASSIVE_TYPE(element);
+        const int64_t e = element.handle;
+        const double* p = prm + e * n_params;
+        Mat<P, 3, 3> Mr;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Mr.m[i] = P(p[i]);
+        const Vec<T, 3> a = element.variables(vtx[e * 4 + 0]);
+        const Vec<T, 3> b = element.variables(vtx[e * 4 + 1]);
+        const Vec<T, 3> c = element.variables(vtx[e * 4 + 2]);
+        const Vec<T, 3> dd = element.variables(vtx[e * 4 + 3]);
+        const Mat<T, 3, 3> M = col_mat(b - a, c - a, dd - a);
+        if (determinant(M) <= 0.0) return T(INFINITY);
+        return ((M * inverse(Mr)).squaredNorm() + (Mr * inverse(M)).squaredNorm()) * P(p[9]);
+    }
+};
+
+template <int D>
+struct PositionPenalty
+{
+    static constexpr int d = D, N = 1, n_params = D + 1;
+    const int32_t* vtx;
+    const double* prm;
+
+    template <typename El>
+    TAD_HD auto operator()(El& element) const -> TAD_SCALAR_TYPE(element)
+    {
+        using T = TAD_SCALAR_TYPE(element);
+        using P = TAD_PASSIVE_TYPE(element);
+        const int64_t e = element.handle;
+        const double* p = prm + e * n_params;
+        Vec<P, D> target;
+#pragma unroll
+        for (int i = 0; i < D; ++i) target[i] = P(p[i]);
+        const Vec<T, D> x = element.variables(vtx[e]);
+        return (target - x).squaredNorm() * P(p[D]);
+    }
+};
+
+/* E = sum_ij A_ij x_i x_j + sum_i b_i x_i + c over the element's variables */
+template <int D, int NV>
+struct Quadratic
+{
+    static constexpr int d = D, N = NV, k = D * NV, n_params = D * NV * D * NV + D * NV + 1;
+    const int32_t* vtx;
+    const double* prm;
+
+    template <typename El>
+    TAD_HD auto operator()(El& element) const -> TAD_SCALAR_TYPE(element)
+    {
+        using T = TAD_SCALAR_TYPE(element);
+        using P = TAD_PASSIVE_TYPE(element);
+        const int64_t e = element.handle;
+        const double* p = prm + e * n_params;
+        T xs[k];
+#pragma unroll
+        for (int n = 0; n < NV; ++n)
+        {
+            const Vec<T, D> v = element.variables(vtx[e * NV + n]);
+#pragma unroll
+            for (int i = 0; i < D; ++i) xs[n * D + i] = v[i];
+        }
+        T acc = T(P(p[k * k + k]));
+#pragma unroll
+        for (int i = 0; i < k; ++i)
+#pragma unroll
+            for (int j = 0; j < k; ++j)
+                if (p[i * k + j] != 0.0) acc = acc + P(p[i * k + j]) * xs[i] * xs[j];
+#pragma unroll
+        for (int i = 0; i < k; ++i)
+            if (p[k * k + i] != 0.0) acc = acc + P(p[k * k + i]) * xs[i];
+        return acc;
+    }
+};
+
+template <int D>
+struct DirichletTri
+{
+    static constexpr int d = D, N = 3, n_params = 1;
+    const int32_t* vtx;
+    const double* prm;
+
+    template <typename El>
+    TAD_HD auto operator()(El& element) const -> TAD_SCALAR_TYPE(element)
+    {
+        using T = TAD_SCALAR_TYPE(element);
+        using P = TAD_PASSIVE_TYPE(element);
+        const int64_t e = element.handle;
+        const Vec<T, D> a = element.variables(vtx[e * 3 + 0]);
+        const Vec<T, D> b = element.variables(vtx[e * 3 + 1]);
+        const Vec<T, D> c = element.variables(vtx[e * 3 + 2]);
+        return ((b - a).squaredNorm() + (c - b).squaredNorm() + (a - c).squaredNorm()) * P(prm[e]);
+    }
+};
+
+} // namespace tad

@@ -1,0 +1,617 @@
+/*
+ * tad/Scalar.cuh -- forward-mode second-order scalar for device code.
+ *
+ * Same semantics as TinyAD's Scalar<k, PassiveT, with_hessian>
+ * (include/TinyAD/Scalar.hh:24-1347): a value, a dense k-gradient and a k x k
+ * Hessian propagated through every operation by the chain rule; comparisons
+ * look at the value only.  `Double<k>` / `Float<k>` are the aliases of
+ * Scalar.hh:1389-1391.
+ *
+ * GB300 layout: the Hessian is symmetric, so only its upper triangle is
+ * stored, packed row-major (k(k+1)/2 entries: 21 for k = 6, 78 for k = 12).
+ * Every loop runs over compile-time k and unrolls, so a Scalar lives in
+ * registers and each operation costs half the FMAs of the dense form.  The
+ * optional `HR0, HC0` block restriction of the reference (a rectangular
+ * Hessian block, used for mixed second derivatives, Scalar.hh:24, :186-196)
+ * is provided by MixedScalar below.
+ *
+ * Precision split: Scalar<k, T, with_hessian, V, G> keeps the value in V,
+ * the gradient in G and the Hessian in T.  Mixed<k> = Scalar<k, float, true,
+ * double, double> is the mixed-precision scalar: values (edge vectors,
+ * Jacobian determinants and inverses, the energy) and the O(k) gradient are
+ * FP64, the O(k^2) Hessian arithmetic is FP32.  An FP64 gradient keeps the
+ * Newton fixed point, and the gradient's components along (near-)null
+ * directions of the Hessian such as rigid motions, at FP64 accuracy.  With
+ * V = G = T it is the reference's plain scalar.
+ *
+ * All functions are __host__ __device__ so element functors can be written
+ * once and run on either side.
+ */
+#pragma once
+
+#include <cmath>
+#include <type_traits>
+
+#if defined(__CUDACC__)
+#define TAD_HD __host__ __device__ __forceinline__
+#else
+#define TAD_HD inline
+#endif
+
+namespace tad {
+
+/* index of (i, j), i <= j, in the packed upper triangle of a k x k matrix */
+TAD_HD constexpr int packed_index(int i, int j, int k) { return i * k - (i * (i - 1)) / 2 + (j - i); }
+
+template <int K, typename T, bool WithHessian = true, typename V = T, typename G = V>
+struct Scalar
+{
+    static constexpr int k = K;
+    static constexpr bool with_hessian = WithHessian;
+    static constexpr int n_hess = WithHessian ? K * (K + 1) / 2 : 0;
+    using passive_type = V;
+    using grad_type = G;
+    using deriv_type = T;
+
+    V val;
+    G grad[K];
+    T hess[n_hess > 0 ? n_hess : 1];
+
+    TAD_HD Scalar() : val(V(0))
+    {
+#pragma unroll
+        for (int i = 0; i < K; ++i) grad[i] = G(0);
+#pragma unroll
+        for (int i = 0; i < (n_hess > 0 ? n_hess : 1); ++i) hess[i] = T(0);
+    }
+
+    /* passive constant (Scalar.hh:58-63) */
+    TAD_HD Scalar(V v) : Scalar() { val = v; }
+    template <typename U, typename = std::enable_if_t<std::is_arithmetic<U>::value && !std::is_same<U, V>::value>>
+    TAD_HD Scalar(U v) : Scalar() { val = V(v); }
+
+    /* active variable with index idx (Scalar.hh:67-75) */
+    TAD_HD Scalar(V v, int idx) : Scalar()
+    {
+        val = v;
+#pragma unroll
+        for (int i = 0; i < K; ++i) grad[i] = (i == idx) ? G(1) : G(0);
+    }
+
+    /* univariate known derivatives (Scalar.hh:89-101) */
+    TAD_HD static Scalar known_derivatives(V v, G g, T h)
+    {
+        Scalar r(v);
+        r.grad[0] = g;
+        if (WithHessian) r.hess[0] = h;
+        return r;
+    }
+
+    /* full-matrix read access to the Hessian */
+    TAD_HD T H(int i, int j) const { return i <= j ? hess[packed_index(i, j, K)] : hess[packed_index(j, i, K)]; }
+
+    /* the gradient in the Hessian's precision */
+    TAD_HD void grad_as_hess_type(T (&t)[K]) const
+    {
+#pragma unroll
+        for (int i = 0; i < K; ++i) t[i] = T(grad[i]);
+    }
+
+    /* chain rule for f(a) with f, f', f'' known (Scalar.hh:199-214):
+       grad = f' ga, Hess = f'' ga ga^T + f' Ha */
+    TAD_HD static Scalar chain(V f, V f1v, V f2v, const Scalar& a)
+    {
+        Scalar r;
+        r.val = f;
+        const G f1g = G(f1v);
+#pragma unroll
+        for (int i = 0; i < K; ++i) r.grad[i] = f1g * a.grad[i];
+        if (WithHessian)
+        {
+            const T f1 = T(f1v), f2 = T(f2v);
+            T ta[K];
+            a.grad_as_hess_type(ta);
+            int q = 0;
+#pragma unroll
+            for (int i = 0; i < K; ++i)
+            {
+                const T fgi = f2 * ta[i];
+#pragma unroll
+                for (int j = i; j < K; ++j, ++q) r.hess[q] = fgi * ta[j] + f1 * a.hess[q];
+            }
+        }
+        return r;
+    }
+};
+
+template <int K, bool WithHessian = true> using Double = Scalar<K, double, WithHessian>;
+template <int K, bool WithHessian = true> using Float = Scalar<K, float, WithHessian>;
+/* mixed precision: FP64 value and gradient, FP32 Hessian */
+template <int K, bool WithHessian = true> using Mixed = Scalar<K, float, WithHessian, double, double>;
+
+template <typename S> struct is_scalar : std::false_type {};
+template <int K, typename T, bool H, typename V, typename G> struct is_scalar<Scalar<K, T, H, V, G>> : std::true_type {};
+
+/* ---- passive helpers: to_passive / value_of ---------------------------- */
+template <typename T, typename = std::enable_if_t<std::is_arithmetic<T>::value>>
+TAD_HD T to_passive(T v) { return v; }
+template <int K, typename T, bool H, typename V, typename G>
+TAD_HD V to_passive(const Scalar<K, T, H, V, G>& a) { return a.val; }
+
+#define TAD_S Scalar<K, T, H, V, G>
+#define TAD_TPL template <int K, typename T, bool H, typename V, typename G>
+#define TAD_TPLU template <int K, typename T, bool H, typename V, typename G, typename U, typename = std::enable_if_t<std::is_arithmetic<U>::value>>
+
+/* ---- unary -------------------------------------------------------------- */
+TAD_TPL TAD_HD TAD_S operator-(const TAD_S& a)                              // Scalar.hh:220-234
+{
+    TAD_S r;
+    r.val = -a.val;
+#pragma unroll
+    for (int i = 0; i < K; ++i) r.grad[i] = -a.grad[i];
+#pragma unroll
+    for (int i = 0; i < TAD_S::n_hess; ++i) r.hess[i] = -a.hess[i];
+    return r;
+}
+TAD_TPL TAD_HD TAD_S operator+(const TAD_S& a) { return a; }
+
+TAD_TPL TAD_HD TAD_S sqrt(const TAD_S& a)                                    // Scalar.hh:236-247
+{
+    using std::sqrt;
+    const V f = sqrt(a.val);
+    return TAD_S::chain(f, V(0.5) / f, V(-0.25) / (f * a.val), a);
+}
+
+TAD_TPL TAD_HD TAD_S sqr(const TAD_S& a)                                     // Scalar.hh:249-264
+{
+    TAD_S r;
+    r.val = a.val * a.val;
+    const G two_vg = G(V(2) * a.val);
+#pragma unroll
+    for (int i = 0; i < K; ++i) r.grad[i] = two_vg * a.grad[i];
+    if (H)
+    {
+        const T two_v = T(V(2) * a.val);
+        T ta[K];
+        a.grad_as_hess_type(ta);
+        int q = 0;
+#pragma unroll
+        for (int i = 0; i < K; ++i)
+        {
+            const T gi2 = T(2) * ta[i];
+#pragma unroll
+            for (int j = i; j < K; ++j, ++q) r.hess[q] = two_v * a.hess[q] + gi2 * ta[j];
+        }
+    }
+    return r;
+}
+
+TAD_TPL TAD_HD TAD_S pow(const TAD_S& a, int e)                              // Scalar.hh:266-289
+{
+    using std::pow;
+    if (e == 0) return TAD_S::chain(V(1), V(0), V(0), a);
+    if (e == 1) return TAD_S::chain(a.val, V(1), V(0), a);
+    const V f2 = (V)pow(a.val, e - 2);
+    const V f1 = f2 * a.val;
+    return TAD_S::chain(f1 * a.val, V(e) * f1, V(e * (e - 1)) * f2, a);
+}
+
+template <int K, typename T, bool H, typename V, typename G, typename U, typename = std::enable_if_t<std::is_floating_point<U>::value>>
+TAD_HD TAD_S pow(const TAD_S& a, U eu)                                       // Scalar.hh:291-307
+{
+    using std::pow;
+    const V e = V(eu);
+    const V f2 = pow(a.val, e - V(2));
+    const V f1 = f2 * a.val;
+    return TAD_S::chain(f1 * a.val, e * f1, e * (e - V(1)) * f2, a);
+}
+
+TAD_TPL TAD_HD TAD_S exp(const TAD_S& a) { using std::exp; const V e = exp(a.val); return TAD_S::chain(e, e, e, a); }   // Scalar.hh:324-332
+TAD_TPL TAD_HD TAD_S log(const TAD_S& a)                                                                               // Scalar.hh:334-346
+{
+    using std::log;
+    const V ai = V(1) / a.val;
+    return TAD_S::chain(log(a.val), ai, -ai * ai, a);
+}
+TAD_TPL TAD_HD TAD_S log2(const TAD_S& a)                                   // Scalar.hh:348-358
+{
+    using std::log; using std::log2;
+    const V ai = V(1) / (a.val * V(log(2.0)));
+    return TAD_S::chain(log2(a.val), ai, -ai / a.val, a);
+}
+TAD_TPL TAD_HD TAD_S log10(const TAD_S& a)                                  // Scalar.hh:360-370
+{
+    using std::log; using std::log10;
+    const V ai = V(1) / (a.val * V(log(10.0)));
+    return TAD_S::chain(log10(a.val), ai, -ai / a.val, a);
+}
+TAD_TPL TAD_HD TAD_S sin(const TAD_S& a) { using std::sin; using std::cos; const V s = sin(a.val); return TAD_S::chain(s, cos(a.val), -s, a); }
+TAD_TPL TAD_HD TAD_S cos(const TAD_S& a) { using std::sin; using std::cos; const V c = cos(a.val); return TAD_S::chain(c, -sin(a.val), -c, a); }
+TAD_TPL TAD_HD TAD_S tan(const TAD_S& a)
+{
+    using std::tan; using std::cos; using std::sin;
+    const V c = cos(a.val);
+    const V c2 = c * c;
+    return TAD_S::chain(tan(a.val), V(1) / c2, V(2) * sin(a.val) / (c2 * c), a);
+}
+TAD_TPL TAD_HD TAD_S asin(const TAD_S& a)
+{
+    using std::asin; using std::sqrt;
+    const V s = V(1) - a.val * a.val;
+    const V ss = sqrt(s);
+    return TAD_S::chain(asin(a.val), V(1) / ss, a.val / (ss * s), a);
+}
+TAD_TPL TAD_HD TAD_S acos(const TAD_S& a)
+{
+    using std::acos; using std::sqrt;
+    const V s = V(1) - a.val * a.val;
+    const V ss = sqrt(s);
+    return TAD_S::chain(acos(a.val), V(-1) / ss, -a.val / (ss * s), a);
+}
+TAD_TPL TAD_HD TAD_S atan(const TAD_S& a)
+{
+    using std::atan;
+    const V s = a.val * a.val + V(1);
+    return TAD_S::chain(atan(a.val), V(1) / s, V(-2) * a.val / (s * s), a);
+}
+TAD_TPL TAD_HD TAD_S sinh(const TAD_S& a) { using std::sinh; using std::cosh; const V s = sinh(a.val); return TAD_S::chain(s, cosh(a.val), s, a); }
+TAD_TPL TAD_HD TAD_S cosh(const TAD_S& a) { using std::sinh; using std::cosh; const V c = cosh(a.val); return TAD_S::chain(c, sinh(a.val), c, a); }
+TAD_TPL TAD_HD TAD_S tanh(const TAD_S& a)
+{
+    using std::tanh; using std::cosh; using std::sinh;
+    const V c = cosh(a.val);
+    const V c2 = c * c;
+    return TAD_S::chain(tanh(a.val), V(1) / c2, V(-2) * sinh(a.val) / (c2 * c), a);
+}
+TAD_TPL TAD_HD TAD_S asinh(const TAD_S& a)                                  // Scalar.hh:501-515
+{
+    using std::asinh; using std::sqrt;
+    const V s = a.val * a.val + V(1);
+    const V ss = sqrt(s);
+    return TAD_S::chain(asinh(a.val), V(1) / ss, -a.val / (ss * s), a);
+}
+TAD_TPL TAD_HD TAD_S acosh(const TAD_S& a)                                  // Scalar.hh:517-534
+{
+    using std::acosh; using std::sqrt;
+    const V sm = a.val - V(1), sp = a.val + V(1);
+    const V prod = sqrt(sm) * sqrt(sp);
+    return TAD_S::chain(acosh(a.val), V(1) / prod, -a.val / (prod * sm * sp), a);
+}
+TAD_TPL TAD_HD TAD_S atanh(const TAD_S& a)                                  // Scalar.hh:536-546
+{
+    using std::atanh;
+    const V s = V(1) - a.val * a.val;
+    return TAD_S::chain(atanh(a.val), V(1) / s, V(2) * a.val / (s * s), a);
+}
+TAD_TPL TAD_HD TAD_S fabs(const TAD_S& a)                                   // Scalar.hh:309-322
+{
+    return a.val >= V(0) ? TAD_S::chain(a.val, V(1), V(0), a) : TAD_S::chain(-a.val, V(-1), V(0), a);
+}
+TAD_TPL TAD_HD TAD_S abs(const TAD_S& a) { return fabs(a); }
+
+TAD_TPL TAD_HD bool isnan(const TAD_S& a) { using std::isnan; return isnan(a.val); }
+TAD_TPL TAD_HD bool isinf(const TAD_S& a) { using std::isinf; return isinf(a.val); }
+TAD_TPL TAD_HD bool isfinite(const TAD_S& a) { using std::isfinite; return isfinite(a.val); }
+
+/* ---- binary: + - -------------------------------------------------------- */
+TAD_TPL TAD_HD TAD_S operator+(const TAD_S& a, const TAD_S& b)              // Scalar.hh:579-595
+{
+    TAD_S r;
+    r.val = a.val + b.val;
+#pragma unroll
+    for (int i = 0; i < K; ++i) r.grad[i] = a.grad[i] + b.grad[i];
+#pragma unroll
+    for (int i = 0; i < TAD_S::n_hess; ++i) r.hess[i] = a.hess[i] + b.hess[i];
+    return r;
+}
+TAD_TPL TAD_HD TAD_S operator-(const TAD_S& a, const TAD_S& b)              // Scalar.hh:651-667
+{
+    TAD_S r;
+    r.val = a.val - b.val;
+#pragma unroll
+    for (int i = 0; i < K; ++i) r.grad[i] = a.grad[i] - b.grad[i];
+#pragma unroll
+    for (int i = 0; i < TAD_S::n_hess; ++i) r.hess[i] = a.hess[i] - b.hess[i];
+    return r;
+}
+TAD_TPLU TAD_HD TAD_S operator+(const TAD_S& a, U b) { TAD_S r = a; r.val += V(b); return r; }   // Scalar.hh:597-621
+TAD_TPLU TAD_HD TAD_S operator+(U a, const TAD_S& b) { TAD_S r = b; r.val += V(a); return r; }
+TAD_TPLU TAD_HD TAD_S operator-(const TAD_S& a, U b) { TAD_S r = a; r.val -= V(b); return r; }   // Scalar.hh:669-698
+TAD_TPLU TAD_HD TAD_S operator-(U a, const TAD_S& b) { TAD_S r = -b; r.val += V(a); return r; }
+
+/* ---- binary: * ---------------------------------------------------------- */
+/* Hess(ab) = b Ha + ga gb^T + gb ga^T + a Hb (Scalar.hh:738-769) */
+TAD_TPL TAD_HD TAD_S operator*(const TAD_S& a, const TAD_S& b)
+{
+    TAD_S r;
+    r.val = a.val * b.val;
+    const G avg = G(a.val), bvg = G(b.val);
+#pragma unroll
+    for (int i = 0; i < K; ++i) r.grad[i] = bvg * a.grad[i] + avg * b.grad[i];
+    if (H)
+    {
+        const T av = T(a.val), bv = T(b.val);
+        T ta[K], tb[K];
+        a.grad_as_hess_type(ta);
+        b.grad_as_hess_type(tb);
+        int q = 0;
+#pragma unroll
+        for (int i = 0; i < K; ++i)
+#pragma unroll
+            for (int j = i; j < K; ++j, ++q)
+                r.hess[q] = bv * a.hess[q] + ta[i] * tb[j] + tb[i] * ta[j] + av * b.hess[q];
+    }
+    return r;
+}
+TAD_TPLU TAD_HD TAD_S operator*(const TAD_S& a, U b)                        // Scalar.hh:771-786
+{
+    TAD_S r;
+    r.val = a.val * V(b);
+    const G sg = G(b);
+#pragma unroll
+    for (int i = 0; i < K; ++i) r.grad[i] = a.grad[i] * sg;
+    const T s = T(b);
+#pragma unroll
+    for (int i = 0; i < TAD_S::n_hess; ++i) r.hess[i] = a.hess[i] * s;
+    return r;
+}
+TAD_TPLU TAD_HD TAD_S operator*(U a, const TAD_S& b) { return b * a; }
+
+/* ---- binary: / ---------------------------------------------------------- */
+/* r = a/b: grad = (ga - r gb)/b, Hess = (Ha - gr gb^T - gb gr^T - r Hb)/b
+   (Scalar.hh:823-840; the reciprocal of b is taken once) */
+TAD_TPL TAD_HD TAD_S operator/(const TAD_S& a, const TAD_S& b)
+{
+    TAD_S r;
+    const V ibv = V(1) / b.val;
+    r.val = a.val * ibv;
+    const G ibg = G(ibv), rvg = G(r.val);
+#pragma unroll
+    for (int i = 0; i < K; ++i) r.grad[i] = (a.grad[i] - rvg * b.grad[i]) * ibg;
+    if (H)
+    {
+        const T ib = T(ibv), rv = T(r.val);
+        T tr[K], tb[K];
+        r.grad_as_hess_type(tr);
+        b.grad_as_hess_type(tb);
+        int q = 0;
+#pragma unroll
+        for (int i = 0; i < K; ++i)
+#pragma unroll
+            for (int j = i; j < K; ++j, ++q)
+                r.hess[q] = (a.hess[q] - tr[i] * tb[j] - tb[i] * tr[j] - rv * b.hess[q]) * ib;
+    }
+    return r;
+}
+TAD_TPLU TAD_HD TAD_S operator/(const TAD_S& a, U b)                        // Scalar.hh:842-857
+{
+    TAD_S r;
+    const V ibv = V(1) / V(b);
+    r.val = a.val * ibv;
+    const G ibg = G(ibv);
+#pragma unroll
+    for (int i = 0; i < K; ++i) r.grad[i] = a.grad[i] * ibg;
+    const T ib = T(ibv);
+#pragma unroll
+    for (int i = 0; i < TAD_S::n_hess; ++i) r.hess[i] = a.hess[i] * ib;
+    return r;
+}
+/* passive / Scalar (Scalar.hh:859-877): r = c/b, gr = -r gb / b,
+   Hess = (-gr gb^T - gb gr^T - r Hb) / b */
+TAD_TPLU TAD_HD TAD_S operator/(U c, const TAD_S& b)
+{
+    TAD_S r;
+    const V ibv = V(1) / b.val;
+    r.val = V(c) * ibv;
+    const G sg = G(-r.val * ibv);
+#pragma unroll
+    for (int i = 0; i < K; ++i) r.grad[i] = sg * b.grad[i];
+    if (H)
+    {
+        const T ib = T(ibv), rv = T(r.val);
+        T tr[K], tb[K];
+        r.grad_as_hess_type(tr);
+        b.grad_as_hess_type(tb);
+        int q = 0;
+#pragma unroll
+        for (int i = 0; i < K; ++i)
+#pragma unroll
+            for (int j = i; j < K; ++j, ++q)
+                r.hess[q] = -(tr[i] * tb[j] + tb[i] * tr[j] + rv * b.hess[q]) * ib;
+    }
+    return r;
+}
+
+TAD_TPL TAD_HD TAD_S& operator+=(TAD_S& a, const TAD_S& b) { a = a + b; return a; }
+TAD_TPL TAD_HD TAD_S& operator-=(TAD_S& a, const TAD_S& b) { a = a - b; return a; }
+TAD_TPL TAD_HD TAD_S& operator*=(TAD_S& a, const TAD_S& b) { a = a * b; return a; }
+TAD_TPL TAD_HD TAD_S& operator/=(TAD_S& a, const TAD_S& b) { a = a / b; return a; }
+TAD_TPLU TAD_HD TAD_S& operator+=(TAD_S& a, U b) { a.val += V(b); return a; }
+TAD_TPLU TAD_HD TAD_S& operator-=(TAD_S& a, U b) { a.val -= V(b); return a; }
+TAD_TPLU TAD_HD TAD_S& operator*=(TAD_S& a, U b) { a = a * b; return a; }
+TAD_TPLU TAD_HD TAD_S& operator/=(TAD_S& a, U b) { a = a / b; return a; }
+
+/* atan2 (Scalar.hh:891-915).  The full Hessian is symmetric; only i <= j is
+   formed. */
+TAD_TPL TAD_HD TAD_S atan2(const TAD_S& y, const TAD_S& x)
+{
+    using std::atan2;
+    TAD_S r;
+    r.val = atan2(y.val, x.val);
+    const V ivv = V(1) / (x.val * x.val + y.val * y.val);
+    const G ivg = G(ivv), xg = G(x.val), yg = G(y.val);
+#pragma unroll
+    for (int i = 0; i < K; ++i) r.grad[i] = (xg * y.grad[i] - yg * x.grad[i]) * ivg;
+    if (H)
+    {
+        const T iv = T(ivv), xv = T(x.val), yv = T(y.val);
+        T tx[K], ty[K], tr[K], dv[K];
+        x.grad_as_hess_type(tx);
+        y.grad_as_hess_type(ty);
+        r.grad_as_hess_type(tr);
+#pragma unroll
+        for (int i = 0; i < K; ++i) dv[i] = T(2) * (xv * tx[i] + yv * ty[i]);
+        int q = 0;
+#pragma unroll
+        for (int i = 0; i < K; ++i)
+#pragma unroll
+            for (int j = i; j < K; ++j, ++q)
+            {
+                const T du = xv * y.hess[q] - yv * x.hess[q] + ty[i] * tx[j] - tx[i] * ty[j];
+                r.hess[q] = (du - tr[i] * dv[j]) * iv;
+            }
+    }
+    return r;
+}
+TAD_TPL TAD_HD TAD_S hypot(const TAD_S& a, const TAD_S& b) { return sqrt(a * a + b * b); }   // Scalar.hh:917-926
+
+/* ---- comparisons on the value (Scalar.hh:933-1095) ---------------------- */
+#define TAD_CMP(OP)                                                                           \
+    TAD_TPL TAD_HD bool operator OP(const TAD_S& a, const TAD_S& b) { return a.val OP b.val; } \
+    TAD_TPLU TAD_HD bool operator OP(const TAD_S& a, U b) { return a.val OP V(b); }            \
+    TAD_TPLU TAD_HD bool operator OP(U a, const TAD_S& b) { return V(a) OP b.val; }
+TAD_CMP(==)
+TAD_CMP(!=)
+TAD_CMP(<)
+TAD_CMP(<=)
+TAD_CMP(>)
+TAD_CMP(>=)
+#undef TAD_CMP
+
+TAD_TPL TAD_HD TAD_S min(const TAD_S& a, const TAD_S& b) { return (b < a) ? b : a; }
+TAD_TPL TAD_HD TAD_S max(const TAD_S& a, const TAD_S& b) { return (a < b) ? b : a; }
+TAD_TPL TAD_HD TAD_S fmin(const TAD_S& a, const TAD_S& b) { return min(a, b); }
+TAD_TPL TAD_HD TAD_S fmax(const TAD_S& a, const TAD_S& b) { return max(a, b); }
+TAD_TPL TAD_HD TAD_S clamp(const TAD_S& x, const TAD_S& a, const TAD_S& b) { return (x < a) ? a : ((x > b) ? b : x); }
+
+#undef TAD_TPLU
+#undef TAD_TPL
+#undef TAD_S
+
+/* passive overloads so functors written for Scalar also compile passively */
+TAD_HD double sqr(double v) { return v * v; }
+TAD_HD float sqr(float v) { return v * v; }
+
+/* ---------------------------------------------------------------------------
+ * MixedScalar<KX, KP, T>: value, full gradient over KX + KP variables and
+ * only the KX x KP block d2f/dx dp of the Hessian -- the truncated-block
+ * scalar Scalar<KX+KP, T, true, 0, KX, KX, KP> of the reference
+ * (Scalar.hh:24, :186-196; pinned by tests/ScalarTestHessianBlock.cc).
+ * The block is not symmetric and is stored dense, row-major.
+ * ------------------------------------------------------------------------ */
+template <int KX, int KP, typename T>
+struct MixedScalar
+{
+    static constexpr int k = KX + KP;
+    using passive_type = T;
+    T val;
+    T grad[KX + KP];
+    T blk[KX * KP];
+
+    TAD_HD MixedScalar() : val(T(0))
+    {
+#pragma unroll
+        for (int i = 0; i < k; ++i) grad[i] = T(0);
+#pragma unroll
+        for (int i = 0; i < KX * KP; ++i) blk[i] = T(0);
+    }
+    TAD_HD MixedScalar(T v) : MixedScalar() { val = v; }
+    TAD_HD MixedScalar(T v, int idx) : MixedScalar()
+    {
+        val = v;
+#pragma unroll
+        for (int i = 0; i < k; ++i) grad[i] = (i == idx) ? T(1) : T(0);
+    }
+    TAD_HD static MixedScalar chain(T f, T f1, T f2, const MixedScalar& a)
+    {
+        MixedScalar r;
+        r.val = f;
+#pragma unroll
+        for (int i = 0; i < k; ++i) r.grad[i] = f1 * a.grad[i];
+#pragma unroll
+        for (int i = 0; i < KX; ++i)
+#pragma unroll
+            for (int j = 0; j < KP; ++j)
+                r.blk[i * KP + j] = f2 * a.grad[i] * a.grad[KX + j] + f1 * a.blk[i * KP + j];
+        return r;
+    }
+};
+
+#define TAD_M MixedScalar<KX, KP, T>
+#define TAD_TPL template <int KX, int KP, typename T>
+#define TAD_TPLU template <int KX, int KP, typename T, typename U, typename = std::enable_if_t<std::is_arithmetic<U>::value>>
+TAD_TPL TAD_HD TAD_M operator-(const TAD_M& a)
+{
+    TAD_M r; r.val = -a.val;
+#pragma unroll
+    for (int i = 0; i < KX + KP; ++i) r.grad[i] = -a.grad[i];
+#pragma unroll
+    for (int i = 0; i < KX * KP; ++i) r.blk[i] = -a.blk[i];
+    return r;
+}
+TAD_TPL TAD_HD TAD_M operator+(const TAD_M& a, const TAD_M& b)
+{
+    TAD_M r; r.val = a.val + b.val;
+#pragma unroll
+    for (int i = 0; i < KX + KP; ++i) r.grad[i] = a.grad[i] + b.grad[i];
+#pragma unroll
+    for (int i = 0; i < KX * KP; ++i) r.blk[i] = a.blk[i] + b.blk[i];
+    return r;
+}
+TAD_TPL TAD_HD TAD_M operator-(const TAD_M& a, const TAD_M& b) { return a + (-b); }
+TAD_TPL TAD_HD TAD_M operator*(const TAD_M& a, const TAD_M& b)
+{
+    TAD_M r; r.val = a.val * b.val;
+#pragma unroll
+    for (int i = 0; i < KX + KP; ++i) r.grad[i] = b.val * a.grad[i] + a.val * b.grad[i];
+#pragma unroll
+    for (int i = 0; i < KX; ++i)
+#pragma unroll
+        for (int j = 0; j < KP; ++j)
+            r.blk[i * KP + j] = b.val * a.blk[i * KP + j] + a.grad[i] * b.grad[KX + j]
+                              + b.grad[i] * a.grad[KX + j] + a.val * b.blk[i * KP + j];
+    return r;
+}
+TAD_TPL TAD_HD TAD_M operator/(const TAD_M& a, const TAD_M& b)
+{
+    TAD_M r;
+    const T ib = T(1) / b.val;
+    r.val = a.val * ib;
+#pragma unroll
+    for (int i = 0; i < KX + KP; ++i) r.grad[i] = (a.grad[i] - r.val * b.grad[i]) * ib;
+#pragma unroll
+    for (int i = 0; i < KX; ++i)
+#pragma unroll
+        for (int j = 0; j < KP; ++j)
+            r.blk[i * KP + j] = (a.blk[i * KP + j] - r.grad[i] * b.grad[KX + j] - b.grad[i] * r.grad[KX + j]
+                                 - r.val * b.blk[i * KP + j]) * ib;
+    return r;
+}
+TAD_TPLU TAD_HD TAD_M operator*(const TAD_M& a, U s)
+{
+    TAD_M r; const T t = T(s); r.val = a.val * t;
+#pragma unroll
+    for (int i = 0; i < KX + KP; ++i) r.grad[i] = a.grad[i] * t;
+#pragma unroll
+    for (int i = 0; i < KX * KP; ++i) r.blk[i] = a.blk[i] * t;
+    return r;
+}
+TAD_TPLU TAD_HD TAD_M operator*(U s, const TAD_M& a) { return a * s; }
+TAD_TPLU TAD_HD TAD_M operator+(const TAD_M& a, U s) { TAD_M r = a; r.val += T(s); return r; }
+TAD_TPLU TAD_HD TAD_M operator-(const TAD_M& a, U s) { TAD_M r = a; r.val -= T(s); return r; }
+TAD_TPLU TAD_HD TAD_M operator/(U c, const TAD_M& b) { const TAD_M one{T(c)}; return one / b; }
+TAD_TPLU TAD_HD TAD_M operator/(const TAD_M& a, U s) { return a * (T(1) / T(s)); }
+TAD_TPL TAD_HD TAD_M sqrt(const TAD_M& a)
+{
+    using std::sqrt;
+    const T f = sqrt(a.val);
+    return TAD_M::chain(f, T(0.5) / f, T(-0.25) / (f * a.val), a);
+}
+TAD_TPL TAD_HD TAD_M sqr(const TAD_M& a) { return a * a; }
+TAD_TPLU TAD_HD bool operator<=(const TAD_M& a, U b) { return a.val <= T(b); }
+TAD_TPL TAD_HD T to_passive(const TAD_M& a) { return a.val; }
+#undef TAD_TPLU
+#undef TAD_TPL
+#undef TAD_M
+
+} // namespace tad

@@ -1,0 +1,247 @@
+"""GPU parity tests: the CUDA path through the C ABI against the oracle (the
+CPU restatement of TinyAD's path) on the same seeded inputs.
+
+Tolerances (FP64 path): f, g and H within 1e-10 normwise relative error
+(max |a - b| / max |b|); final Newton energy within 1e-8 relative.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import rel_err, sparse_rel_err, torus_mesh, valid_perturbation
+from tinyad_gb300 import meshes
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "known_answers.json")
+
+
+def _pair(tad, oracle, w, **kw):
+    return tad.ScalarFunction.from_workload(w, **kw), oracle.Problem.from_workload(w)
+
+
+def test_known_answers_device(tad):
+    """Operator known answers (tests/ScalarTest{Unary,Binary}Operators.cc) on
+    the device Double<1>, and on Mixed<1> (FP32 derivatives) at FP32 accuracy."""
+    for c in json.load(open(GOLDEN)):
+        exp = np.asarray(c["expected"])
+        scale = max(1.0, np.max(np.abs(exp)))
+        got = tad.debug_scalar_op(c["op"], c["a"], c["b"], tad.PREC_FP64)
+        np.testing.assert_allclose(got, exp, rtol=0, atol=c["tol"] * scale, err_msg=f'{c["name"]} ({c["source"]})')
+        got = tad.debug_scalar_op(c["op"], c["a"], c["b"], tad.PREC_MIXED)
+        np.testing.assert_allclose(got, exp, rtol=0, atol=max(c["tol"], 2e-6) * scale, err_msg=c["name"])
+
+
+def _quad(A, b, c):
+    return np.concatenate([np.asarray(A, float).ravel(), np.asarray(b, float), [c]])[None, :]
+
+
+def test_scalar_function_quadratics(tad):
+    """tests/ScalarFunctionTest.cc:10-151 on the device."""
+    f1 = tad.ScalarFunction(1, 1)
+    f1.add_elements(meshes.TAD_ENERGY_QUADRATIC, [[0]], _quad([[2.0]], [1.0], 1.0))
+    f, g, H = f1.eval_with_hessian_proj(np.array([1.0]))
+    assert f == 4.0 and g[0] == 5.0 and H[0, 0] == 4.0
+    A2 = [[2.0, 1.0], [1.0, 1.0]]
+    f2 = tad.ScalarFunction(2, 1)
+    f2.add_elements(meshes.TAD_ENERGY_QUADRATIC, [[0]], _quad(A2, [1.0, 0.0], 1.0))
+    x = np.array([1.0, 2.0])
+    assert f2.eval(x) == 12.0
+    fg, gg = f2.eval_with_gradient(x)
+    assert fg == 12.0 and list(gg) == [9.0, 6.0]
+    for f, g, H in (f2.eval_with_derivatives(x), f2.eval_with_hessian_proj(x)):
+        assert f == 12.0 and list(g) == [9.0, 6.0]
+        assert np.array_equal(H.toarray(), [[4.0, 2.0], [2.0, 2.0]])
+    f3 = tad.ScalarFunction(2, 1)
+    f3.add_elements(meshes.TAD_ENERGY_QUADRATIC, [[0]], _quad(-np.array(A2), [-1.0, 0.0], -1.0))
+    f, g, H = f3.eval_with_derivatives(x)
+    assert f == -12.0 and list(g) == [-9.0, -6.0] and np.array_equal(H.toarray(), [[-4.0, -2.0], [-2.0, -2.0]])
+    f, g, Hp = f3.eval_with_hessian_proj(x)
+    assert np.all(np.linalg.eigvalsh(Hp.toarray()) > 0)
+
+
+def test_planar_newton(tad, oracle):
+    """tests/NewtonTest.cc:57-111 on the device: nnz formula, f -> 4 and
+    g -> 0, same final energy as the oracle, bitwise deterministic."""
+    w = meshes.planar_test_mesh()
+    fn, p = _pair(tad, oracle, w, pcg_rel_tol=1e-14, pcg_max_iters=200)
+    f, g, H = fn.eval_with_hessian_proj(w.x0)
+    assert H.nnz == 4 * 6 + 8 * (6 + 4 - 1)
+    fo, go, Ho = p.eval_with_hessian_proj(w.x0)
+    assert rel_err(f, fo) <= TOL and rel_err(g, go) <= TOL and sparse_rel_err(H, Ho) <= TOL
+    x, fh = fn.newton_solve(w.x0, 10)
+    x2, fh2 = fn.newton_solve(w.x0, 10)
+    assert np.array_equal(x, x2) and np.array_equal(fh, fh2)
+    f, g, H = fn.eval_with_hessian_proj(x)
+    assert abs(fn.eval(x) - f) <= 1e-15
+    assert abs(f - 4.0) <= 1e-12
+    assert np.max(np.abs(g)) <= 1e-10
+    xo, fho, _ = p.newton(w.x0, 10)
+    assert abs(fh[-1] - fho[-1]) <= 1e-8 * abs(fho[-1])
+
+
+def _perturbed(w, scale, seed):
+    rng = np.random.default_rng(seed)
+    return w.x0 + rng.normal(scale=scale, size=w.x0.size)
+
+
+@pytest.mark.parametrize("grid", [12, 64])
+def test_disk_eval_parity(tad, oracle, grid):
+    """f, g, H of eval / eval_with_gradient / eval_with_derivatives /
+    eval_with_hessian_proj on the disk parametrisation (config 0 at grid 64)."""
+    w = meshes.disk_param(grid, seed=0)
+    fn, p = _pair(tad, oracle, w)
+    for x in (w.x0, valid_perturbation(w, p, 0.002, 1)):
+        assert rel_err(fn.eval(x), p.eval(x)) <= TOL
+        f, g = fn.eval_with_gradient(x)
+        fo, go = p.eval_with_gradient(x)
+        assert rel_err(f, fo) <= TOL and rel_err(g, go) <= TOL
+        f, g, H = fn.eval_with_derivatives(x)
+        fo, go, Ho = p.eval_with_derivatives(x)
+        assert rel_err(f, fo) <= TOL and rel_err(g, go) <= TOL and sparse_rel_err(H, Ho) <= TOL
+        assert H.nnz == Ho.nnz
+        f, g, H = fn.eval_with_hessian_proj(x)
+        fo, go, Ho = p.eval_with_hessian_proj(x)
+        assert rel_err(f, fo) <= TOL and rel_err(g, go) <= TOL and sparse_rel_err(H, Ho) <= TOL
+
+
+def test_inverted_elements(tad, oracle):
+    """det <= 0 -> +inf energy, zero derivatives and an eps*I projected block
+    (NewtonTest.cc:40-41, HessianProjection.hh:66-98), as in the oracle."""
+    w = meshes.disk_param(12, seed=0)
+    x = _perturbed(w, 0.2, 2)
+    fn, p = _pair(tad, oracle, w)
+    f, g, H = fn.eval_with_hessian_proj(x)
+    fo, go, Ho = p.eval_with_hessian_proj(x)
+    assert f == np.inf and fo == np.inf
+    assert rel_err(g, go) <= TOL and sparse_rel_err(H, Ho) <= TOL
+    assert fn.eval(x) == np.inf
+
+
+def test_disk_newton_parity(tad, oracle):
+    """Config 0: 20 Projected-Newton iterations on the device reach the
+    oracle's (LDL^T-based) final energy within 1e-8 relative."""
+    w = meshes.disk_param(64, seed=0)
+    fn, p = _pair(tad, oracle, w, pcg_rel_tol=1e-10, pcg_max_iters=2000)
+    x, fh = fn.newton_solve(w.x0, 20)
+    xo, fho, _ = p.newton(w.x0, 20)
+    assert abs(fh[-1] - fho[-1]) <= 1e-8 * abs(fho[-1]), (fh, fho)
+    assert abs(fn.eval(x) - p.eval(x)) <= TOL * abs(fho[-1])
+
+
+def test_tet_eval_parity(tad, oracle):
+    """k = 12 symmetric Dirichlet tets + penalties (config 1 at 4^3 cells)."""
+    w = meshes.tet_twist(4, seed=1)
+    fn, p = _pair(tad, oracle, w)
+    for x in (w.x0, valid_perturbation(w, p, 0.01, 3)):
+        f, g, H = fn.eval_with_hessian_proj(x)
+        fo, go, Ho = p.eval_with_hessian_proj(x)
+        assert rel_err(f, fo) <= TOL and rel_err(g, go) <= TOL and sparse_rel_err(H, Ho) <= TOL
+        f, g, H = fn.eval_with_derivatives(x)
+        fo, go, Ho = p.eval_with_derivatives(x)
+        assert rel_err(f, fo) <= TOL and rel_err(g, go) <= TOL and sparse_rel_err(H, Ho) <= TOL
+
+
+def test_tet_newton_parity(tad, oracle):
+    w = meshes.tet_twist(4, seed=1)
+    fn, p = _pair(tad, oracle, w, pcg_rel_tol=1e-10, pcg_max_iters=3000)
+    x, fh = fn.newton_solve(w.x0, 40)
+    xo, fho, _ = p.newton(w.x0, 40)
+    assert abs(fh[-1] - fho[-1]) <= 1e-8 * abs(fho[-1]), (fh[-3:], fho[-3:])
+
+
+def test_laplacian_device(tad):
+    """Hessian of the Dirichlet energy = graph Laplacian (DynamicElementsTest.cc:60-91)."""
+    import scipy.sparse as sp
+    nv, F = torus_mesh()
+    fn = tad.ScalarFunction(1, nv)
+    fn.add_elements(meshes.TAD_ENERGY_DIRICHLET_TRI, F, np.full((F.shape[0], 1), 0.25))
+    H = fn.eval_hessian_of_quadratic()
+    rows, cols, vals = [], [], []
+    for t in F:
+        for i in range(3):
+            rows += [t[i], t[i]]
+            cols += [t[i], t[(i + 1) % 3]]
+            vals += [1.0, -1.0]
+    Lref = sp.coo_matrix((vals, (rows, cols)), shape=(nv, nv)).tocsr()
+    Lref.sum_duplicates()
+    assert H.nnz == Lref.nnz and abs(H - Lref).max() <= 1e-12
+
+
+def test_determinism(tad):
+    """Bitwise reproducible evaluations and solves (NewtonTest.cc:97-111)."""
+    w = meshes.disk_param(40, seed=5)
+    fn = tad.ScalarFunction.from_workload(w)
+    a = fn.eval_with_hessian_proj(w.x0)
+    b = fn.eval_with_hessian_proj(w.x0)
+    assert a[0] == b[0] and np.array_equal(a[1], b[1]) and np.array_equal(a[2].data, b[2].data)
+    x1, f1 = fn.newton_solve(w.x0, 3)
+    x2, f2 = fn.newton_solve(w.x0, 3)
+    assert np.array_equal(x1, x2) and np.array_equal(f1, f2)
+
+
+def test_errors_leave_function_usable(tad):
+    """Bad input raises RuntimeError and the function stays usable
+    (tests/ExceptionTest.cc:8-53)."""
+    fn = tad.ScalarFunction(2, 3)
+    with pytest.raises(RuntimeError):
+        fn.add_elements(meshes.TAD_ENERGY_POSITION_PENALTY, [[7]], [[0.0, 0.0, 1.0]])
+    with pytest.raises(RuntimeError):
+        fn.add_elements(meshes.TAD_ENERGY_SYMMETRIC_DIRICHLET_TET, [[0, 1, 2, 0]], np.zeros((1, 10)))
+    fn.add_elements(meshes.TAD_ENERGY_POSITION_PENALTY, [[1]], [[1.0, 2.0, 1.0]])
+    with pytest.raises(RuntimeError):
+        fn.eval(np.zeros(5))
+    f, g = fn.eval_with_gradient(np.zeros(6))
+    assert f == 5.0 and list(g) == [0.0, 0.0, -2.0, -4.0, 0.0, 0.0]
+    with pytest.raises(RuntimeError):
+        fn.add_elements(meshes.TAD_ENERGY_POSITION_PENALTY, [[0]], [[1.0, 2.0, 1.0]])   # after finalize
+
+
+def test_line_search_api(tad, oracle):
+    """line_search matches the reference's sequential Armijo search."""
+    w = meshes.disk_param(20, seed=6)
+    fn, p = _pair(tad, oracle, w)
+    f, g, H = fn.eval_with_hessian_proj(w.x0)
+    d = p.newton_direction(g)
+    x_gpu = fn.line_search(w.x0, d, f, g)
+    x_cpu, _, ok = p.line_search(w.x0, d, f, g)
+    assert ok and rel_err(x_gpu, x_cpu) <= 1e-14
+    x_bad = fn.line_search(w.x0, g, f, g)          # ascent direction: x unchanged
+    assert np.array_equal(x_bad, w.x0)
+
+
+def test_newton_direction_api(tad, oracle):
+    """newton_direction (PCG) against the oracle's LDL^T direction."""
+    w = meshes.disk_param(20, seed=6)
+    fn, p = _pair(tad, oracle, w, pcg_rel_tol=1e-13, pcg_max_iters=5000)
+    d, f, g = fn.newton_direction(w.x0)
+    fo, go, Ho = p.eval_with_hessian_proj(w.x0)
+    do = p.newton_direction(go)
+    # the direction solves the oracle's system (it differs from LDL^T's only
+    # along the eps-scaled translation null space)
+    assert rel_err(Ho @ d, -go) <= 1e-9
+    assert rel_err(Ho @ do, -go) <= 1e-9
+    assert abs(d @ go - do @ go) <= 1e-8 * abs(do @ go)
+
+
+def test_mixed_precision(tad, oracle):
+    """Mixed mode: FP32 element Hessians, projection and PCG; FP64 values
+    (edge vectors, determinant, inverse, energy), gradient, line-search
+    energy and refinement residuals.  f and g match the FP64 oracle, H carries
+    FP32 rounding, and the Newton loop reaches the FP64 final energy within
+    1e-8 relative."""
+    w = meshes.disk_param(64, seed=0)
+    fm = tad.ScalarFunction.from_workload(w, precision=tad.PREC_MIXED, pcg_rel_tol=1e-8, pcg_max_iters=2000)
+    p = oracle.Problem.from_workload(w)
+    x = w.x0
+    f, g, H = fm.eval_with_hessian_proj(x)
+    fo, go, Ho = p.eval_with_hessian_proj(x)
+    assert rel_err(f, fo) <= 1e-12
+    assert rel_err(g, go) <= 1e-10
+    assert sparse_rel_err(H, Ho) <= 5e-5
+    xm, fhm = fm.newton_solve(w.x0, 25)
+    xo, fho, _ = p.newton(w.x0, 25)
+    assert abs(fhm[-1] - fho[-1]) <= 1e-8 * abs(fho[-1]), (fhm[-4:], fho[-4:])

@@ -1,0 +1,348 @@
+"""tinyad_gb300 -- GB300-native sparse per-element derivative path.
+
+Python mirror of TinyAD's ScalarFunction interface for this path
+(include/TinyAD/ScalarFunction.hh:57-248), calling the CUDA library
+(libtad.so, C ABI in include/tad.h) through ctypes.  Method names, argument
+meanings and error behaviour follow the reference: every failure raises
+RuntimeError (the reference throws std::runtime_error, Out.hh:73-79) and the
+function stays usable afterwards.
+
+There is no CPU fallback: loading fails loudly when the CUDA library or a
+GPU is missing.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import meshes  # noqa: F401  (workload generators)
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libtad.so")
+
+TAD_OK = 0
+TAD_ERR_ARG = 1
+TAD_ERR_NONFINITE = 2
+TAD_ERR_PCG_NOCONV = 3
+TAD_ERR_LS_FAIL = 4
+TAD_ERR_TIMEOUT = 5
+TAD_ERR_CUDA = 6
+TAD_ERR_STATE = 7
+TAD_ERR_TOO_MANY_VARS = 8
+
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+default_hessian_projection_eps = 1e-9   # HessianProjection.hh:16
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int32)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+
+
+class Settings(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int), ("pcg_max_iters", ctypes.c_int), ("pcg_rel_tol", ctypes.c_double),
+                ("refine_max_iters", ctypes.c_int), ("refine_rel_tol", ctypes.c_double),
+                ("ls_max_iters", ctypes.c_int), ("ls_shrink", ctypes.c_double), ("ls_armijo", ctypes.c_double),
+                ("verbose", ctypes.c_int)]
+
+
+class TinyADError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(msg)
+        self.status = status
+
+
+_lib = None
+
+# every symbol include/tad.h declares (checked by the CPU tests)
+EXPORTS = [
+    "tad_settings_default", "tad_last_error_message", "tad_version", "tad_problem_create", "tad_problem_destroy",
+    "tad_problem_set_settings", "tad_n_vars", "tad_add_elements", "tad_add_elements_custom", "tad_finalize",
+    "tad_hessian_nnz", "tad_hessian_pattern", "tad_eval", "tad_eval_with_gradient", "tad_eval_with_derivatives",
+    "tad_eval_with_hessian_proj", "tad_eval_d", "tad_eval_with_hessian_proj_d", "tad_newton_direction",
+    "tad_line_search", "tad_newton_solve", "tad_newton_solve_d", "tad_last_solve_stats", "tad_debug_scalar_op",
+    "tad_get_stream", "tad_measure_fma_peak",
+]
+
+
+def load(build_if_missing: bool = True):
+    """Load libtad.so (building it in-tree with nvcc if needed)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if not build_if_missing:
+            raise OSError(f"CUDA library not built: {LIB_PATH}")
+        from . import build as _b
+        _b.build()
+    L = ctypes.CDLL(LIB_PATH)
+    L.tad_last_error_message.restype = ctypes.c_char_p
+    L.tad_version.restype = ctypes.c_char_p
+    L.tad_settings_default.argtypes = [ctypes.POINTER(Settings)]
+    L.tad_problem_create.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.POINTER(Settings), ctypes.POINTER(ctypes.c_void_p)]
+    L.tad_problem_destroy.argtypes = [ctypes.c_void_p]
+    L.tad_problem_set_settings.argtypes = [ctypes.c_void_p, ctypes.POINTER(Settings)]
+    L.tad_n_vars.argtypes = [ctypes.c_void_p]
+    L.tad_n_vars.restype = ctypes.c_int64
+    L.tad_add_elements.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int64, _ip, _dp, ctypes.c_int]
+    L.tad_finalize.argtypes = [ctypes.c_void_p]
+    L.tad_hessian_nnz.argtypes = [ctypes.c_void_p, _i64p]
+    L.tad_hessian_pattern.argtypes = [ctypes.c_void_p, _ip, _ip]
+    L.tad_eval.argtypes = [ctypes.c_void_p, _dp, _dp]
+    L.tad_eval_with_gradient.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
+    L.tad_eval_with_derivatives.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, _dp]
+    L.tad_eval_with_hessian_proj.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double, _dp, _dp, _dp]
+    L.tad_eval_d.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _dp]
+    L.tad_eval_with_hessian_proj_d.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, _dp,
+                                               ctypes.c_void_p, ctypes.c_void_p]
+    L.tad_newton_direction.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double, ctypes.c_double, _dp, _dp, _dp]
+    L.tad_line_search.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double, _dp, ctypes.c_double, _dp, _dp]
+    L.tad_newton_solve.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_double, ctypes.c_double, _dp,
+                                   ctypes.POINTER(ctypes.c_int)]
+    L.tad_newton_solve_d.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                     _dp, ctypes.POINTER(ctypes.c_int)]
+    L.tad_last_solve_stats.argtypes = [ctypes.c_void_p, _dp, _i64p, _i64p]
+    L.tad_debug_scalar_op.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
+    L.tad_get_stream.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]
+    L.tad_measure_fma_peak.argtypes = [ctypes.c_int, _dp]
+    _lib = L
+    return L
+
+
+def default_settings(**kw) -> Settings:
+    s = Settings()
+    load().tad_settings_default(ctypes.byref(s))
+    for k, v in kw.items():
+        setattr(s, k, v)
+    return s
+
+
+def _d(a: np.ndarray):
+    return a.ctypes.data_as(_dp)
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class ScalarFunction:
+    """A sum of per-element energies over d-dimensional variable handles.
+
+    Mirrors TinyAD::ScalarFunction<d, double, Eigen::Index> for the built-in
+    energies (tad_energy in include/tad.h); user functors use the C++ front
+    end include/tad/ScalarFunction.cuh.
+    """
+
+    def __init__(self, var_dim: int, n_handles: int, settings: Settings | None = None, **kw):
+        self.L = load()
+        self.var_dim = var_dim
+        self.n_handles = n_handles
+        self.n_vars = var_dim * n_handles
+        self.settings = settings if settings is not None else default_settings(**kw)
+        h = ctypes.c_void_p()
+        self._check(self.L.tad_problem_create(var_dim, n_handles, ctypes.byref(self.settings), ctypes.byref(h)))
+        self.h = h
+        self._pattern = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.tad_problem_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int, allow=()) -> int:
+        if rc != TAD_OK and rc not in allow:
+            raise TinyADError(rc, self.L.tad_last_error_message().decode())
+        return rc
+
+    def set_settings(self, **kw):
+        for k, v in kw.items():
+            setattr(self.settings, k, v)
+        self._check(self.L.tad_problem_set_settings(self.h, ctypes.byref(self.settings)))
+
+    # ---- setup -------------------------------------------------------------
+    def add_elements(self, energy: int, handles, params):
+        """add_elements<N>(range, lambda) for a built-in energy."""
+        handles = np.ascontiguousarray(handles, dtype=np.int32)
+        if handles.ndim == 1:
+            handles = handles[:, None]
+        params = _f64(params)
+        if params.ndim == 1:
+            params = params[:, None]
+        n, N = handles.shape
+        self._check(self.L.tad_add_elements(self.h, int(energy), N, n, handles.ctypes.data_as(_ip), _d(params),
+                                            params.shape[1] if n > 0 else int(params.shape[-1])))
+        self._pattern = None
+
+    @classmethod
+    def from_workload(cls, w, **kw) -> "ScalarFunction":
+        f = cls(w.var_dim, w.n_handles, **kw)
+        for t in w.terms:
+            f.add_elements(t.energy, t.handles, t.params)
+        return f
+
+    def finalize(self):
+        self._check(self.L.tad_finalize(self.h))
+
+    def hessian_pattern(self):
+        if self._pattern is None:
+            nnz = np.zeros(1, np.int64)
+            self._check(self.L.tad_hessian_nnz(self.h, nnz.ctypes.data_as(_i64p)))
+            outer = np.zeros(self.n_vars + 1, np.int32)
+            inner = np.zeros(int(nnz[0]), np.int32)
+            self._check(self.L.tad_hessian_pattern(self.h, outer.ctypes.data_as(_ip), inner.ctypes.data_as(_ip)))
+            self._pattern = (outer, inner)
+        return self._pattern
+
+    def _csr(self, vals):
+        import scipy.sparse as sp
+        outer, inner = self.hessian_pattern()
+        return sp.csr_matrix((vals, inner, outer), shape=(self.n_vars, self.n_vars))
+
+    # ---- data marshalling (ScalarFunctionImpl.hh:216-254) --------------------
+    def x_from_data(self, read):
+        x = np.full(self.n_vars, np.nan)
+        for v in range(self.n_handles):
+            x[v * self.var_dim:(v + 1) * self.var_dim] = read(v)
+        if not np.all(np.isfinite(x)):
+            raise TinyADError(TAD_ERR_NONFINITE, "Assertion failed: Not finite x")
+        return x
+
+    def x_to_data(self, x, write):
+        x = _f64(x)
+        if x.size != self.n_vars:
+            raise TinyADError(TAD_ERR_ARG, "Assertion failed: x.size() == n_vars")
+        for v in range(self.n_handles):
+            write(v, x[v * self.var_dim:(v + 1) * self.var_dim])
+
+    # ---- evaluation --------------------------------------------------------
+    def _x(self, x) -> np.ndarray:
+        x = _f64(x)
+        if x.size != self.n_vars:
+            raise TinyADError(TAD_ERR_ARG, f"Assertion failed: {x.size} == {self.n_vars}")
+        return x
+
+    def eval(self, x) -> float:
+        x = self._x(x)
+        f = np.zeros(1)
+        self._check(self.L.tad_eval(self.h, _d(x), _d(f)))
+        return float(f[0])
+
+    __call__ = eval
+
+    def eval_with_gradient(self, x):
+        x = self._x(x)
+        f = np.zeros(1)
+        g = np.zeros(self.n_vars)
+        self._check(self.L.tad_eval_with_gradient(self.h, _d(x), _d(f), _d(g)))
+        return float(f[0]), g
+
+    def eval_with_derivatives(self, x):
+        x = self._x(x)
+        f = np.zeros(1)
+        g = np.zeros(self.n_vars)
+        outer, inner = self.hessian_pattern()
+        vals = np.zeros(inner.size)
+        self._check(self.L.tad_eval_with_derivatives(self.h, _d(x), _d(f), _d(g), _d(vals)))
+        return float(f[0]), g, self._csr(vals)
+
+    def eval_hessian(self, x):
+        return self.eval_with_derivatives(x)[2]
+
+    def eval_hessian_of_quadratic(self):
+        return self.eval_hessian(np.zeros(self.n_vars))
+
+    def eval_with_hessian_proj(self, x, projection_eps: float = default_hessian_projection_eps):
+        x = self._x(x)
+        f = np.zeros(1)
+        g = np.zeros(self.n_vars)
+        outer, inner = self.hessian_pattern()
+        vals = np.zeros(inner.size)
+        self._check(self.L.tad_eval_with_hessian_proj(self.h, _d(x), projection_eps, _d(f), _d(g), _d(vals)))
+        return float(f[0]), g, self._csr(vals)
+
+    # ---- solver utilities ----------------------------------------------------
+    def newton_direction(self, x, projection_eps: float = default_hessian_projection_eps):
+        """d = -H_proj(x)^-1 g(x) (device PCG).  Returns (d, f, g)."""
+        x = self._x(x)
+        d = np.zeros(self.n_vars)
+        g = np.zeros(self.n_vars)
+        f = np.zeros(1)
+        self._check(self.L.tad_newton_direction(self.h, _d(x), projection_eps, 0.0, _d(d), _d(f), _d(g)),
+                    allow=(TAD_ERR_PCG_NOCONV,))
+        return d, float(f[0]), g
+
+    def line_search(self, x0, d, f, g, s_max: float = 1.0):
+        """line_search(x0, d, f, g, func, s_max) -> x (x0 when no decrease)."""
+        x0, d, g = self._x(x0), self._x(d), self._x(g)
+        xo = np.zeros(self.n_vars)
+        fo = np.zeros(1)
+        self._check(self.L.tad_line_search(self.h, _d(x0), _d(d), float(f), _d(g), s_max, _d(xo), _d(fo)),
+                    allow=(TAD_ERR_LS_FAIL,))
+        return xo
+
+    def newton_solve(self, x, n_iters: int, projection_eps: float = default_hessian_projection_eps,
+                     stop_decrement: float = 0.0):
+        """n_iters Projected-Newton iterations on the device.  Returns (x, f_hist)."""
+        x = self._x(x).copy()
+        fh = np.zeros(n_iters + 1)
+        done = ctypes.c_int(0)
+        self._check(self.L.tad_newton_solve(self.h, _d(x), n_iters, projection_eps, stop_decrement, _d(fh),
+                                            ctypes.byref(done)))
+        return x, fh[:done.value + 1]
+
+    @property
+    def stream_ptr(self) -> int:
+        s = ctypes.c_void_p()
+        self._check(self.L.tad_get_stream(self.h, ctypes.byref(s)))
+        return int(s.value or 0)
+
+    def newton_solve_device(self, x_ptr: int, n_iters: int, projection_eps: float = default_hessian_projection_eps,
+                            stop_decrement: float = 0.0):
+        """Newton iterations on a device-resident x (pointer to n_vars doubles)."""
+        fh = np.zeros(n_iters + 1)
+        done = ctypes.c_int(0)
+        self._check(self.L.tad_newton_solve_d(self.h, ctypes.c_void_p(x_ptr), n_iters, projection_eps, stop_decrement,
+                                              _d(fh), ctypes.byref(done)))
+        return fh[:done.value + 1]
+
+    def last_solve_stats(self) -> dict:
+        ms = np.zeros(4)
+        it = np.zeros(1, np.int64)
+        tr = np.zeros(1, np.int64)
+        self._check(self.L.tad_last_solve_stats(self.h, _d(ms), it.ctypes.data_as(_i64p), tr.ctypes.data_as(_i64p)))
+        return {"ms_eval": ms[0], "ms_assemble": ms[1], "ms_pcg": ms[2], "ms_linesearch": ms[3],
+                "pcg_iters": int(it[0]), "ls_trials": int(tr[0])}
+
+
+def debug_scalar_op(op: int, a, b=(0.0, 0.0, 0.0), precision: int = PREC_FP64) -> np.ndarray:
+    """Apply one device Scalar<1> operator (op codes in include/tad.h)."""
+    L = load()
+    a3, b3, out = _f64(a), _f64(b), np.zeros(3)
+    rc = L.tad_debug_scalar_op(op, precision, _d(a3), _d(b3), _d(out))
+    if rc != TAD_OK:
+        raise TinyADError(rc, L.tad_last_error_message().decode())
+    return out
+
+
+def measure_fma_peak(precision: int) -> float:
+    """CUDA-core FMA throughput (TFLOP/s) measured on the current GPU."""
+    L = load()
+    out = np.zeros(1)
+    rc = L.tad_measure_fma_peak(precision, _d(out))
+    if rc != TAD_OK:
+        raise TinyADError(rc, L.tad_last_error_message().decode())
+    return float(out[0])
+
+
+def scalar_function(var_dim: int, n_handles: int, **kw) -> ScalarFunction:
+    """scalar_function<d>(range(n)) (ScalarFunctionImpl.hh:418-442)."""
+    return ScalarFunction(var_dim, n_handles, **kw)

@@ -1,0 +1,174 @@
+/*
+ * Library internals shared by the C-ABI translation units.
+ *
+ * HBM layout of one problem (n = d * n_handles variables, interleaved x[d*v+i]):
+ *   per term:  rec[n_elem][N] int32   recorded access order (-1 = unused slot)
+ *              vtx/prm                 built-in energies' vertex lists / params
+ *   element outputs, all terms concatenated (term offsets in units below):
+ *              ef[n_elem_total]                 double, element energies
+ *                                              (x LS_BATCH in line-search mode)
+ *              eg[n_slots_total][d]             double, element gradient slots
+ *              eH[n_pairs_total][d][d]          double (FP64) or float (mixed)
+ *   pattern (built once, like LinearSolver's analyzePattern, LinearSolver.hh:12-19):
+ *              bptr[n_handles+1], bcol[nb]      BSR block rows (d x d blocks)
+ *              diag[n_handles]                  BSR index of each diagonal block
+ *              cptr[nb+1], cidx[ncontrib]       per block: element pair blocks in
+ *                                              element order (bit 31 = transposed)
+ *              gptr[n_handles+1], gidx[...]     per handle: element slots
+ *   assembled: g[n] double, H[nb][d][d] double (plain) / float (mixed)
+ *   solver:    r, z, p, Ap, dx [n] double (plain) / float (mixed inner PCG),
+ *              Dinv[n_handles][d][d]
+ */
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/tad.h"
+
+namespace tadlib {
+
+constexpr int LS_BATCH = 8;        // trial step sizes evaluated per launch
+constexpr int RED_BLOCKS = 608;    // 4 x 152 SMs: fixed grid of the reductions
+constexpr int RED_THREADS = 256;
+
+void set_error(const std::string& msg);
+
+#define TAD_CUDA_TRY(expr)                                                          \
+    do {                                                                            \
+        cudaError_t _e = (expr);                                                    \
+        if (_e != cudaSuccess) {                                                    \
+            tadlib::set_error(std::string("CUDA error: ") + cudaGetErrorString(_e)   \
+                              + " at " + __FILE__ + ":" + std::to_string(__LINE__)); \
+            return TAD_ERR_CUDA;                                                    \
+        }                                                                           \
+    } while (0)
+
+struct Term
+{
+    int energy = -1;                 // tad_energy, or -1 for a custom functor
+    int N = 0;
+    int64_t n_elem = 0;
+    int n_params = 0;
+    std::vector<int32_t> vtx_h;      // built-in: element vertex handles
+    int32_t* vtx_d = nullptr;
+    double* prm_d = nullptr;
+    int32_t* rec_d = nullptr;        // recorded access order
+    std::vector<int32_t> rec_h;
+    tad_term_eval_fn fn = nullptr;
+    void* user = nullptr;
+    int64_t elem_off = 0, slot_off = 0, pair_off = 0;
+};
+
+/* device-side scalars of one problem */
+struct DevScalars
+{
+    double f;            // energy at x
+    double f_trial[LS_BATCH];
+    double dg;           // d . g
+    double alpha, beta, rz, rz_new, rr, bb, pAp;
+    double tol2;         // (rel_tol * |b|)^2
+    int32_t done;        // PCG converged / stopped
+    int32_t breakdown;   // non-positive curvature
+    int32_t iters;       // PCG iterations
+    int32_t max_iters;   // PCG iteration cap
+    int32_t ls_choice;   // index of accepted trial in the batch, -1 none
+    double ls_f;         // accepted energy
+    double ls_s;         // accepted step
+    double decrement;    // -0.5 d.g
+};
+
+struct Problem
+{
+    int d = 0;
+    int64_t n_handles = 0, n_vars = 0;
+    tad_settings settings{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<Term> terms;
+    bool finalized = false;
+    int precision = TAD_PREC_FP64;
+
+    int64_t n_elem_total = 0, n_slots_total = 0, n_pairs_total = 0;
+    double* ef = nullptr;
+    double* eg = nullptr;
+    void* eH = nullptr;
+    size_t eH_bytes = 0;
+
+    // pattern
+    int64_t nb = 0, ncontrib = 0, ninc = 0;
+    std::vector<int32_t> bptr_h, bcol_h;
+    int32_t *bptr = nullptr, *bcol = nullptr, *diag = nullptr;
+    int32_t *cptr = nullptr, *cidx = nullptr;
+    int32_t *gptr = nullptr, *gidx = nullptr;
+
+    // assembled quantities
+    double* x = nullptr;
+    double* g = nullptr;
+    void* H = nullptr;         // nb*d*d, double or float
+    double* H64 = nullptr;     // FP64 copy for mixed-mode refinement residuals (optional)
+    double* csr_tmp = nullptr; // CSR-ordered values for export
+
+    // solver work
+    double *r = nullptr, *z = nullptr, *p = nullptr, *Ap = nullptr, *dx = nullptr, *dinv = nullptr;
+    float *r32 = nullptr, *z32 = nullptr, *p32 = nullptr, *Ap32 = nullptr, *dx32 = nullptr, *dinv32 = nullptr;
+    double *rhs = nullptr, *res = nullptr;
+    double* steps = nullptr;   // LS_BATCH trial step sizes (device)
+    double* partials = nullptr;
+    unsigned* counters = nullptr;
+    DevScalars* ds = nullptr;
+    DevScalars* hs = nullptr;  // pinned mirror
+    int32_t* err = nullptr;
+    int32_t* err_h = nullptr;  // pinned
+
+    // captured PCG iteration graphs (chunk of iterations)
+    cudaGraphExec_t pcg_graph = nullptr;
+    int pcg_graph_chunk = 0;
+    int pcg_graph_prec = -1;
+    const void* pcg_graph_x = nullptr;
+
+    // stats of the last solve
+    double ms_stage[4] = {0, 0, 0, 0};
+    int64_t pcg_iters_total = 0, ls_trials_total = 0;
+    cudaEvent_t ev[8] = {};
+    bool timing = false;
+};
+
+// ---- problem.cu
+tad_status ensure_finalized(Problem& P);
+tad_status check_device_error(Problem& P);
+
+// ---- builtin_*.cu: launch a built-in energy term for one evaluation mode
+tad_status launch_builtin(Problem& P, Term& T, const tad_term_eval_args& a);
+tad_status launch_builtin_tri(Problem& P, Term& T, const tad_term_eval_args& a);
+tad_status launch_builtin_tet(Problem& P, Term& T, const tad_term_eval_args& a);
+tad_status launch_builtin_misc(Problem& P, Term& T, const tad_term_eval_args& a);
+
+// ---- eval.cu
+/* evaluate all terms in `mode` at x (device) into the element buffers */
+tad_status eval_elements(Problem& P, int mode, const double* x, double eps, int precision,
+                         const double* dir = nullptr, int n_steps = 0);
+/* assemble element buffers -> f (device scalar ds->f), g, H */
+tad_status assemble(Problem& P, bool gradient, bool hessian, int precision);
+/* full f/g/H evaluation at device x */
+tad_status eval_full(Problem& P, const double* x, int mode, double eps, int precision);
+
+// ---- kernels (kernels.cu)
+void launch_reduce_f(Problem& P, int n_rows, double* out);      // sums ef rows into out[row]
+void launch_assemble_grad(Problem& P);
+void launch_assemble_hess(Problem& P, int precision);
+void launch_bsr_to_csr(Problem& P, double* out, int precision);
+void launch_zero(double* p, int64_t n, cudaStream_t s);
+
+// ---- solver.cu
+tad_status pcg_solve(Problem& P, const double* b, double* xsol, double w_identity, int precision,
+                     double rel_tol, int max_iters, int* iters_out);
+tad_status line_search_device(Problem& P, double* x, const double* d, double f, double s_max,
+                              bool* found, double* f_out, int* trials);
+tad_status newton_solve(Problem& P, double* x_d, int n_iters, double eps, double stop_decrement,
+                        double* f_hist, int* iters_done);
+
+} // namespace tadlib
+
+struct tad_problem : public tadlib::Problem {};

@@ -1,0 +1,214 @@
+/*
+ * Assembly and reduction kernels.  All of them are HBM-bound gathers; none
+ * uses floating-point atomics, so every result is bitwise reproducible.
+ *
+ *   k_reduce_rows     f = sum of element energies (one row per line-search
+ *                     trial), fixed partition over RED_BLOCKS blocks, then
+ *                     the last block to finish sums the block partials in
+ *                     block order.
+ *   k_assemble_grad   g[v] = sum over v's element slots, in element order
+ *                     (ScalarObjectiveTerm.hh:262-264 adds them in that order).
+ *   k_assemble_hess   H block (u,w) = sum over its element pair blocks, in
+ *                     element order (the order setFromTriplets sums
+ *                     duplicates, ScalarFunctionImpl.hh:398).  Algorithmic
+ *                     bytes per block: its contributions' d*d values + 4-byte
+ *                     ids, plus d*d values written.
+ *   k_bsr_to_csr      scalar CSR values (Eigen's CSC arrays for symmetric H)
+ *                     from the BSR blocks, for the host-facing Hessian.
+ */
+#include "internal.hh"
+
+namespace tadlib {
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+/* fixed-order block sum; result valid in thread 0 */
+__device__ __forceinline__ double block_sum(double v, double* sh)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    v = warp_sum(v);
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    v = 0.0;
+    if (w == 0)
+    {
+        v = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
+        v = warp_sum(v);
+    }
+    __syncthreads();
+    return v;
+}
+
+__global__ void __launch_bounds__(RED_THREADS) k_reduce_rows(const double* ef, int64_t n, int64_t stride,
+                                                             double* partials, unsigned* counters, double* out)
+{
+    __shared__ double sh[32];
+    __shared__ bool last;
+    const int row = blockIdx.y;
+    const double* a = ef + (int64_t)row * stride;
+    const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+    const int64_t beg = (int64_t)blockIdx.x * chunk;
+    const int64_t end = min(n, beg + chunk);
+    double v = 0.0;
+    for (int64_t i = beg + threadIdx.x; i < end; i += blockDim.x) v += a[i];
+    v = block_sum(v, sh);
+    if (threadIdx.x == 0)
+    {
+        partials[(int64_t)row * gridDim.x + blockIdx.x] = v;
+        __threadfence();
+        const unsigned t = atomicAdd(&counters[row], 1u);
+        last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double s = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) s += __ldcg(&partials[(int64_t)row * gridDim.x + i]);
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0)
+    {
+        out[row] = s;
+        counters[row] = 0u;
+    }
+}
+
+void launch_reduce_f(Problem& P, int n_rows, double* out)
+{
+    const int64_t n = P.n_elem_total;
+    int blocks = (int)std::min<int64_t>(RED_BLOCKS, std::max<int64_t>(1, (n + 4095) / 4096));
+    dim3 grid(blocks, n_rows);
+    k_reduce_rows<<<grid, RED_THREADS, 0, P.stream>>>(P.ef, n, n, P.partials, P.counters, out);
+}
+
+template <int d>
+__global__ void k_assemble_grad(int64_t nh, const int32_t* __restrict__ gptr, const int32_t* __restrict__ gidx,
+                                const double* __restrict__ eg, double* __restrict__ g)
+{
+    const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (u >= nh) return;
+    double acc[d];
+#pragma unroll
+    for (int p = 0; p < d; ++p) acc[p] = 0.0;
+    const int32_t q1 = gptr[u + 1];
+    for (int32_t q = gptr[u]; q < q1; ++q)
+    {
+        const int64_t s = gidx[q];
+#pragma unroll
+        for (int p = 0; p < d; ++p) acc[p] += eg[s * d + p];
+    }
+#pragma unroll
+    for (int p = 0; p < d; ++p) g[u * d + p] = acc[p];
+}
+
+void launch_assemble_grad(Problem& P)
+{
+    const unsigned grid = (unsigned)((P.n_handles + 255) / 256);
+    switch (P.d)
+    {
+    case 1: k_assemble_grad<1><<<grid, 256, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g); break;
+    case 2: k_assemble_grad<2><<<grid, 256, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g); break;
+    default: k_assemble_grad<3><<<grid, 256, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g); break;
+    }
+}
+
+template <int d, typename T>
+__global__ void k_assemble_hess(int64_t nb, const int32_t* __restrict__ cptr, const int32_t* __restrict__ cidx,
+                                const T* __restrict__ eH, T* __restrict__ H)
+{
+    const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    T acc[d * d];
+#pragma unroll
+    for (int i = 0; i < d * d; ++i) acc[i] = T(0);
+    const int32_t q1 = cptr[b + 1];
+    for (int32_t q = cptr[b]; q < q1; ++q)
+    {
+        const int32_t c = cidx[q];
+        const T* blk = eH + (int64_t)(c & 0x7fffffff) * (d * d);
+        T v[d * d];
+#pragma unroll
+        for (int i = 0; i < d * d; ++i) v[i] = blk[i];
+        if (c < 0)
+        {
+#pragma unroll
+            for (int p = 0; p < d; ++p)
+#pragma unroll
+                for (int r = 0; r < d; ++r) acc[p * d + r] += v[r * d + p];
+        }
+        else
+        {
+#pragma unroll
+            for (int i = 0; i < d * d; ++i) acc[i] += v[i];
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < d * d; ++i) H[b * (d * d) + i] = acc[i];
+}
+
+void launch_assemble_hess(Problem& P, int precision)
+{
+    const unsigned grid = (unsigned)((P.nb + 255) / 256);
+    if (P.nb == 0) return;
+#define TAD_ASM(D)                                                                                         \
+    if (precision == TAD_PREC_MIXED)                                                                       \
+        k_assemble_hess<D, float><<<grid, 256, 0, P.stream>>>(P.nb, P.cptr, P.cidx, (const float*)P.eH, (float*)P.H); \
+    else                                                                                                   \
+        k_assemble_hess<D, double><<<grid, 256, 0, P.stream>>>(P.nb, P.cptr, P.cidx, (const double*)P.eH, (double*)P.H);
+    switch (P.d)
+    {
+    case 1: TAD_ASM(1); break;
+    case 2: TAD_ASM(2); break;
+    default: TAD_ASM(3); break;
+    }
+#undef TAD_ASM
+}
+
+template <int d, typename T>
+__global__ void k_bsr_to_csr(int64_t nh, const int32_t* __restrict__ bptr, const T* __restrict__ H, double* __restrict__ out)
+{
+    const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (u >= nh) return;
+    const int32_t b0 = bptr[u];
+    const int32_t nbr = bptr[u + 1] - b0;
+    const int64_t base = (int64_t)d * d * b0;
+    for (int32_t j = 0; j < nbr; ++j)
+#pragma unroll
+        for (int p = 0; p < d; ++p)
+#pragma unroll
+            for (int q = 0; q < d; ++q)
+                out[base + (int64_t)p * d * nbr + j * d + q] = (double)H[(int64_t)(b0 + j) * d * d + p * d + q];
+}
+
+void launch_bsr_to_csr(Problem& P, double* out, int precision)
+{
+    const unsigned grid = (unsigned)((P.n_handles + 255) / 256);
+#define TAD_B2C(D)                                                                                      \
+    if (precision == TAD_PREC_MIXED)                                                                    \
+        k_bsr_to_csr<D, float><<<grid, 256, 0, P.stream>>>(P.n_handles, P.bptr, (const float*)P.H, out); \
+    else                                                                                                \
+        k_bsr_to_csr<D, double><<<grid, 256, 0, P.stream>>>(P.n_handles, P.bptr, (const double*)P.H, out);
+    switch (P.d)
+    {
+    case 1: TAD_B2C(1); break;
+    case 2: TAD_B2C(2); break;
+    default: TAD_B2C(3); break;
+    }
+#undef TAD_B2C
+}
+
+__global__ void k_zero(double* p, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = 0.0;
+}
+
+void launch_zero(double* p, int64_t n, cudaStream_t s)
+{
+    k_zero<<<RED_BLOCKS, RED_THREADS, 0, s>>>(p, n);
+}
+
+} // namespace tadlib

@@ -1,0 +1,669 @@
+/*
+ * Projected-Newton step on the device: linear solve + backtracking line
+ * search (the reference's newton_direction, include/TinyAD/Utils/
+ * NewtonDirection.hh:25-65, and line_search, include/TinyAD/Utils/
+ * LineSearch.hh:14-65, around the loop of tests/NewtonTest.cc:69-75).
+ *
+ * Linear solve.  The reference factorises H with Eigen's SimplicialLDLT; a
+ * serial sparse factorisation has no good GB300 mapping, so d = -(H + wI)^-1 g
+ * is solved by preconditioned conjugate gradients with a block-Jacobi
+ * preconditioner (inverted d x d diagonal blocks).  One iteration is three
+ * kernels over a fixed grid (RED_BLOCKS x RED_THREADS, grid-stride):
+ *   k_pcg_spmv    Ap = H p (BSR) fused with the p.Ap reduction; the last
+ *                 block computes alpha on the device
+ *   k_pcg_update  x += alpha p, r -= alpha Ap, z = M^-1 r fused with the r.z
+ *                 and r.r reductions; the last block computes beta and sets
+ *                 the convergence flag (|r| <= tol |b|) or the iteration cap
+ *   k_pcg_pupdate p = z + beta p
+ * Scalars never leave the device; every kernel returns at once when the flag
+ * is set, so chunks of iterations are captured once in a CUDA graph and
+ * replayed, with one host check per replay.  Reductions have a fixed order
+ * (bitwise reproducible).
+ *
+ * Mixed precision: H, the PCG vectors and the SpMV are FP32 (dot products are
+ * accumulated per thread in FP32 and combined in FP64); an FP64 iterative-
+ * refinement loop around it computes r = b - H d with FP64 accumulation and
+ * FP64 d, solving the FP32 system for the correction each pass.
+ *
+ * Line search.  Trial step sizes follow the reference's sequence (s_max,
+ * s *= shrink, snap to 1); the energy at x + s d is evaluated for a batch of
+ * trials in one launch per term (first batch 1 trial, then LS_BATCH), the
+ * first trial meeting the Armijo condition is accepted, as in the
+ * reference's sequential loop.
+ */
+#include <cmath>
+#include <vector>
+
+#include "internal.hh"
+
+namespace tadlib {
+
+__device__ __forceinline__ double warp_sum_d(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+/* fixed-order sum of NV values over the block; results valid in thread 0 */
+template <int NV>
+__device__ __forceinline__ void block_sum_n(double (&v)[NV], double (*sh)[32])
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) v[i] = warp_sum_d(v[i]);
+    if (lane == 0)
+#pragma unroll
+        for (int i = 0; i < NV; ++i) sh[i][w] = v[i];
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NV; ++i)
+    {
+        v[i] = 0.0;
+        if (w == 0)
+        {
+            v[i] = (lane < (int)(blockDim.x >> 5)) ? sh[i][lane] : 0.0;
+            v[i] = warp_sum_d(v[i]);
+        }
+    }
+    __syncthreads();
+}
+
+/* Grid-wide reduction of NV values: block partials, then the last block to
+   arrive sums them in block order.  Returns true in the last block, with the
+   totals in tot (all threads). */
+template <int NV>
+__device__ __forceinline__ bool grid_sum(double (&v)[NV], double* partials, unsigned* counter, double (&tot)[NV])
+{
+    __shared__ double sh[NV][32];
+    __shared__ bool last;
+    __shared__ double res[NV];
+    block_sum_n<NV>(v, sh);
+    if (threadIdx.x == 0)
+    {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) partials[i * gridDim.x + blockIdx.x] = v[i];
+        __threadfence();
+        const unsigned t = atomicAdd(counter, 1u);
+        last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double s[NV];
+#pragma unroll
+    for (int i = 0; i < NV; ++i)
+    {
+        s[i] = 0.0;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s[i] += __ldcg(&partials[i * gridDim.x + b]);
+    }
+    block_sum_n<NV>(s, sh);
+    if (threadIdx.x == 0)
+    {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) res[i] = s[i];
+        *counter = 0u;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NV; ++i) tot[i] = res[i];
+    return true;
+}
+
+#define GRID_STRIDE(i, n) for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (n); i += (int64_t)gridDim.x * blockDim.x)
+
+/* ---- block-Jacobi preconditioner: invert (H_uu + w I) ------------------- */
+template <int d, typename T>
+__global__ void k_diag_inv(int64_t nh, const int32_t* __restrict__ diag, const T* __restrict__ H, double w, T* __restrict__ dinv)
+{
+    GRID_STRIDE(u, nh)
+    {
+        double A[d * d];
+        const int32_t b = diag[u];
+#pragma unroll
+        for (int i = 0; i < d * d; ++i) A[i] = b >= 0 ? (double)H[(int64_t)b * d * d + i] : 0.0;
+#pragma unroll
+        for (int i = 0; i < d; ++i) A[i * d + i] += w;
+        double I[d * d];
+        double det;
+        if (d == 1) { det = A[0]; I[0] = 1.0 / A[0]; }
+        else if (d == 2)
+        {
+            det = A[0] * A[3] - A[1] * A[2];
+            const double id = 1.0 / det;
+            I[0] = A[3] * id; I[1] = -A[1] * id; I[2] = -A[2] * id; I[3] = A[0] * id;
+        }
+        else
+        {
+            const double c00 = A[4] * A[8] - A[5] * A[7], c01 = A[5] * A[6] - A[3] * A[8], c02 = A[3] * A[7] - A[4] * A[6];
+            det = A[0] * c00 + A[1] * c01 + A[2] * c02;
+            const double id = 1.0 / det;
+            I[0] = c00 * id; I[3] = c01 * id; I[6] = c02 * id;
+            I[1] = (A[2] * A[7] - A[1] * A[8]) * id; I[4] = (A[0] * A[8] - A[2] * A[6]) * id; I[7] = (A[1] * A[6] - A[0] * A[7]) * id;
+            I[2] = (A[1] * A[5] - A[2] * A[4]) * id; I[5] = (A[2] * A[3] - A[0] * A[5]) * id; I[8] = (A[0] * A[4] - A[1] * A[3]) * id;
+        }
+        const bool ok = det > 0.0 && isfinite(det);
+#pragma unroll
+        for (int i = 0; i < d; ++i)
+#pragma unroll
+            for (int j = 0; j < d; ++j)
+            {
+                double v = I[i * d + j];
+                if (!ok) v = (i == j && A[i * d + i] > 0.0) ? 1.0 / A[i * d + i] : (i == j ? 1.0 : 0.0);
+                dinv[u * d * d + i * d + j] = (T)v;
+            }
+    }
+}
+
+template <int d, typename T>
+__device__ __forceinline__ void apply_dinv(const T* __restrict__ dinv, int64_t u, const T (&r)[d], T (&z)[d])
+{
+#pragma unroll
+    for (int i = 0; i < d; ++i)
+    {
+        T acc = T(0);
+#pragma unroll
+        for (int j = 0; j < d; ++j) acc += dinv[u * d * d + i * d + j] * r[j];
+        z[i] = acc;
+    }
+}
+
+/* x = 0, r = b, z = M^-1 r, p = z; rz = r.z, bb = b.b */
+template <int d, typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_pcg_init(int64_t nh, const double* __restrict__ b, T* x, T* r, T* z, T* p,
+                                                          const T* __restrict__ dinv, double* partials, unsigned* counter,
+                                                          DevScalars* ds, double rel_tol, int max_iters)
+{
+    double part[2] = {0.0, 0.0};
+    GRID_STRIDE(u, nh)
+    {
+        T rv[d], zv[d];
+#pragma unroll
+        for (int i = 0; i < d; ++i) { rv[i] = (T)b[u * d + i]; x[u * d + i] = T(0); r[u * d + i] = rv[i]; }
+        apply_dinv<d, T>(dinv, u, rv, zv);
+#pragma unroll
+        for (int i = 0; i < d; ++i)
+        {
+            z[u * d + i] = zv[i];
+            p[u * d + i] = zv[i];
+            part[0] += (double)rv[i] * (double)zv[i];
+            part[1] += b[u * d + i] * b[u * d + i];
+        }
+    }
+    double tot[2];
+    if (!grid_sum<2>(part, partials, counter, tot)) return;
+    if (threadIdx.x == 0)
+    {
+        ds->rz = tot[0];
+        ds->bb = tot[1];
+        ds->rr = tot[1];
+        ds->tol2 = rel_tol * rel_tol * tot[1];
+        ds->iters = 0;
+        ds->breakdown = 0;
+        ds->done = (tot[1] == 0.0) ? 1 : 0;
+        ds->max_iters = max_iters;
+    }
+}
+
+template <int d, typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_pcg_spmv(int64_t nh, const int32_t* __restrict__ bptr, const int32_t* __restrict__ bcol,
+                                                          const T* __restrict__ H, const T* __restrict__ p, T* __restrict__ Ap,
+                                                          double* partials, unsigned* counter, DevScalars* ds)
+{
+    if (*(volatile int32_t*)&ds->done) return;
+    T part = T(0);
+    GRID_STRIDE(u, nh)
+    {
+        T y[d];
+#pragma unroll
+        for (int i = 0; i < d; ++i) y[i] = T(0);
+        const int32_t b1 = bptr[u + 1];
+        for (int32_t b = bptr[u]; b < b1; ++b)
+        {
+            const int64_t v = bcol[b];
+            T pv[d];
+#pragma unroll
+            for (int j = 0; j < d; ++j) pv[j] = p[v * d + j];
+            const T* B = H + (int64_t)b * d * d;
+#pragma unroll
+            for (int i = 0; i < d; ++i)
+#pragma unroll
+                for (int j = 0; j < d; ++j) y[i] += B[i * d + j] * pv[j];
+        }
+#pragma unroll
+        for (int i = 0; i < d; ++i)
+        {
+            Ap[u * d + i] = y[i];
+            part += p[u * d + i] * y[i];
+        }
+    }
+    double v[1] = {(double)part}, tot[1];
+    if (!grid_sum<1>(v, partials, counter, tot)) return;
+    if (threadIdx.x == 0)
+    {
+        ds->pAp = tot[0];
+        if (!(tot[0] > 0.0) || !isfinite(tot[0]))
+        {
+            ds->breakdown = 1;
+            ds->done = 1;
+            ds->alpha = 0.0;
+        }
+        else ds->alpha = ds->rz / tot[0];
+    }
+}
+
+template <int d, typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_pcg_update(int64_t nh, T* x, T* r, T* z, const T* __restrict__ p, const T* __restrict__ Ap,
+                                                            const T* __restrict__ dinv, double* partials, unsigned* counter, DevScalars* ds)
+{
+    if (*(volatile int32_t*)&ds->done) return;
+    const T alpha = (T)ds->alpha;
+    T part0 = T(0), part1 = T(0);
+    GRID_STRIDE(u, nh)
+    {
+        T rv[d], zv[d];
+#pragma unroll
+        for (int i = 0; i < d; ++i)
+        {
+            x[u * d + i] += alpha * p[u * d + i];
+            rv[i] = r[u * d + i] - alpha * Ap[u * d + i];
+            r[u * d + i] = rv[i];
+        }
+        apply_dinv<d, T>(dinv, u, rv, zv);
+#pragma unroll
+        for (int i = 0; i < d; ++i)
+        {
+            z[u * d + i] = zv[i];
+            part0 += rv[i] * zv[i];
+            part1 += rv[i] * rv[i];
+        }
+    }
+    double v[2] = {(double)part0, (double)part1}, tot[2];
+    if (!grid_sum<2>(v, partials, counter, tot)) return;
+    if (threadIdx.x == 0)
+    {
+        ds->beta = tot[0] / ds->rz;
+        ds->rz = tot[0];
+        ds->rr = tot[1];
+        ds->iters += 1;
+        if (tot[1] <= ds->tol2 || ds->iters >= ds->max_iters || !isfinite(tot[1])) ds->done = 1;
+    }
+}
+
+template <int d, typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_pcg_pupdate(int64_t n, const T* __restrict__ z, T* __restrict__ p, const DevScalars* ds)
+{
+    if (*(volatile const int32_t*)&ds->done) return;
+    const T beta = (T)ds->beta;
+    GRID_STRIDE(i, n) p[i] = z[i] + beta * p[i];
+}
+
+/* ---- vector helpers ------------------------------------------------------ */
+__global__ void k_neg(int64_t n, const double* __restrict__ a, double* __restrict__ out)
+{
+    GRID_STRIDE(i, n) out[i] = -a[i];
+}
+
+template <typename T>
+__global__ void k_to_double(int64_t n, const T* __restrict__ a, double* __restrict__ out, int accumulate)
+{
+    GRID_STRIDE(i, n) out[i] = (accumulate ? out[i] : 0.0) + (double)a[i];
+}
+
+/* res = b - (H + wI) y with FP64 accumulation; partial |res|^2 -> ds->rr */
+template <int d, typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_residual(int64_t nh, const int32_t* __restrict__ bptr, const int32_t* __restrict__ bcol,
+                                                          const T* __restrict__ H, double w, const double* __restrict__ y,
+                                                          const double* __restrict__ b, double* __restrict__ res,
+                                                          double* partials, unsigned* counter, DevScalars* ds)
+{
+    double part[1] = {0.0};
+    GRID_STRIDE(u, nh)
+    {
+        double acc[d];
+#pragma unroll
+        for (int i = 0; i < d; ++i) acc[i] = b[u * d + i] - w * y[u * d + i];
+        const int32_t b1 = bptr[u + 1];
+        for (int32_t bb = bptr[u]; bb < b1; ++bb)
+        {
+            const int64_t v = bcol[bb];
+            const T* B = H + (int64_t)bb * d * d;
+#pragma unroll
+            for (int i = 0; i < d; ++i)
+#pragma unroll
+                for (int j = 0; j < d; ++j) acc[i] -= (double)B[i * d + j] * y[v * d + j];
+        }
+#pragma unroll
+        for (int i = 0; i < d; ++i) { res[u * d + i] = acc[i]; part[0] += acc[i] * acc[i]; }
+    }
+    double tot[1];
+    if (!grid_sum<1>(part, partials, counter, tot)) return;
+    if (threadIdx.x == 0) ds->rr = tot[0];
+}
+
+/* dg = d.g, decrement = -0.5 dg */
+__global__ void __launch_bounds__(RED_THREADS) k_dot_dg(int64_t n, const double* __restrict__ a, const double* __restrict__ b,
+                                                        double* partials, unsigned* counter, DevScalars* ds)
+{
+    double part[1] = {0.0};
+    GRID_STRIDE(i, n) part[0] += a[i] * b[i];
+    double tot[1];
+    if (!grid_sum<1>(part, partials, counter, tot)) return;
+    if (threadIdx.x == 0) { ds->dg = tot[0]; ds->decrement = -0.5 * tot[0]; }
+}
+
+/* first trial j (of n) with f_trial[j] <= f + c s_j dg (LineSearch.hh:14-24, :53) */
+__global__ void k_ls_select(int n, const double* __restrict__ steps, double c, DevScalars* ds)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    ds->ls_choice = -1;
+    for (int j = 0; j < n; ++j)
+    {
+        const double fn = ds->f_trial[j];
+        if (fn != fn) { ds->ls_choice = -2; return; }   // NaN energy
+        if (fn <= ds->f + c * steps[j] * ds->dg)
+        {
+            ds->ls_choice = j;
+            ds->ls_f = fn;
+            ds->ls_s = steps[j];
+            return;
+        }
+    }
+}
+
+__global__ void k_axpy_ds(int64_t n, double* __restrict__ x, const double* __restrict__ dx, const DevScalars* ds)
+{
+    const double s = ds->ls_s;
+    GRID_STRIDE(i, n) x[i] += s * dx[i];
+}
+
+/* ------------------------------------------------------------------------ */
+/* host orchestration                                                        */
+/* ------------------------------------------------------------------------ */
+static tad_status fail(tad_status s, const std::string& m) { set_error(m); return s; }
+
+template <int d, typename T>
+static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double rel_tol, int max_iters, int* iters_out,
+                           T* r, T* z, T* p, T* Ap, T* dinv, int prec)
+{
+    const T* H = (const T*)P.H;
+    const int64_t nh = P.n_handles, n = P.n_vars;
+    cudaStream_t s = P.stream;
+    k_diag_inv<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, P.diag, H, w, dinv);
+    k_pcg_init<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, b, xs, r, z, p, dinv, P.partials, P.counters, P.ds, rel_tol, max_iters);
+    TAD_CUDA_TRY(cudaGetLastError());
+    // CHUNK iterations captured once per (precision, solution buffer)
+    constexpr int CHUNK = 8;
+    if (P.pcg_graph == nullptr || P.pcg_graph_prec != prec || P.pcg_graph_chunk != CHUNK || P.pcg_graph_x != (const void*)xs)
+    {
+        if (P.pcg_graph) { cudaGraphExecDestroy(P.pcg_graph); P.pcg_graph = nullptr; }
+        cudaGraph_t graph;
+        TAD_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        for (int it = 0; it < CHUNK; ++it)
+        {
+            k_pcg_spmv<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, P.bptr, P.bcol, H, p, Ap, P.partials, P.counters + 1, P.ds);
+            k_pcg_update<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, xs, r, z, p, Ap, dinv, P.partials, P.counters + 2, P.ds);
+            k_pcg_pupdate<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, z, p, P.ds);
+        }
+        TAD_CUDA_TRY(cudaStreamEndCapture(s, &graph));
+        TAD_CUDA_TRY(cudaGraphInstantiate(&P.pcg_graph, graph, 0));
+        cudaGraphDestroy(graph);
+        P.pcg_graph_prec = prec;
+        P.pcg_graph_chunk = CHUNK;
+        P.pcg_graph_x = (const void*)xs;
+    }
+    int replays_between_checks = 1;
+    for (;;)
+    {
+        for (int k = 0; k < replays_between_checks; ++k) TAD_CUDA_TRY(cudaGraphLaunch(P.pcg_graph, s));
+        TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
+        TAD_CUDA_TRY(cudaStreamSynchronize(s));
+        if (P.hs->done) break;
+        if (replays_between_checks < 8) replays_between_checks *= 2;
+    }
+    if (iters_out) *iters_out = P.hs->iters;
+    if (P.hs->breakdown) return TAD_ERR_PCG_NOCONV;
+    if (!(P.hs->rr <= P.hs->tol2)) return TAD_ERR_PCG_NOCONV;
+    return TAD_OK;
+}
+
+template <int d>
+static tad_status pcg_dispatch(Problem& P, const double* b, double* xsol, int precision, double rel_tol, int max_iters, int* iters)
+{
+    const int64_t n = P.n_vars;
+    cudaStream_t s = P.stream;
+    if (precision != TAD_PREC_MIXED)
+        return pcg_core<d, double>(P, b, xsol, 0.0, rel_tol, max_iters, iters, P.r, P.z, P.p, P.Ap, P.dinv, 0);
+    // mixed: FP64 iterative refinement around FP32 PCG
+    const double tol = P.settings.refine_rel_tol;
+    const double inner_tol = std::max(rel_tol, 1e-6);
+    launch_zero(xsol, n, s);
+    TAD_CUDA_TRY(cudaMemcpyAsync(P.res, b, n * 8, cudaMemcpyDeviceToDevice, s));
+    // |b|^2 for the outer criterion
+    k_residual<d, float><<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_handles, P.bptr, P.bcol, (const float*)P.H, 0.0, xsol, b, P.res,
+                                                            P.partials, P.counters + 3, P.ds);
+    TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
+    TAD_CUDA_TRY(cudaStreamSynchronize(s));
+    const double bb = P.hs->rr;
+    int total = 0;
+    tad_status st = TAD_OK;
+    const int passes = std::max(1, P.settings.refine_max_iters);
+    for (int pass = 0; pass < passes; ++pass)
+    {
+        int it = 0;
+        st = pcg_core<d, float>(P, P.res, P.dx32, 0.0, inner_tol, max_iters - total, &it, P.r32, P.z32, P.p32, P.Ap32, P.dinv32, 1);
+        total += it;
+        k_to_double<float><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, P.dx32, xsol, 1);
+        k_residual<d, float><<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_handles, P.bptr, P.bcol, (const float*)P.H, 0.0, xsol, b, P.res,
+                                                                P.partials, P.counters + 3, P.ds);
+        TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
+        TAD_CUDA_TRY(cudaStreamSynchronize(s));
+        if (P.hs->rr <= tol * tol * bb || total >= max_iters) break;
+        if (rel_tol >= inner_tol && P.hs->rr <= rel_tol * rel_tol * bb) break;
+    }
+    if (iters) *iters = total;
+    if (!(P.hs->rr <= rel_tol * rel_tol * bb * 1.0001) && !(P.hs->rr <= tol * tol * bb)) return TAD_ERR_PCG_NOCONV;
+    return st == TAD_ERR_PCG_NOCONV ? TAD_OK : st;
+}
+
+tad_status pcg_solve(Problem& P, const double* b, double* xsol, double w_identity, int precision, double rel_tol,
+                     int max_iters, int* iters_out)
+{
+    if (w_identity != 0.0) return fail(TAD_ERR_ARG, "w_identity must be 0 on the device path");
+    switch (P.d)
+    {
+    case 1: return pcg_dispatch<1>(P, b, xsol, precision, rel_tol, max_iters, iters_out);
+    case 2: return pcg_dispatch<2>(P, b, xsol, precision, rel_tol, max_iters, iters_out);
+    default: return pcg_dispatch<3>(P, b, xsol, precision, rel_tol, max_iters, iters_out);
+    }
+}
+
+/* reference step sequence (LineSearch.hh:41-59) */
+static void step_sequence(double s_max, double shrink, int n, std::vector<double>& out)
+{
+    const bool try_one = s_max > 1.0;
+    double s = s_max;
+    out.resize(n);
+    for (int i = 0; i < n; ++i)
+    {
+        out[i] = s;
+        if (try_one && s > 1.0 && s * shrink < 1.0) s = 1.0;
+        else s *= shrink;
+    }
+}
+
+tad_status line_search_device(Problem& P, double* x, const double* d, double f, double s_max, bool* found,
+                              double* f_out, int* trials)
+{
+    cudaStream_t s = P.stream;
+    const int max_iters = P.settings.ls_max_iters > 0 ? P.settings.ls_max_iters : 64;
+    std::vector<double> seq;
+    step_sequence(s_max, P.settings.ls_shrink, max_iters, seq);
+    k_dot_dg<<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_vars, d, P.g, P.partials, P.counters + 4, P.ds);
+    // current energy: caller provides it in ds->f
+    TAD_CUDA_TRY(cudaMemcpyAsync(&P.ds->f, &f, sizeof(double), cudaMemcpyHostToDevice, s));
+    *found = false;
+    int t0 = 0;
+    int batch = 1;
+    while (t0 < max_iters)
+    {
+        const int nb = std::min(batch, max_iters - t0);
+        TAD_CUDA_TRY(cudaMemcpyAsync(P.steps, seq.data() + t0, nb * sizeof(double), cudaMemcpyHostToDevice, s));
+        tad_status st = eval_elements(P, TAD_MODE_LINESEARCH, x, 0.0, TAD_PREC_FP64, d, nb);
+        if (st != TAD_OK) return st;
+        launch_reduce_f(P, nb, P.ds->f_trial);
+        k_ls_select<<<1, 32, 0, s>>>(nb, P.steps, P.settings.ls_armijo, P.ds);
+        TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
+        TAD_CUDA_TRY(cudaStreamSynchronize(s));
+        if (P.hs->ls_choice == -2) return fail(TAD_ERR_NONFINITE, "Assertion failed: f_new == f_new (NaN energy in line search)");
+        if (P.hs->ls_choice >= 0)
+        {
+            k_axpy_ds<<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_vars, x, d, P.ds);
+            *found = true;
+            if (f_out) *f_out = P.hs->ls_f;
+            if (trials) *trials = t0 + P.hs->ls_choice + 1;
+            return TAD_OK;
+        }
+        t0 += nb;
+        batch = LS_BATCH;
+    }
+    if (f_out) *f_out = f;
+    if (trials) *trials = max_iters;
+    return TAD_OK;
+}
+
+tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double stop_decrement, double* f_hist, int* iters_done)
+{
+    tad_status s = ensure_finalized(P);
+    if (s != TAD_OK) return s;
+    cudaStream_t st = P.stream;
+    const int prec = P.precision;
+    for (int i = 0; i < 4; ++i) P.ms_stage[i] = 0.0;
+    P.pcg_iters_total = 0;
+    P.ls_trials_total = 0;
+    double f = 0.0;
+    int it = 0;
+    for (; it < n_iters; ++it)
+    {
+        cudaEventRecord(P.ev[0], st);
+        s = eval_elements(P, TAD_MODE_HESSIAN_PROJ, x, eps, prec);
+        if (s != TAD_OK) return s;
+        cudaEventRecord(P.ev[1], st);
+        s = assemble(P, true, true, prec);
+        if (s != TAD_OK) return s;
+        k_neg<<<RED_BLOCKS, RED_THREADS, 0, st>>>(P.n_vars, P.g, P.rhs);
+        cudaEventRecord(P.ev[2], st);
+        s = check_device_error(P);
+        if (s != TAD_OK) return s;
+        TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, st));
+        TAD_CUDA_TRY(cudaStreamSynchronize(st));
+        f = P.hs->f;
+        if (f_hist) f_hist[it] = f;
+        int pit = 0;
+        s = pcg_solve(P, P.rhs, P.dx, 0.0, prec, P.settings.pcg_rel_tol, P.settings.pcg_max_iters, &pit);
+        P.pcg_iters_total += pit;
+        if (s != TAD_OK && s != TAD_ERR_PCG_NOCONV) return s;
+        cudaEventRecord(P.ev[3], st);
+        bool found = false;
+        double fn = f;
+        int trials = 0;
+        s = line_search_device(P, x, P.dx, f, 1.0, &found, &fn, &trials);
+        if (s != TAD_OK) return s;
+        cudaEventRecord(P.ev[4], st);
+        TAD_CUDA_TRY(cudaEventSynchronize(P.ev[4]));
+        float ms;
+        cudaEventElapsedTime(&ms, P.ev[0], P.ev[1]); P.ms_stage[0] += ms;
+        cudaEventElapsedTime(&ms, P.ev[1], P.ev[2]); P.ms_stage[1] += ms;
+        cudaEventElapsedTime(&ms, P.ev[2], P.ev[3]); P.ms_stage[2] += ms;
+        cudaEventElapsedTime(&ms, P.ev[3], P.ev[4]); P.ms_stage[3] += ms;
+        P.ls_trials_total += trials;
+        f = fn;
+        if (stop_decrement > 0.0 && P.hs->decrement < stop_decrement) { ++it; break; }
+        if (!found) { ++it; break; }
+    }
+    if (f_hist) f_hist[it] = f;
+    if (iters_done) *iters_done = it;
+    return TAD_OK;
+}
+
+} // namespace tadlib
+
+using namespace tadlib;
+
+extern "C" {
+
+TAD_API tad_status tad_newton_direction(tad_problem* P, const double* x_h, double eps, double w, double* d_h, double* f, double* g_h)
+{
+    if (!P || !x_h || !d_h) return fail(TAD_ERR_ARG, "NULL argument");
+    if (w != 0.0) return fail(TAD_ERR_ARG, "w_identity != 0 is not supported");
+    TAD_CUDA_TRY(cudaSetDevice(P->device));
+    tad_status s = ensure_finalized(*P);
+    if (s != TAD_OK) return s;
+    TAD_CUDA_TRY(cudaMemcpyAsync(P->x, x_h, P->n_vars * 8, cudaMemcpyHostToDevice, P->stream));
+    s = eval_full(*P, P->x, TAD_MODE_HESSIAN_PROJ, eps, P->precision);
+    if (s != TAD_OK) return s;
+    k_neg<<<RED_BLOCKS, RED_THREADS, 0, P->stream>>>(P->n_vars, P->g, P->rhs);
+    s = check_device_error(*P);
+    if (s != TAD_OK) return s;
+    int it = 0;
+    tad_status ps = pcg_solve(*P, P->rhs, P->dx, 0.0, P->precision, P->settings.pcg_rel_tol, P->settings.pcg_max_iters, &it);
+    if (ps != TAD_OK && ps != TAD_ERR_PCG_NOCONV) return ps;
+    TAD_CUDA_TRY(cudaMemcpyAsync(d_h, P->dx, P->n_vars * 8, cudaMemcpyDeviceToHost, P->stream));
+    if (g_h) TAD_CUDA_TRY(cudaMemcpyAsync(g_h, P->g, P->n_vars * 8, cudaMemcpyDeviceToHost, P->stream));
+    TAD_CUDA_TRY(cudaMemcpyAsync(P->hs, P->ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, P->stream));
+    TAD_CUDA_TRY(cudaStreamSynchronize(P->stream));
+    if (f) *f = P->hs->f;
+    P->pcg_iters_total = it;
+    if (ps == TAD_ERR_PCG_NOCONV) set_error("Linear solve did not reach its tolerance.");
+    return ps;
+}
+
+TAD_API tad_status tad_line_search(tad_problem* P, const double* x_h, const double* d_h, double f, const double* g_h,
+                                   double s_max, double* x_out_h, double* f_out)
+{
+    if (!P || !x_h || !d_h || !g_h || !x_out_h) return fail(TAD_ERR_ARG, "NULL argument");
+    if (s_max <= 0.0) return fail(TAD_ERR_ARG, "Max step size not positive.");
+    TAD_CUDA_TRY(cudaSetDevice(P->device));
+    tad_status s = ensure_finalized(*P);
+    if (s != TAD_OK) return s;
+    const int64_t n = P->n_vars;
+    TAD_CUDA_TRY(cudaMemcpyAsync(P->x, x_h, n * 8, cudaMemcpyHostToDevice, P->stream));
+    TAD_CUDA_TRY(cudaMemcpyAsync(P->dx, d_h, n * 8, cudaMemcpyHostToDevice, P->stream));
+    TAD_CUDA_TRY(cudaMemcpyAsync(P->g, g_h, n * 8, cudaMemcpyHostToDevice, P->stream));
+    bool found = false;
+    double fo = f;
+    int trials = 0;
+    s = line_search_device(*P, P->x, P->dx, f, s_max, &found, &fo, &trials);
+    if (s != TAD_OK) return s;
+    TAD_CUDA_TRY(cudaMemcpyAsync(x_out_h, P->x, n * 8, cudaMemcpyDeviceToHost, P->stream));
+    TAD_CUDA_TRY(cudaStreamSynchronize(P->stream));
+    if (f_out) *f_out = fo;
+    P->ls_trials_total = trials;
+    if (!found) { set_error("Line search couldn't find improvement."); return TAD_ERR_LS_FAIL; }
+    return TAD_OK;
+}
+
+TAD_API tad_status tad_newton_solve_d(tad_problem* P, double* x_d, int n_iters, double eps, double stop_decrement,
+                                      double* f_hist_h, int* iters_done)
+{
+    if (!P || !x_d) return fail(TAD_ERR_ARG, "NULL argument");
+    TAD_CUDA_TRY(cudaSetDevice(P->device));
+    return newton_solve(*P, x_d, n_iters, eps, stop_decrement, f_hist_h, iters_done);
+}
+
+TAD_API tad_status tad_newton_solve(tad_problem* P, double* x_h, int n_iters, double eps, double stop_decrement,
+                                    double* f_hist_h, int* iters_done)
+{
+    if (!P || !x_h) return fail(TAD_ERR_ARG, "NULL argument");
+    TAD_CUDA_TRY(cudaSetDevice(P->device));
+    tad_status s = ensure_finalized(*P);
+    if (s != TAD_OK) return s;
+    TAD_CUDA_TRY(cudaMemcpyAsync(P->x, x_h, P->n_vars * 8, cudaMemcpyHostToDevice, P->stream));
+    s = newton_solve(*P, P->x, n_iters, eps, stop_decrement, f_hist_h, iters_done);
+    if (s != TAD_OK) return s;
+    TAD_CUDA_TRY(cudaMemcpyAsync(x_h, P->x, P->n_vars * 8, cudaMemcpyDeviceToHost, P->stream));
+    TAD_CUDA_TRY(cudaStreamSynchronize(P->stream));
+    return TAD_OK;
+}
+
+} // extern "C"
