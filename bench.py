@@ -1,0 +1,351 @@
+#!/usr/bin/env python
+"""Benchmark: Projected-Newton iterations/s of the sparse per-element
+derivative path on one GB300 (TinyAD's eval_with_hessian_proj +
+newton_direction + line_search loop, tests/NewtonTest.cc:69-75).
+
+Default workload: the large mixed-precision parametrisation -- symmetric
+Dirichlet on a jittered, lifted disk from a 1024 x 1024 grid (1.64M faces,
+1.64M variables), Tutte initial UVs -- in mixed precision (FP32 element
+Hessians, projection and PCG; FP64 values, gradient, line-search energy and
+refinement).  One step = one Newton iteration (element eval + projection +
+assembly + PCG solve + line search) on the device-resident state.
+
+Also reported: the same loop in FP64 (the plain drop-in), element-Hessians/s,
+kernel roofline figures, an end-to-end figure through the C ABI with host
+buffers, and the CPU restatement of the reference path timed on this host.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload disk1024|disk64|tet48] [--precision mixed|fp64]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "Newton iters/s & element-Hessians/s, mixed vs FP64 GPU at 1e-8 energy err"
+UNIT = "Newton iters/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="disk1024")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison leg")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    return ap.parse_args()
+
+
+def make_workload(name: str, rank: int = 0):
+    from tinyad_gb300 import meshes
+    if name.startswith("disk"):
+        grid = int(name[4:])
+        return meshes.disk_param(grid, seed=2 + 1000 * rank, name=name)
+    if name.startswith("tet"):
+        return meshes.tet_twist(int(name[3:]), seed=1 + 1000 * rank, name=name)
+    raise SystemExit(f"unknown workload {name}")
+
+
+def workload_desc(w) -> str:
+    if w.name.startswith("disk"):
+        return (f"{w.name}: symmetric Dirichlet planar parametrisation of a jittered, lifted disk from a "
+                f"{w.info['grid']}x{w.info['grid']} grid ({w.info['n_faces']} faces, {w.info['n_verts']} vertices), "
+                f"Tutte initial UVs, k=6")
+    return (f"{w.name}: {w.info['cells']}^3 cube, 6 tets/cube ({w.info['n_tets']} tets, {w.info['n_verts']} vertices), "
+            f"symmetric Dirichlet k=12 + z=0 pin / z=1 45-degree twist penalties")
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    def __init__(self, index: int = 0):
+        self.proc = None
+        self.lines = []
+        self.index = index
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], None, set()
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(nm)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle (restatement of the reference's OpenMP path)
+# ---------------------------------------------------------------------------
+CPU_SAMPLE = "disk512"
+
+
+def cpu_baseline(full_w, threads: int | None = None) -> dict:
+    """One oracle Projected-Newton iteration (OpenMP element eval, serial
+    scatter + triplet sort, sparse LDL^T, Armijo) on the 512-grid disk of the
+    same family, scaled to the benchmark mesh by face count."""
+    from oracle import pyoracle
+    w = make_workload(CPU_SAMPLE)
+    nthreads = threads if threads else -1
+    p = pyoracle.Problem.from_workload(w, n_threads=nthreads)
+    t0 = time.perf_counter()
+    x, fh, times = p.newton(w.x0, 1)
+    dt = time.perf_counter() - t0
+    scale = w.n_elements / full_w.n_elements
+    return {"value": (1.0 / dt) * scale, "unit": UNIT, "cores": p.n_threads, "kind": "port",
+            "sample": (f"1 Projected-Newton iteration of the oracle (CPU restatement of the reference path: OpenMP "
+                       f"element eval + projection, serial triplet assembly, sparse LDL^T, Armijo) on {CPU_SAMPLE} "
+                       f"({w.n_elements} faces) = {dt:.2f} s, scaled by faces to {full_w.n_elements} faces "
+                       f"(linear scaling; the LDL^T grows faster, so this favours the CPU)"),
+            "stage_s": {"eval_assemble": times[0], "ldlt": times[1], "line_search": times[2]}}
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU path (its restatement in oracle/;
+    the reference itself needs Eigen 3, absent here) on all host threads."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import pyoracle
+    full = make_workload(args.workload)
+    w = make_workload(CPU_SAMPLE) if args.workload.startswith("disk") else full
+    threads = os.cpu_count() or 1
+    p = pyoracle.Problem.from_workload(w, n_threads=threads)
+    x = w.x0.copy()
+    for _ in range(args.warmup):
+        x, _, _ = p.newton(x, 1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        x, _, _ = p.newton(x, 1)
+    dt = time.perf_counter() - t0
+    scale = w.n_elements / full.n_elements
+    v = args.steps / dt * scale
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3 / scale,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": workload_desc(full)},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": p.n_threads, "kind": "port",
+                             "sample": f"{args.steps} oracle Newton iterations on {w.name} ({w.n_elements} elements), "
+                                       f"scaled by element count to {full.n_elements}"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+    import tinyad_gb300 as tad
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    prec = tad.PREC_MIXED if args.precision == "mixed" else tad.PREC_FP64
+    t_gen = time.perf_counter()
+    w = make_workload(args.workload, rank)
+    t_gen = time.perf_counter() - t_gen
+    settings = dict(pcg_rel_tol=1e-6, pcg_max_iters=2000, forcing=1, refine_max_iters=3, refine_rel_tol=1e-8)
+
+    def make_fn(p):
+        fn = tad.ScalarFunction.from_workload(w, precision=p, **settings)
+        fn.finalize()
+        return fn
+
+    fn = make_fn(prec)
+    stream = torch.cuda.ExternalStream(fn.stream_ptr)
+    x = torch.from_numpy(w.x0.copy()).cuda()
+
+    # warm-up
+    fn.newton_solve_device(x.data_ptr(), args.warmup)
+    torch.cuda.synchronize()
+    barrier()
+
+    # timed region: K Newton iterations on the device-resident state
+    launches0 = fn.launch_count
+    stage = {"ms_eval": 0.0, "ms_assemble": 0.0, "ms_pcg": 0.0, "ms_linesearch": 0.0, "pcg_iters": 0, "ls_trials": 0}
+    fh = []
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fh.append(fn.newton_solve_device(x.data_ptr(), 1))
+            st = fn.last_solve_stats()
+            for k in stage:
+                stage[k] += st[k]
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+    launches = fn.launch_count - launches0
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * args.steps / (ms / 1e3)
+    ms_elem_stage = stage["ms_eval"] + stage["ms_assemble"]
+    elem_hess_per_s = world * w.n_elements * args.steps / (ms_elem_stage / 1e3) if ms_elem_stage > 0 else None
+
+    # kernel figures at the final state (CUDA events on the library stream)
+    prof = fn.profile_kernels(x.data_ptr(), reps=5)
+    nb = fn.hessian_pattern()[1].size // (w.var_dim ** 2)
+    n = w.n_vars
+    vb = 4 if prec == tad.PREC_MIXED else 8
+    spmv_bytes = nb * (w.var_dim ** 2 * vb + 4) + (w.n_handles + 1) * 4 + 3 * n * vb
+    pcg_ms = stage["pcg_iters"] * (prof["spmv"] + prof["pcg_update"])
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    hbm_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    spmv_gbs = spmv_bytes / (prof["spmv"] * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": "k_pcg_spmv (BSR SpMV fused with p.Ap)", "achieved": spmv_gbs,
+                "peak": hbm, "unit": "GB/s", "frac": spmv_gbs / hbm, "traffic": None,
+                "peak_source": f"{hbm_src} copy bandwidth (MEASURED_PEAKS.json hbm_gbs)",
+                "algorithmic_bytes_per_launch": spmv_bytes,
+                "ms_per_launch": prof["spmv"],
+                "share_of_step_est": pcg_ms * prof["spmv"] / max(prof["spmv"] + prof["pcg_update"], 1e-12) / ms}
+    fp_peak = tad.measure_fma_peak(prec)
+    kernels = {k: round(v, 5) for k, v in prof.items()}
+
+    # end to end through the C ABI with host buffers (pinned), one step per call
+    xh = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    xh.copy_(x.cpu())
+    xh_np = xh.numpy()
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        fn.newton_solve_inplace(xh_np, 1)
+    t_e2e = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([t_e2e], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    e2e = {"value": world * args.steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n + 8,
+           "path": "tad_newton_solve (C ABI) with pinned host x in and out every step"}
+
+    # FP64 plain path on the same workload (the drop-in), same protocol
+    fp64 = None
+    if not args.no_fp64 and prec == tad.PREC_MIXED:
+        fd = make_fn(tad.PREC_FP64)
+        xd = torch.from_numpy(w.x0.copy()).cuda()
+        fd.newton_solve_device(xd.data_ptr(), args.warmup)
+        k64 = max(2, min(args.steps, 4))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fd.newton_solve_device(xd.data_ptr(), k64)
+        torch.cuda.synchronize()
+        t64 = time.perf_counter() - t0
+        st64 = fd.last_solve_stats()
+        prof64 = fd.profile_kernels(xd.data_ptr(), reps=2)
+        fp64 = {"value": k64 / t64, "unit": UNIT, "steps": k64,
+                "element_hessians_per_s": w.n_elements * k64 / ((st64["ms_eval"] + st64["ms_assemble"]) / 1e3),
+                "pcg_iters_per_step": st64["pcg_iters"] / k64,
+                "kernels_ms": {k: round(v, 5) for k, v in prof64.items()},
+                "fp64_fma_peak_tflops": tad.measure_fma_peak(tad.PREC_FP64)}
+        del fd
+
+    cpu = None
+    if not args.no_cpu and rank == 0 and world == 1:
+        cpu = cpu_baseline(w)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 Hessian/PCG + f64 value/gradient" if prec == tad.PREC_MIXED else "f64",
+        "data": "synthetic (seeded generator)",
+        "config": {"workload": workload_desc(w), "precision": args.precision,
+                   "n_vars": n, "n_elements": w.n_elements, "hessian_nnz": int(nb * w.var_dim ** 2),
+                   "newton": "projected Newton, eps=1e-9, inexact PCG (block Jacobi, tol_k = max(1e-6, "
+                             "min(0.5, sqrt(|g_k|/|g_0|))), <= 2000 iters), Armijo line search (0.8, 1e-4, 64)",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "l2": "working set per step (element blocks, BSR Hessian, vectors) larger than L2",
+                   "mesh_generation_s": round(t_gen, 2)},
+        "element_hessians_per_s": elem_hess_per_s,
+        "stages_ms_per_step": {k: (v / args.steps if k.startswith("ms") else v / args.steps) for k, v in stage.items()},
+        "kernels_ms_per_launch": kernels,
+        "fp_pipe_peak_tflops": fp_peak,
+        "f_history": [float(a[0]) for a in fh] + [float(fh[-1][-1])],
+        "roofline": roofline,
+        "e2e": e2e,
+        "fp64_path": fp64,
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+        "gpu_launches": int(launches),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

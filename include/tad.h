@@ -105,6 +105,11 @@ typedef struct tad_settings {
     int ls_max_iters;         /* line search trials (reference default 64) */
     double ls_shrink;         /* 0.8 */
     double ls_armijo;         /* 1e-4 */
+    int forcing;              /* Newton loop: 0 = fixed pcg_rel_tol; 1 = inexact
+                                 Newton, tol_k = max(pcg_rel_tol,
+                                 min(0.5, sqrt(|g_k| / |g_0|))), g_0 = the
+                                 gradient at the first Newton iteration after
+                                 tad_problem_create / tad_problem_set_settings */
     int verbose;
 } tad_settings;
 
@@ -200,10 +205,12 @@ TAD_API tad_status tad_eval_with_hessian_proj_d(tad_problem* p, const double* x_
                                                 double proj_eps, double* f,
                                                 double* g_d, double* H_values_d);
 
-/* d = -(H + w I)^-1 g with H the PSD-projected Hessian at x (block-Jacobi PCG
-   on the device).  Returns TAD_ERR_PCG_NOCONV if the tolerance is not met
-   (d then holds the last iterate). */
-TAD_API tad_status tad_newton_direction(tad_problem* p, const double* x_h,
+/* d = -(H + w I)^-1 g with H the Hessian at x -- PSD-projected with proj_eps
+   if `projected` (eval_with_hessian_proj), else exact (eval_with_derivatives)
+   -- solved by block-Jacobi PCG on the device (w_identity must be 0).
+   Returns TAD_ERR_PCG_NOCONV if the tolerance is not met (d then holds the
+   last iterate). */
+TAD_API tad_status tad_newton_direction(tad_problem* p, const double* x_h, int projected,
                                         double proj_eps, double w_identity,
                                         double* d_h, double* f, double* g_h);
 
@@ -225,6 +232,27 @@ TAD_API tad_status tad_newton_solve(tad_problem* p, double* x_h, int n_iters,
 TAD_API tad_status tad_newton_solve_d(tad_problem* p, double* x_d, int n_iters,
                                       double proj_eps, double stop_decrement,
                                       double* f_hist_h, int* iters_done);
+
+/* Adjoint: gradient of a loss L(x*) with respect to the 3D rest positions
+   (n_handles x 3, host) of the built-in symmetric Dirichlet triangle terms,
+   x* being a minimiser (x_h).  Solves H lambda = dL/dx (dLdx_h) with the
+   PCG (H projected with proj_eps if `projected`, else the exact Hessian),
+   then dL/drest = -(d2E/dx drest)^T lambda with per-element mixed second
+   derivatives recomputed on the device.  lambda_h (n_vars) and pcg_iters
+   are optional outputs.  No reference counterpart: the reference offers the
+   building block (block-restricted Hessians, Scalar.hh:24) but no adjoint. */
+TAD_API tad_status tad_adjoint_rest_gradient(tad_problem* p, const double* x_h, const double* dLdx_h,
+                                             const double* rest_h, int projected, double proj_eps,
+                                             double* dLdrest_h, double* lambda_h, int* pcg_iters);
+
+/* Time the main kernels once each at x_d (device), averaged over reps
+   launches with CUDA events on the problem's stream: ms5 = [element Hessian
+   kernels, gradient + Hessian assembly, one PCG SpMV, one PCG vector update,
+   one line-search energy evaluation]. */
+TAD_API tad_status tad_profile_kernels(tad_problem* p, const double* x_d, int reps, double* ms5);
+
+/* Cumulative number of CUDA kernels the problem has launched. */
+TAD_API tad_status tad_launch_count(tad_problem* p, int64_t* n);
 
 /* The CUDA stream (cudaStream_t) all work of the problem is issued on. */
 TAD_API tad_status tad_get_stream(tad_problem* p, void** stream);

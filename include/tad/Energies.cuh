@@ -150,3 +150,37 @@ struct DirichletTri
 };
 
 } // namespace tad
+
+namespace tad {
+
+/* Symmetric Dirichlet of one triangle as a function of its UVs (a, b, c)
+   and of its 3D rest positions (Pa, Pb, Pc): the rest edge matrix is the
+   triangle in its own orthonormal frame, Mr = [[l, e.f/l], [0, |e x f|/l]]
+   with e = Pb - Pa, f = Pc - Pa, l = |e|, and the weight is the rest area
+   |e x f| / 2 -- the same formulas that produce the [Mr, w] parameters of
+   SymmetricDirichletTri.  Used by the adjoint (mixed second derivatives
+   d2E/dx dP); S is any scalar type (double, tad::MixedScalar, ...). */
+template <typename S>
+TAD_HD S symmetric_dirichlet_tri_rest(const Vec<S, 2>& a, const Vec<S, 2>& b, const Vec<S, 2>& c,
+                                      const Vec<S, 3>& Pa, const Vec<S, 3>& Pb, const Vec<S, 3>& Pc)
+{
+    using std::sqrt;
+    const Vec<S, 3> e = Pb - Pa;
+    const Vec<S, 3> f = Pc - Pa;
+    const S l = sqrt(dot(e, e));
+    Vec<S, 3> n;
+    n[0] = e[1] * f[2] - e[2] * f[1];
+    n[1] = e[2] * f[0] - e[0] * f[2];
+    n[2] = e[0] * f[1] - e[1] * f[0];
+    const S an = sqrt(dot(n, n));
+    Mat<S, 2, 2> Mr;
+    Mr(0, 0) = l;
+    Mr(1, 0) = S(0.0);
+    Mr(0, 1) = dot(e, f) / l;
+    Mr(1, 1) = an / l;
+    const Mat<S, 2, 2> M = col_mat(b - a, c - a);
+    if (to_passive(determinant(M)) <= 0.0) return S(INFINITY);
+    return ((M * inverse(Mr)).squaredNorm() + (Mr * inverse(M)).squaredNorm()) * (an * 0.5);
+}
+
+} // namespace tad

@@ -608,6 +608,8 @@ TAD_TPL TAD_HD TAD_M sqrt(const TAD_M& a)
     return TAD_M::chain(f, T(0.5) / f, T(-0.25) / (f * a.val), a);
 }
 TAD_TPL TAD_HD TAD_M sqr(const TAD_M& a) { return a * a; }
+TAD_TPLU TAD_HD TAD_M operator+(U s, const TAD_M& a) { return a + s; }
+TAD_TPLU TAD_HD TAD_M operator-(U s, const TAD_M& a) { return (-a) + s; }
 TAD_TPLU TAD_HD bool operator<=(const TAD_M& a, U b) { return a.val <= T(b); }
 TAD_TPL TAD_HD T to_passive(const TAD_M& a) { return a.val; }
 #undef TAD_TPLU

@@ -778,6 +778,7 @@ static void ldl_solve(const Problem& p, const double* b, double* x)
 // newton_direction (NewtonDirection.hh:25-48): d = -(H + wI)^-1 g
 static void newton_direction(Problem& p, const std::vector<double>& g, double w, std::vector<double>& d)
 {
+    if (p.outer.size() != (size_t)p.n_vars + 1) throw std::runtime_error("no assembled Hessian: call eval_with_hessian_proj first");
     if (!p.ldl_ready || p.pattern_outer != p.outer || p.pattern_inner != p.inner) ldl_symbolic(p);
     ldl_numeric(p, w);
     std::vector<double> mg(g.size());
@@ -996,6 +997,84 @@ __attribute__((visibility("default"))) int oracle_scalar_op(int op, const double
     }
     out[0] = r.val; out[1] = r.grad[0]; out[2] = r.hess[0];
     return 0;
+}
+
+} // extern "C"
+
+// Rest-parameterised symmetric Dirichlet of one triangle (UVs a, b, c and 3D
+// rest positions Pa, Pb, Pc): the rest edge matrix in the triangle's own
+// frame, weight = rest area.
+template <typename S>
+static S symdir_tri_rest(const std::array<S, 6>& u, const std::array<S, 9>& P)
+{
+    std::array<S, 3> e, f, n;
+    for (int i = 0; i < 3; ++i) { e[i] = P[3 + i] - P[i]; f[i] = P[6 + i] - P[i]; }
+    const S l = sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+    n[0] = e[1] * f[2] - e[2] * f[1];
+    n[1] = e[2] * f[0] - e[0] * f[2];
+    n[2] = e[0] * f[1] - e[1] * f[0];
+    const S an = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    Mat<S, 2, 2> Mr;
+    Mr(0, 0) = l; Mr(1, 0) = S(0.0); Mr(0, 1) = (e[0] * f[0] + e[1] * f[1] + e[2] * f[2]) / l; Mr(1, 1) = an / l;
+    Mat<S, 2, 2> M;
+    M(0, 0) = u[2] - u[0]; M(1, 0) = u[3] - u[1]; M(0, 1) = u[4] - u[0]; M(1, 1) = u[5] - u[1];
+    if (value_of(det2(M)) <= 0.0) return S(INFINITY);
+    Mat<S, 2, 2> Mri = inv2(Mr), Mi = inv2(M);
+    Mat<S, 2, 2> J, K;
+    for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j)
+        {
+            J(i, j) = M(i, 0) * Mri(0, j) + M(i, 1) * Mri(1, j);
+            K(i, j) = Mr(i, 0) * Mi(0, j) + Mr(i, 1) * Mi(1, j);
+        }
+    return (squared_norm(J) + squared_norm(K)) * (an * 0.5);
+}
+
+extern "C" {
+
+// dL/d(rest) = -(d2E/dx dP)^T lambda with H lambda = dLdx (LDL^T), mixed blocks
+// from AD<15> restricted to the x-rows / P-columns block.
+__attribute__((visibility("default"))) int oracle_adjoint_rest_gradient(void* pp, const double* x, const double* dLdx,
+                                                                        const double* rest, int projected, double eps,
+                                                                        double* out, double* lambda)
+{
+    ORACLE_TRY(
+        Problem& p = *(Problem*)pp;
+        double f;
+        std::vector<double> g;
+        eval_derivs(p, x, true, projected != 0, eps, f, g);
+        std::vector<double> b(dLdx, dLdx + p.n_vars), lam;
+        // newton_direction solves H d = -g: pass -b to get lambda = H^-1 b
+        for (double& v : b) v = -v;
+        newton_direction(p, b, 0.0, lam);
+        if (lambda) std::memcpy(lambda, lam.data(), sizeof(double) * p.n_vars);
+        std::fill(out, out + 3 * p.n_handles, 0.0);
+        using S = AD<15, double, 0, 6, 6, 9>;
+        for (const Term& t : p.terms)
+        {
+            if (t.energy != TAD_ENERGY_SYMMETRIC_DIRICHLET_TRI) continue;
+            for (int64_t e = 0; e < t.n_elem; ++e)
+            {
+                const int* h = &t.handles[e * 3];
+                std::array<S, 6> u;
+                std::array<S, 9> P;
+                for (int a = 0; a < 3; ++a)
+                {
+                    for (int i = 0; i < 2; ++i) u[2 * a + i] = S(x[2 * h[a] + i], 2 * a + i);
+                    for (int i = 0; i < 3; ++i) P[3 * a + i] = S(rest[3 * h[a] + i], 6 + 3 * a + i);
+                }
+                const S E = symdir_tri_rest(u, P);
+                if (!std::isfinite(E.val)) continue;
+                for (int j = 0; j < 9; ++j)
+                {
+                    double c = 0.0;
+                    for (int i = 0; i < 6; ++i) c -= E.H(i, j) * lam[2 * h[i / 2] + (i % 2)];
+                    out[3 * h[j / 3] + (j % 3)] += c;
+                }
+            }
+        }
+        return 0;
+    )
 }
 
 } // extern "C"

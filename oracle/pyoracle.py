@@ -47,6 +47,7 @@ def lib():
         L.oracle_line_search.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double, _dp, ctypes.c_double, _dp, _dp]
         L.oracle_newton.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_double, _dp, _dp]
         L.oracle_n_threads.argtypes = [ctypes.c_void_p]
+        L.oracle_adjoint_rest_gradient.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, ctypes.c_int, ctypes.c_double, _dp, _dp]
         for name in ("oracle_scalar_unary", "oracle_scalar_binary"):
             if hasattr(L, name):
                 pass
@@ -134,6 +135,8 @@ class Problem:
         return self._hessian(x, True, eps)
 
     def newton_direction(self, g, w: float = 0.0):
+        """d = -(H + wI)^-1 g for the Hessian of the last eval_with_hessian_proj /
+        eval_with_derivatives call."""
         g = np.ascontiguousarray(g, np.float64)
         d = np.zeros(self.n_vars)
         self._check(self.L.oracle_newton_direction(self.h, _d(g), w, _d(d)))
@@ -147,6 +150,16 @@ class Problem:
         fo = np.zeros(1)
         rc = self._check(self.L.oracle_line_search(self.h, _d(x), _d(d), f, _d(g), s_max, _d(xo), _d(fo)))
         return xo, float(fo[0]), rc == 0
+
+    def adjoint_rest_gradient(self, x, dLdx, rest, projected: bool = True, eps: float = 1e-9):
+        """dL/d(rest positions) by an LDL^T adjoint solve and AD<15> mixed blocks."""
+        x, dLdx = np.ascontiguousarray(x, np.float64), np.ascontiguousarray(dLdx, np.float64)
+        rest = np.ascontiguousarray(rest, np.float64).reshape(-1)
+        out = np.zeros(rest.size)
+        lam = np.zeros(self.n_vars)
+        self._check(self.L.oracle_adjoint_rest_gradient(self.h, _d(x), _d(dLdx), _d(rest), int(projected), eps,
+                                                        _d(out), _d(lam)))
+        return out.reshape(-1, 3), lam
 
     def newton(self, x, iters: int, eps: float = 1e-9):
         """Projected Newton as in tests/NewtonTest.cc:69-75; returns (x, f_hist, times)."""

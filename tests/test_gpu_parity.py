@@ -205,6 +205,7 @@ def test_line_search_api(tad, oracle):
     w = meshes.disk_param(20, seed=6)
     fn, p = _pair(tad, oracle, w)
     f, g, H = fn.eval_with_hessian_proj(w.x0)
+    p.eval_with_hessian_proj(w.x0)
     d = p.newton_direction(g)
     x_gpu = fn.line_search(w.x0, d, f, g)
     x_cpu, _, ok = p.line_search(w.x0, d, f, g)

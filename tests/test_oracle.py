@@ -185,3 +185,43 @@ def test_bad_handle_raises(oracle):
     p.add_elements(meshes.TAD_ENERGY_POSITION_PENALTY, np.array([[5]]), np.array([[0.0, 0.0, 1.0]]))
     with pytest.raises(oracle.OracleError):
         p.eval(np.zeros(6))
+
+
+def test_newton_direction_needs_hessian(oracle):
+    w = meshes.planar_test_mesh()
+    p = oracle.Problem.from_workload(w)
+    with pytest.raises(oracle.OracleError):
+        p.newton_direction(np.zeros(w.n_vars))
+
+
+def _converge(oracle, w, x, iters=40):
+    """Projected Newton, then two full Newton steps on the exact Hessian (PD at
+    the minimum): the Armijo search stalls once the energy decrease drops
+    below FP64 resolution, the full steps converge quadratically past it."""
+    p = oracle.Problem.from_workload(w)
+    x, fh, _ = p.newton(x, iters)
+    for _ in range(2):
+        f, g, H = p.eval_with_derivatives(x)
+        x = x + p.newton_direction(g)
+    return x, p
+
+
+def test_adjoint_matches_fd(oracle):
+    """Oracle adjoint dL/d(rest) (LDL^T solve + AD<15> block-restricted mixed
+    derivatives, ScalarTestHessianBlock.cc) against central differences of
+    re-solved minimisers."""
+    w = meshes.disk_param_pinned(10, seed=3)
+    xs, p = _converge(oracle, w, w.x0)
+    rng = np.random.default_rng(7)
+    target = xs + rng.normal(scale=0.01, size=xs.size)
+    L = lambda x: 0.5 * np.sum((x - target) ** 2)  # noqa: E731
+    grad, lam = p.adjoint_rest_gradient(xs, xs - target, w.rest, projected=False)
+    h = 1e-5
+    for _ in range(3):
+        dP = rng.normal(size=w.rest.shape)
+        dP /= np.linalg.norm(dP)
+        xp, _ = _converge(oracle, meshes.with_rest(w, w.rest + h * dP), xs, 8)
+        xm, _ = _converge(oracle, meshes.with_rest(w, w.rest - h * dP), xs, 8)
+        fd = (L(xp) - L(xm)) / (2 * h)
+        an = float(np.sum(grad * dP))
+        assert abs(fd - an) <= 1e-6 * max(abs(fd), 1e-3), (fd, an)

@@ -46,7 +46,7 @@ class Settings(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("pcg_max_iters", ctypes.c_int), ("pcg_rel_tol", ctypes.c_double),
                 ("refine_max_iters", ctypes.c_int), ("refine_rel_tol", ctypes.c_double),
                 ("ls_max_iters", ctypes.c_int), ("ls_shrink", ctypes.c_double), ("ls_armijo", ctypes.c_double),
-                ("verbose", ctypes.c_int)]
+                ("forcing", ctypes.c_int), ("verbose", ctypes.c_int)]
 
 
 class TinyADError(RuntimeError):
@@ -64,7 +64,8 @@ EXPORTS = [
     "tad_hessian_nnz", "tad_hessian_pattern", "tad_eval", "tad_eval_with_gradient", "tad_eval_with_derivatives",
     "tad_eval_with_hessian_proj", "tad_eval_d", "tad_eval_with_hessian_proj_d", "tad_newton_direction",
     "tad_line_search", "tad_newton_solve", "tad_newton_solve_d", "tad_last_solve_stats", "tad_debug_scalar_op",
-    "tad_get_stream", "tad_measure_fma_peak",
+    "tad_get_stream", "tad_measure_fma_peak", "tad_profile_kernels",
+    "tad_launch_count", "tad_adjoint_rest_gradient",
 ]
 
 
@@ -98,7 +99,7 @@ def load(build_if_missing: bool = True):
     L.tad_eval_d.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _dp]
     L.tad_eval_with_hessian_proj_d.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, _dp,
                                                ctypes.c_void_p, ctypes.c_void_p]
-    L.tad_newton_direction.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double, ctypes.c_double, _dp, _dp, _dp]
+    L.tad_newton_direction.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_double, ctypes.c_double, _dp, _dp, _dp]
     L.tad_line_search.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double, _dp, ctypes.c_double, _dp, _dp]
     L.tad_newton_solve.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_double, ctypes.c_double, _dp,
                                    ctypes.POINTER(ctypes.c_int)]
@@ -108,6 +109,10 @@ def load(build_if_missing: bool = True):
     L.tad_debug_scalar_op.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
     L.tad_get_stream.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]
     L.tad_measure_fma_peak.argtypes = [ctypes.c_int, _dp]
+    L.tad_profile_kernels.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, _dp]
+    L.tad_launch_count.argtypes = [ctypes.c_void_p, _i64p]
+    L.tad_adjoint_rest_gradient.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, ctypes.c_int, ctypes.c_double, _dp, _dp,
+                                            ctypes.POINTER(ctypes.c_int)]
     _lib = L
     return L
 
@@ -270,13 +275,14 @@ class ScalarFunction:
         return float(f[0]), g, self._csr(vals)
 
     # ---- solver utilities ----------------------------------------------------
-    def newton_direction(self, x, projection_eps: float = default_hessian_projection_eps):
-        """d = -H_proj(x)^-1 g(x) (device PCG).  Returns (d, f, g)."""
+    def newton_direction(self, x, projection_eps: float = default_hessian_projection_eps, projected: bool = True):
+        """d = -H(x)^-1 g(x) (device PCG), H projected (default) or exact.
+        Returns (d, f, g)."""
         x = self._x(x)
         d = np.zeros(self.n_vars)
         g = np.zeros(self.n_vars)
         f = np.zeros(1)
-        self._check(self.L.tad_newton_direction(self.h, _d(x), projection_eps, 0.0, _d(d), _d(f), _d(g)),
+        self._check(self.L.tad_newton_direction(self.h, _d(x), int(projected), projection_eps, 0.0, _d(d), _d(f), _d(g)),
                     allow=(TAD_ERR_PCG_NOCONV,))
         return d, float(f[0]), g
 
@@ -299,6 +305,18 @@ class ScalarFunction:
                                             ctypes.byref(done)))
         return x, fh[:done.value + 1]
 
+    def newton_solve_inplace(self, x: np.ndarray, n_iters: int,
+                             projection_eps: float = default_hessian_projection_eps, stop_decrement: float = 0.0):
+        """Like newton_solve, updating the caller's float64 host array in place
+        (no extra copies; pass pinned memory for fast transfers)."""
+        if x.dtype != np.float64 or not x.flags["C_CONTIGUOUS"] or x.size != self.n_vars:
+            raise TinyADError(TAD_ERR_ARG, "x must be a contiguous float64 array of n_vars entries")
+        fh = np.zeros(n_iters + 1)
+        done = ctypes.c_int(0)
+        self._check(self.L.tad_newton_solve(self.h, _d(x), n_iters, projection_eps, stop_decrement, _d(fh),
+                                            ctypes.byref(done)))
+        return fh[:done.value + 1]
+
     @property
     def stream_ptr(self) -> int:
         s = ctypes.c_void_p()
@@ -313,6 +331,34 @@ class ScalarFunction:
         self._check(self.L.tad_newton_solve_d(self.h, ctypes.c_void_p(x_ptr), n_iters, projection_eps, stop_decrement,
                                               _d(fh), ctypes.byref(done)))
         return fh[:done.value + 1]
+
+    def adjoint_rest_gradient(self, x, dLdx, rest, projected: bool = True,
+                              projection_eps: float = default_hessian_projection_eps):
+        """dL/d(rest positions) at a minimiser x for dL/dx given (adjoint
+        solve + mixed second derivatives).  Returns (dL/drest (n_handles, 3),
+        lambda, pcg_iters)."""
+        x, dLdx = self._x(x), self._x(dLdx)
+        rest = _f64(rest).reshape(-1)
+        if rest.size != 3 * self.n_handles:
+            raise TinyADError(TAD_ERR_ARG, "rest must hold n_handles x 3 positions")
+        out = np.zeros(3 * self.n_handles)
+        lam = np.zeros(self.n_vars)
+        it = ctypes.c_int(0)
+        self._check(self.L.tad_adjoint_rest_gradient(self.h, _d(x), _d(dLdx), _d(rest), int(projected), projection_eps,
+                                                     _d(out), _d(lam), ctypes.byref(it)), allow=(TAD_ERR_PCG_NOCONV,))
+        return out.reshape(-1, 3), lam, it.value
+
+    @property
+    def launch_count(self) -> int:
+        n = np.zeros(1, np.int64)
+        self._check(self.L.tad_launch_count(self.h, n.ctypes.data_as(_i64p)))
+        return int(n[0])
+
+    def profile_kernels(self, x_ptr: int, reps: int = 5) -> dict:
+        """Per-launch ms of the main kernels at device x (CUDA events)."""
+        ms = np.zeros(5)
+        self._check(self.L.tad_profile_kernels(self.h, ctypes.c_void_p(x_ptr), reps, _d(ms)))
+        return {"elem_hessian": ms[0], "assemble": ms[1], "spmv": ms[2], "pcg_update": ms[3], "ls_energy": ms[4]}
 
     def last_solve_stats(self) -> dict:
         ms = np.zeros(4)

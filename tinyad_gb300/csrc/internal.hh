@@ -77,6 +77,7 @@ struct DevScalars
     double ls_f;         // accepted energy
     double ls_s;         // accepted step
     double decrement;    // -0.5 d.g
+    double gg;           // g.g
 };
 
 struct Problem
@@ -131,6 +132,8 @@ struct Problem
     // stats of the last solve
     double ms_stage[4] = {0, 0, 0, 0};
     int64_t pcg_iters_total = 0, ls_trials_total = 0;
+    double g0_norm = 0.0;      // |g| at the first iteration of the last solve
+    int64_t n_launches = 0;    // kernels launched by this problem (cumulative)
     cudaEvent_t ev[8] = {};
     bool timing = false;
 };

@@ -294,6 +294,7 @@ tad_status eval_elements(Problem& P, int mode, const double* x, double eps, int 
         tad_status s = T.energy >= 0 ? launch_builtin(P, T, a)
                                      : (T.fn(T.user, &a) == 0 ? TAD_OK : fail(TAD_ERR_ARG, "custom term failed"));
         if (s != TAD_OK) return s;
+        if (T.n_elem > 0) P.n_launches += 1;
     }
     TAD_CUDA_TRY(cudaGetLastError());
     return TAD_OK;
@@ -304,6 +305,7 @@ tad_status assemble(Problem& P, bool gradient, bool hessian, int precision)
     launch_reduce_f(P, 1, &P.ds->f);
     if (gradient) launch_assemble_grad(P);
     if (hessian) launch_assemble_hess(P, precision);
+    P.n_launches += 1 + (gradient ? 1 : 0) + (hessian ? 1 : 0);
     TAD_CUDA_TRY(cudaGetLastError());
     return TAD_OK;
 }
@@ -338,6 +340,7 @@ TAD_API void tad_settings_default(tad_settings* s)
     s->ls_max_iters = 64;
     s->ls_shrink = 0.8;
     s->ls_armijo = 1e-4;
+    s->forcing = 0;
     s->verbose = 0;
 }
 
@@ -402,6 +405,7 @@ TAD_API tad_status tad_problem_set_settings(tad_problem* P, const tad_settings* 
     if (!P || !s) return fail(TAD_ERR_ARG, "NULL argument");
     P->settings = *s;
     P->precision = s->precision;
+    P->g0_norm = 0.0;
     return TAD_OK;
 }
 
@@ -542,6 +546,13 @@ TAD_API tad_status tad_eval_d(tad_problem* P, const double* x_d, double* f)
 TAD_API tad_status tad_eval_with_hessian_proj_d(tad_problem* P, const double* x_d, double eps, double* f, double* g_d, double* H_d)
 {
     return eval_host(P, x_d, TAD_MODE_HESSIAN_PROJ, eps, f, g_d, H_d, true);
+}
+
+TAD_API tad_status tad_launch_count(tad_problem* P, int64_t* n)
+{
+    if (!P || !n) return fail(TAD_ERR_ARG, "NULL argument");
+    *n = P->n_launches;
+    return TAD_OK;
 }
 
 TAD_API tad_status tad_get_stream(tad_problem* P, void** stream)

@@ -352,6 +352,16 @@ __global__ void __launch_bounds__(RED_THREADS) k_dot_dg(int64_t n, const double*
     if (threadIdx.x == 0) { ds->dg = tot[0]; ds->decrement = -0.5 * tot[0]; }
 }
 
+__global__ void __launch_bounds__(RED_THREADS) k_dot_gg(int64_t n, const double* __restrict__ a,
+                                                        double* partials, unsigned* counter, DevScalars* ds)
+{
+    double part[1] = {0.0};
+    GRID_STRIDE(i, n) part[0] += a[i] * a[i];
+    double tot[1];
+    if (!grid_sum<1>(part, partials, counter, tot)) return;
+    if (threadIdx.x == 0) ds->gg = tot[0];
+}
+
 /* first trial j (of n) with f_trial[j] <= f + c s_j dg (LineSearch.hh:14-24, :53) */
 __global__ void k_ls_select(int n, const double* __restrict__ steps, double c, DevScalars* ds)
 {
@@ -391,6 +401,7 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
     cudaStream_t s = P.stream;
     k_diag_inv<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, P.diag, H, w, dinv);
     k_pcg_init<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, b, xs, r, z, p, dinv, P.partials, P.counters, P.ds, rel_tol, max_iters);
+    P.n_launches += 2;
     TAD_CUDA_TRY(cudaGetLastError());
     // CHUNK iterations captured once per (precision, solution buffer)
     constexpr int CHUNK = 8;
@@ -416,6 +427,7 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
     for (;;)
     {
         for (int k = 0; k < replays_between_checks; ++k) TAD_CUDA_TRY(cudaGraphLaunch(P.pcg_graph, s));
+        P.n_launches += 3 * CHUNK * replays_between_checks;
         TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
         TAD_CUDA_TRY(cudaStreamSynchronize(s));
         if (P.hs->done) break;
@@ -442,6 +454,7 @@ static tad_status pcg_dispatch(Problem& P, const double* b, double* xsol, int pr
     // |b|^2 for the outer criterion
     k_residual<d, float><<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_handles, P.bptr, P.bcol, (const float*)P.H, 0.0, xsol, b, P.res,
                                                             P.partials, P.counters + 3, P.ds);
+    P.n_launches += 2;
     TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
     TAD_CUDA_TRY(cudaStreamSynchronize(s));
     const double bb = P.hs->rr;
@@ -454,6 +467,7 @@ static tad_status pcg_dispatch(Problem& P, const double* b, double* xsol, int pr
         st = pcg_core<d, float>(P, P.res, P.dx32, 0.0, inner_tol, max_iters - total, &it, P.r32, P.z32, P.p32, P.Ap32, P.dinv32, 1);
         total += it;
         k_to_double<float><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, P.dx32, xsol, 1);
+        P.n_launches += 2;
         k_residual<d, float><<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_handles, P.bptr, P.bcol, (const float*)P.H, 0.0, xsol, b, P.res,
                                                                 P.partials, P.counters + 3, P.ds);
         TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
@@ -500,6 +514,7 @@ tad_status line_search_device(Problem& P, double* x, const double* d, double f, 
     std::vector<double> seq;
     step_sequence(s_max, P.settings.ls_shrink, max_iters, seq);
     k_dot_dg<<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_vars, d, P.g, P.partials, P.counters + 4, P.ds);
+    P.n_launches += 1;
     // current energy: caller provides it in ds->f
     TAD_CUDA_TRY(cudaMemcpyAsync(&P.ds->f, &f, sizeof(double), cudaMemcpyHostToDevice, s));
     *found = false;
@@ -513,12 +528,14 @@ tad_status line_search_device(Problem& P, double* x, const double* d, double f, 
         if (st != TAD_OK) return st;
         launch_reduce_f(P, nb, P.ds->f_trial);
         k_ls_select<<<1, 32, 0, s>>>(nb, P.steps, P.settings.ls_armijo, P.ds);
+        P.n_launches += 2;
         TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
         TAD_CUDA_TRY(cudaStreamSynchronize(s));
         if (P.hs->ls_choice == -2) return fail(TAD_ERR_NONFINITE, "Assertion failed: f_new == f_new (NaN energy in line search)");
         if (P.hs->ls_choice >= 0)
         {
             k_axpy_ds<<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_vars, x, d, P.ds);
+            P.n_launches += 1;
             *found = true;
             if (f_out) *f_out = P.hs->ls_f;
             if (trials) *trials = t0 + P.hs->ls_choice + 1;
@@ -552,6 +569,8 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
         s = assemble(P, true, true, prec);
         if (s != TAD_OK) return s;
         k_neg<<<RED_BLOCKS, RED_THREADS, 0, st>>>(P.n_vars, P.g, P.rhs);
+        k_dot_gg<<<RED_BLOCKS, RED_THREADS, 0, st>>>(P.n_vars, P.g, P.partials, P.counters + 5, P.ds);
+        P.n_launches += 2;
         cudaEventRecord(P.ev[2], st);
         s = check_device_error(P);
         if (s != TAD_OK) return s;
@@ -559,8 +578,13 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
         TAD_CUDA_TRY(cudaStreamSynchronize(st));
         f = P.hs->f;
         if (f_hist) f_hist[it] = f;
+        const double gnorm = std::sqrt(P.hs->gg);
+        if (P.g0_norm == 0.0) P.g0_norm = gnorm;   // first iteration since create / set_settings
+        double tol = P.settings.pcg_rel_tol;
+        if (P.settings.forcing == 1 && P.g0_norm > 0.0)
+            tol = std::max(tol, std::min(0.5, std::sqrt(gnorm / P.g0_norm)));
         int pit = 0;
-        s = pcg_solve(P, P.rhs, P.dx, 0.0, prec, P.settings.pcg_rel_tol, P.settings.pcg_max_iters, &pit);
+        s = pcg_solve(P, P.rhs, P.dx, 0.0, prec, tol, P.settings.pcg_max_iters, &pit);
         P.pcg_iters_total += pit;
         if (s != TAD_OK && s != TAD_ERR_PCG_NOCONV) return s;
         cudaEventRecord(P.ev[3], st);
@@ -592,7 +616,8 @@ using namespace tadlib;
 
 extern "C" {
 
-TAD_API tad_status tad_newton_direction(tad_problem* P, const double* x_h, double eps, double w, double* d_h, double* f, double* g_h)
+TAD_API tad_status tad_newton_direction(tad_problem* P, const double* x_h, int projected, double eps, double w,
+                                        double* d_h, double* f, double* g_h)
 {
     if (!P || !x_h || !d_h) return fail(TAD_ERR_ARG, "NULL argument");
     if (w != 0.0) return fail(TAD_ERR_ARG, "w_identity != 0 is not supported");
@@ -600,7 +625,7 @@ TAD_API tad_status tad_newton_direction(tad_problem* P, const double* x_h, doubl
     tad_status s = ensure_finalized(*P);
     if (s != TAD_OK) return s;
     TAD_CUDA_TRY(cudaMemcpyAsync(P->x, x_h, P->n_vars * 8, cudaMemcpyHostToDevice, P->stream));
-    s = eval_full(*P, P->x, TAD_MODE_HESSIAN_PROJ, eps, P->precision);
+    s = eval_full(*P, P->x, projected ? TAD_MODE_HESSIAN_PROJ : TAD_MODE_HESSIAN, eps, P->precision);
     if (s != TAD_OK) return s;
     k_neg<<<RED_BLOCKS, RED_THREADS, 0, P->stream>>>(P->n_vars, P->g, P->rhs);
     s = check_device_error(*P);
@@ -641,6 +666,74 @@ TAD_API tad_status tad_line_search(tad_problem* P, const double* x_h, const doub
     P->ls_trials_total = trials;
     if (!found) { set_error("Line search couldn't find improvement."); return TAD_ERR_LS_FAIL; }
     return TAD_OK;
+}
+
+/* Time the main kernels once each at the current state (CUDA events on the
+   problem's stream): [0] element Hessian kernels (all terms, current
+   precision, projected), [1] Hessian + gradient assembly, [2] one PCG SpMV,
+   [3] one PCG update, [4] line-search energy for one trial step. */
+TAD_API tad_status tad_profile_kernels(tad_problem* P, const double* x_d, int reps, double* ms5)
+{
+    if (!P || !x_d || !ms5 || reps < 1) return fail(TAD_ERR_ARG, "bad argument");
+    TAD_CUDA_TRY(cudaSetDevice(P->device));
+    tad_status s = ensure_finalized(*P);
+    if (s != TAD_OK) return s;
+    Problem& Q = *P;
+    cudaStream_t st = Q.stream;
+    const int prec = Q.precision;
+    // a valid state: Hessian at x, a search direction p = z = D^-1 g
+    s = eval_full(Q, x_d, TAD_MODE_HESSIAN_PROJ, 1e-9, prec);
+    if (s != TAD_OK) return s;
+    k_neg<<<RED_BLOCKS, RED_THREADS, 0, st>>>(Q.n_vars, Q.g, Q.rhs);
+    cudaEvent_t e0 = Q.ev[5], e1 = Q.ev[6];
+    float ms = 0.f;
+    auto timed = [&](auto&& launch) -> double {
+        launch();   // warm
+        cudaEventRecord(e0, st);
+        for (int r = 0; r < reps; ++r) launch();
+        cudaEventRecord(e1, st);
+        cudaEventSynchronize(e1);
+        cudaEventElapsedTime(&ms, e0, e1);
+        return (double)ms / reps;
+    };
+    ms5[0] = timed([&] { eval_elements(Q, TAD_MODE_HESSIAN_PROJ, x_d, 1e-9, prec); });
+    ms5[1] = timed([&] { launch_assemble_grad(Q); launch_assemble_hess(Q, prec); });
+    const int64_t nh = Q.n_handles, n = Q.n_vars;
+#define TAD_PROF(D)                                                                                                  \
+    if (prec == TAD_PREC_MIXED)                                                                                     \
+    {                                                                                                               \
+        k_diag_inv<D, float><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.diag, (const float*)Q.H, 0.0, Q.dinv32);     \
+        k_pcg_init<D, float><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.rhs, Q.dx32, Q.r32, Q.z32, Q.p32, Q.dinv32,  \
+                                                                 Q.partials, Q.counters, Q.ds, 1e-30, 1 << 30);     \
+        ms5[2] = timed([&] { k_pcg_spmv<D, float><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.bptr, Q.bcol,          \
+                               (const float*)Q.H, Q.p32, Q.Ap32, Q.partials, Q.counters + 1, Q.ds); });               \
+        ms5[3] = timed([&] { k_pcg_update<D, float><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.dx32, Q.r32, Q.z32,  \
+                               Q.p32, Q.Ap32, Q.dinv32, Q.partials, Q.counters + 2, Q.ds); });                       \
+    }                                                                                                               \
+    else                                                                                                            \
+    {                                                                                                               \
+        k_diag_inv<D, double><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.diag, (const double*)Q.H, 0.0, Q.dinv);     \
+        k_pcg_init<D, double><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.rhs, Q.dx, Q.r, Q.z, Q.p, Q.dinv,           \
+                                                                  Q.partials, Q.counters, Q.ds, 1e-30, 1 << 30);    \
+        ms5[2] = timed([&] { k_pcg_spmv<D, double><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.bptr, Q.bcol,         \
+                               (const double*)Q.H, Q.p, Q.Ap, Q.partials, Q.counters + 1, Q.ds); });                  \
+        ms5[3] = timed([&] { k_pcg_update<D, double><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.dx, Q.r, Q.z,       \
+                               Q.p, Q.Ap, Q.dinv, Q.partials, Q.counters + 2, Q.ds); });                             \
+    }
+    switch (Q.d)
+    {
+    case 1: TAD_PROF(1); break;
+    case 2: TAD_PROF(2); break;
+    default: TAD_PROF(3); break;
+    }
+#undef TAD_PROF
+    // keep the PCG kernels from early-exiting: done was cleared by k_pcg_init with an unreachable tolerance
+    const double one = 1.0;
+    TAD_CUDA_TRY(cudaMemcpyAsync(Q.steps, &one, sizeof(double), cudaMemcpyHostToDevice, st));
+    ms5[4] = timed([&] { eval_elements(Q, TAD_MODE_LINESEARCH, x_d, 0.0, TAD_PREC_FP64, Q.rhs, 1); });
+    TAD_CUDA_TRY(cudaStreamSynchronize(st));
+    TAD_CUDA_TRY(cudaGetLastError());
+    return check_device_error(Q);
 }
 
 TAD_API tad_status tad_newton_solve_d(tad_problem* P, double* x_d, int n_iters, double eps, double stop_decrement,

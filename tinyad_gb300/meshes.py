@@ -215,6 +215,31 @@ def disk_param(grid: int, seed: int = 0, jitter: float = 0.2, lift: bool = True,
     return w
 
 
+def disk_param_pinned(grid: int, seed: int = 0, pin_weight: float = 10.0, name: str | None = None) -> Workload:
+    """disk_param plus position penalties on two opposite boundary vertices
+    (at their initial UVs), which remove the rigid-motion null space so the
+    minimiser x*(rest) is unique -- the adjoint workload."""
+    w = disk_param(grid, seed=seed, name=name or f"disk{grid}_pinned")
+    loop = w.info["boundary"]
+    pins = np.array([loop[0], loop[len(loop) // 2]], np.int32)
+    uv = w.x0.reshape(-1, 2)
+    pp = np.column_stack([uv[pins], np.full(2, pin_weight)])
+    w.terms.append(Term(TAD_ENERGY_POSITION_PENALTY, 1, pins[:, None].copy(), pp))
+    w.info["pins"] = pins
+    return w
+
+
+def with_rest(w: Workload, P: np.ndarray) -> Workload:
+    """The same triangle workload with rest positions P (params recomputed)."""
+    terms = []
+    for t in w.terms:
+        if t.energy == TAD_ENERGY_SYMMETRIC_DIRICHLET_TRI:
+            terms.append(Term(t.energy, t.valence, t.handles, tri_rest_params(P, t.handles)))
+        else:
+            terms.append(t)
+    return Workload(w.name, w.var_dim, w.n_handles, w.x0.copy(), terms, rest=P, faces=w.faces, info=w.info)
+
+
 # ---------------------------------------------------------------------------
 # tet twist
 # ---------------------------------------------------------------------------
