@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison leg")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--kernels-only", action="store_true",
+                    help="profile the main kernels once at the initial state (for ncu captures) and exit")
     return ap.parse_args()
 
 
@@ -218,6 +220,11 @@ def main():
     fn = make_fn(prec)
     stream = torch.cuda.ExternalStream(fn.stream_ptr)
     x = torch.from_numpy(w.x0.copy()).cuda()
+    if args.kernels_only:
+        prof = fn.profile_kernels(x.data_ptr(), reps=3)
+        if rank == 0:
+            print(json.dumps({"kernels_ms_per_launch": prof, "workload": workload_desc(w), "precision": args.precision}))
+        return
 
     # warm-up
     fn.newton_solve_device(x.data_ptr(), args.warmup)
