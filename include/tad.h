@@ -281,6 +281,25 @@ TAD_API tad_status tad_debug_scalar_op(int op, int precision, const double* a3,
    denominator of the element kernels. */
 TAD_API tad_status tad_measure_fma_peak(int precision, double* tflops);
 
+/* Total symmetric Dirichlet energy of a triangle parametrisation, for
+   callers that cannot allocate device memory (code running while another
+   component captures a CUDA graph, hosts whose memory pool forbids outside
+   allocations, real-time loops that cannot take an allocation's implicit
+   synchronisation).  Inputs and output are the caller's device buffers:
+   x_d (2 * n_vertices doubles, interleaved UVs), faces_d (n_faces x 3
+   int32), params_d (n_faces x 5 doubles, as TAD_ENERGY_SYMMETRIC_DIRICHLET_TRI),
+   f_d (1 double); stream is a cudaStream_t (NULL = default stream).  The
+   result equals tad_eval on the same term up to summation-order rounding.
+   Allocates nothing: its reduction scratch is a fixed 513 KiB device array
+   in the library, so n_faces is limited to 16,777,216 (larger sizes return
+   TAD_ERR_ARG).  The first call on each device looks up that array's
+   address (make it before any stream capture); every call shares the array,
+   so calls that overlap on the GPU race.  No counterpart in the reference:
+   TinyAD runs on the CPU and allocates per evaluation. */
+TAD_API tad_status tad_eval_symmetric_dirichlet_tri_noalloc(const double* x_d, const int32_t* faces_d,
+                                                           const double* params_d, int64_t n_faces,
+                                                           double* f_d, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -65,7 +65,7 @@ EXPORTS = [
     "tad_eval_with_hessian_proj", "tad_eval_d", "tad_eval_with_hessian_proj_d", "tad_newton_direction",
     "tad_line_search", "tad_newton_solve", "tad_newton_solve_d", "tad_last_solve_stats", "tad_debug_scalar_op",
     "tad_get_stream", "tad_measure_fma_peak", "tad_profile_kernels",
-    "tad_launch_count", "tad_adjoint_rest_gradient",
+    "tad_launch_count", "tad_adjoint_rest_gradient", "tad_eval_symmetric_dirichlet_tri_noalloc",
 ]
 
 
@@ -111,6 +111,8 @@ def load(build_if_missing: bool = True):
     L.tad_measure_fma_peak.argtypes = [ctypes.c_int, _dp]
     L.tad_profile_kernels.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, _dp]
     L.tad_launch_count.argtypes = [ctypes.c_void_p, _i64p]
+    L.tad_eval_symmetric_dirichlet_tri_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                           ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]
     L.tad_adjoint_rest_gradient.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, ctypes.c_int, ctypes.c_double, _dp, _dp,
                                             ctypes.POINTER(ctypes.c_int)]
     _lib = L
