@@ -1,0 +1,294 @@
+/*
+ * tad/ScalarFunction.cuh -- C++17 front end with TinyAD's spelling:
+ *
+ *   auto func = tad::scalar_function<2>(tad::range(n_vertices));
+ *   func.add_elements<3>(tad::range(n_faces), [=] __device__ (auto& element) {
+ *       using T = TAD_SCALAR_TYPE(element);
+ *       ...
+ *       if (det <= 0.0) return T(INFINITY);
+ *       return energy;                       // every branch returns a T
+ *   });
+ *   auto [f, g, H] = func.eval_with_hessian_proj(x);
+ *
+ * (include/TinyAD/ScalarFunction.hh:57-248, Detail/ScalarFunctionImpl.hh).
+ * The element functor runs on the device only: a generic __device__ lambda
+ * (nvcc --extended-lambda) or a struct with a templated operator(),
+ * capturing device pointers and PODs.  Two nvcc limits shape the lambda
+ * form: generic __host__ __device__ extended lambdas are rejected, and a
+ * trailing return type that depends on the generic parameter (the
+ * reference's `-> TINYAD_SCALAR_TYPE(element)`) breaks nvcc's host stub, so
+ * the lambda deduces its return type and every branch returns T(...).  It is instantiated here, in the user's
+ * translation unit, by the kernels of tad/ElementKernels.cuh and handed to
+ * the library (libtad.so, include/tad.h) as a term callback; the library
+ * records each element's first-access handle order once, builds the sparsity
+ * pattern and runs assembly, PCG and line search.  Results come back in host
+ * std::vectors; the Hessian as CSR arrays (identical to Eigen's CSC arrays
+ * for the symmetric H).  Errors throw std::runtime_error as the reference's
+ * TINYAD_ERROR_throw does.
+ */
+#pragma once
+#include <cuda_runtime.h>
+
+#include <array>
+#include <functional>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <tuple>
+#include <utility>
+#include <vector>
+
+#include "../tad.h"
+#include "ElementKernels.cuh"
+
+namespace tad {
+
+inline void check(tad_status s)
+{
+    if (s != TAD_OK) throw std::runtime_error(tad_last_error_message());
+}
+
+inline void check_cuda(cudaError_t e)
+{
+    if (e != cudaSuccess) throw std::runtime_error(std::string("CUDA error: ") + cudaGetErrorString(e));
+}
+
+/* TinyAD::range(n) (include/TinyAD/Utils/Helpers.hh:17-27) */
+struct IndexRange
+{
+    int64_t n;
+    struct It
+    {
+        int64_t i;
+        int64_t operator*() const { return i; }
+        It& operator++() { ++i; return *this; }
+        bool operator!=(const It& o) const { return i != o.i; }
+    };
+    It begin() const { return {0}; }
+    It end() const { return {n}; }
+    int64_t size() const { return n; }
+};
+inline IndexRange range(int64_t n) { return {n}; }
+
+/* sparse matrix returned by the eval functions: CSR (== CSC of the symmetric H) */
+struct SparseCSR
+{
+    int64_t rows = 0;
+    std::vector<int32_t> outer, inner;
+    std::vector<double> values;
+    int64_t nonZeros() const { return (int64_t)values.size(); }
+    double coeff(int64_t r, int64_t c) const
+    {
+        for (int32_t q = outer[r]; q < outer[r + 1]; ++q)
+            if (inner[q] == c) return values[q];
+        return 0.0;
+    }
+};
+
+namespace detail {
+
+struct TermBase
+{
+    virtual ~TermBase() = default;
+    virtual int launch(const tad_term_eval_args* a) = 0;
+};
+
+/* passes the user's element handle (from the range) instead of the index */
+template <typename F>
+struct HandleMapped
+{
+    F f;
+    const int32_t* handles;
+    template <typename El>
+    __device__ auto operator()(El& element) const
+    {
+        const int64_t e = element.handle;
+        element.handle = handles[e];
+        auto r = f(element);
+        element.handle = e;
+        return r;
+    }
+};
+
+template <int d, int N, typename F>
+struct Term : TermBase
+{
+    HandleMapped<F> fn;
+    explicit Term(HandleMapped<F> f) : fn(std::move(f)) {}
+    int launch(const tad_term_eval_args* a) override
+    {
+        tad::launch_elements<d, N>(a->mode, a->precision, make_launch(*a), fn, (cudaStream_t)a->stream);
+        return cudaGetLastError() == cudaSuccess ? 0 : 1;
+    }
+};
+
+inline int term_callback(void* user, const tad_term_eval_args* a)
+{
+    try { return static_cast<TermBase*>(user)->launch(a); }
+    catch (...) { return 1; }
+}
+
+} // namespace detail
+
+template <int d>
+class ScalarFunction
+{
+public:
+    using VecD = std::array<double, d>;
+
+    explicit ScalarFunction(int64_t n_handles, const tad_settings* settings = nullptr) : n_handles_(n_handles)
+    {
+        check(tad_problem_create(d, n_handles, settings, &p_));
+    }
+    ~ScalarFunction()
+    {
+        if (p_) tad_problem_destroy(p_);
+        for (int32_t* h : handle_bufs_) cudaFree(h);
+    }
+    ScalarFunction(const ScalarFunction&) = delete;
+    ScalarFunction& operator=(const ScalarFunction&) = delete;
+    ScalarFunction(ScalarFunction&& o) noexcept { swap(o); }
+    ScalarFunction& operator=(ScalarFunction&& o) noexcept { swap(o); return *this; }
+
+    int64_t n_vars() const { return d * n_handles_; }
+    tad_problem* handle() { return p_; }
+
+    /* add_elements<N>(range, functor) (ScalarFunctionImpl.hh:63-100) */
+    template <int N, typename Range, typename F>
+    void add_elements(const Range& elements, F functor)
+    {
+        std::vector<int32_t> h;
+        for (auto eh : elements) h.push_back((int32_t)eh);
+        int32_t* hd = nullptr;
+        check_cuda(cudaMalloc(&hd, std::max<size_t>(h.size(), 1) * sizeof(int32_t)));
+        handle_bufs_.push_back(hd);
+        if (!h.empty()) check_cuda(cudaMemcpy(hd, h.data(), h.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+        auto term = std::make_unique<detail::Term<d, N, F>>(detail::HandleMapped<F>{functor, hd});
+        check(tad_add_elements_custom(p_, N, (int64_t)h.size(), &detail::term_callback, term.get()));
+        terms_.push_back(std::move(term));
+    }
+
+    /* x_from_data / x_to_data (ScalarFunctionImpl.hh:216-254) */
+    std::vector<double> x_from_data(const std::function<VecD(int64_t)>& read) const
+    {
+        std::vector<double> x(n_vars());
+        for (int64_t v = 0; v < n_handles_; ++v)
+        {
+            const VecD p = read(v);
+            for (int i = 0; i < d; ++i) x[d * v + i] = p[i];
+        }
+        return x;
+    }
+    void x_to_data(const std::vector<double>& x, const std::function<void(int64_t, const VecD&)>& write) const
+    {
+        for (int64_t v = 0; v < n_handles_; ++v)
+        {
+            VecD p;
+            for (int i = 0; i < d; ++i) p[i] = x[d * v + i];
+            write(v, p);
+        }
+    }
+
+    double eval(const std::vector<double>& x) const
+    {
+        double f;
+        check(tad_eval(p_, x.data(), &f));
+        return f;
+    }
+    double operator()(const std::vector<double>& x) const { return eval(x); }
+
+    std::tuple<double, std::vector<double>> eval_with_gradient(const std::vector<double>& x) const
+    {
+        double f;
+        std::vector<double> g(n_vars());
+        check(tad_eval_with_gradient(p_, x.data(), &f, g.data()));
+        return {f, std::move(g)};
+    }
+
+    std::tuple<double, std::vector<double>, SparseCSR> eval_with_derivatives(const std::vector<double>& x) const
+    {
+        double f;
+        std::vector<double> g(n_vars());
+        SparseCSR H = pattern();
+        check(tad_eval_with_derivatives(p_, x.data(), &f, g.data(), H.values.data()));
+        return {f, std::move(g), std::move(H)};
+    }
+
+    SparseCSR eval_hessian(const std::vector<double>& x) const { return std::get<2>(eval_with_derivatives(x)); }
+
+    std::tuple<double, std::vector<double>, SparseCSR>
+    eval_with_hessian_proj(const std::vector<double>& x, double projection_eps = 1e-9) const
+    {
+        double f;
+        std::vector<double> g(n_vars());
+        SparseCSR H = pattern();
+        check(tad_eval_with_hessian_proj(p_, x.data(), projection_eps, &f, g.data(), H.values.data()));
+        return {f, std::move(g), std::move(H)};
+    }
+
+    /* newton_direction(g, H_proj, solver) at x (NewtonDirection.hh:25-65) */
+    std::vector<double> newton_direction(const std::vector<double>& x, double projection_eps = 1e-9) const
+    {
+        std::vector<double> dvec(n_vars()), g(n_vars());
+        double f;
+        const tad_status s = tad_newton_direction(p_, x.data(), 1, projection_eps, 0.0, dvec.data(), &f, g.data());
+        if (s != TAD_OK && s != TAD_ERR_PCG_NOCONV) check(s);
+        return dvec;
+    }
+
+    /* line_search(x0, d, f, g, func) (LineSearch.hh:26-65) */
+    std::vector<double> line_search(const std::vector<double>& x0, const std::vector<double>& dvec, double f,
+                                    const std::vector<double>& g, double s_max = 1.0) const
+    {
+        std::vector<double> x(n_vars());
+        double fo;
+        const tad_status s = tad_line_search(p_, x0.data(), dvec.data(), f, g.data(), s_max, x.data(), &fo);
+        if (s != TAD_OK && s != TAD_ERR_LS_FAIL) check(s);
+        return x;
+    }
+
+    /* the Projected-Newton loop, fused on the device */
+    std::vector<double> newton_solve(std::vector<double> x, int iters, double projection_eps = 1e-9) const
+    {
+        int done = 0;
+        check(tad_newton_solve(p_, x.data(), iters, projection_eps, 0.0, nullptr, &done));
+        return x;
+    }
+
+private:
+    SparseCSR pattern() const
+    {
+        int64_t nnz = 0;
+        check(tad_hessian_nnz(p_, &nnz));
+        SparseCSR H;
+        H.rows = n_vars();
+        H.outer.resize(n_vars() + 1);
+        H.inner.resize(nnz);
+        H.values.resize(nnz);
+        check(tad_hessian_pattern(p_, H.outer.data(), H.inner.data()));
+        return H;
+    }
+    void swap(ScalarFunction& o)
+    {
+        std::swap(p_, o.p_);
+        std::swap(n_handles_, o.n_handles_);
+        std::swap(terms_, o.terms_);
+        std::swap(handle_bufs_, o.handle_bufs_);
+    }
+
+    tad_problem* p_ = nullptr;
+    int64_t n_handles_ = 0;
+    std::vector<std::unique_ptr<detail::TermBase>> terms_;
+    std::vector<int32_t*> handle_bufs_;
+};
+
+/* scalar_function<d>(range) (ScalarFunctionImpl.hh:418-442) */
+template <int d, typename Range>
+ScalarFunction<d> scalar_function(const Range& variables, const tad_settings* settings = nullptr)
+{
+    int64_t n = 0;
+    for (auto v : variables) { (void)v; ++n; }
+    return ScalarFunction<d>(n, settings);
+}
+
+} // namespace tad

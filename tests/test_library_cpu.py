@@ -46,3 +46,10 @@ def test_problem_create_fails_loudly_without_gpu():
     import tinyad_gb300
     with pytest.raises(RuntimeError):
         tinyad_gb300.ScalarFunction(2, 3)
+
+
+def test_frontend_test_program_builds():
+    """The C++ front end compiles as a user translation unit (no GPU needed)."""
+    from tinyad_gb300 import build
+    build.build()
+    assert os.path.exists(build.FRONTEND_BIN)

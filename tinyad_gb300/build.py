@@ -32,7 +32,7 @@ def sources() -> list[str]:
 
 
 def _deps_mtime() -> float:
-    m = 0.0
+    m = os.path.getmtime(FRONTEND_SRC) if os.path.exists(FRONTEND_SRC) else 0.0
     for d in (CSRC, os.path.join(ROOT, "include"), os.path.join(ROOT, "include", "tad")):
         for f in os.listdir(d):
             if f.endswith((".cu", ".cuh", ".h", ".hh")):
@@ -65,7 +65,25 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    build_frontend_test()
     return LIB
+
+
+FRONTEND_SRC = os.path.join(ROOT, "tests", "cpp", "frontend_test.cu")
+FRONTEND_BIN = os.path.join(OUT, "frontend_test")
+
+
+def build_frontend_test() -> str:
+    """The C++ front-end test program (tests/cpp/frontend_test.cu), a user
+    translation unit compiled against include/tad/ScalarFunction.cuh and
+    linked with libtad.so."""
+    cmd = [nvcc()] + ARCH + ["-std=c++17", "-O2", "--extended-lambda", "--expt-relaxed-constexpr",
+                             "-I", os.path.join(ROOT, "include"), FRONTEND_SRC, "-o", FRONTEND_BIN,
+                             "-L", OUT, "-ltad", "-Xlinker", "-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"front-end test build failed:\n{r.stdout}\n{r.stderr}")
+    return FRONTEND_BIN
 
 
 if __name__ == "__main__":
