@@ -245,6 +245,32 @@ TAD_API tad_status tad_adjoint_rest_gradient(tad_problem* p, const double* x_h, 
                                              const double* rest_h, int projected, double proj_eps,
                                              double* dLdrest_h, double* lambda_h, int* pcg_iters);
 
+/* ---- Batched solves: many independent meshes in one problem --------------
+   No reference counterpart (TinyAD solves one ScalarFunction at a time).
+   Each mesh m has n_handles[m] handles (mesh-local handles 0..n-1, x laid out
+   mesh after mesh); every stage of a Newton iteration is one launch for all
+   meshes, the iteration is one captured CUDA graph, and every mesh keeps its
+   own energy, PCG scalars (pcg_rel_tol, at most pcg_max_iters iterations per
+   Newton step), Armijo choice (16 trial steps) and step. */
+typedef struct tad_batch tad_batch;
+TAD_API tad_status tad_batch_create(int var_dim, int n_meshes, const int64_t* n_handles,
+                                    const tad_settings* settings, tad_batch** out);
+/* n_elem_per_mesh[m] elements per mesh, handles mesh-local, meshes in order */
+TAD_API tad_status tad_batch_add_elements(tad_batch* b, int energy, int valence,
+                                          const int64_t* n_elem_per_mesh, const int32_t* handles_h,
+                                          const double* params_h, int n_params);
+/* f_hist_h (optional): [n_iters + 1][n_meshes] energies */
+TAD_API tad_status tad_batch_newton_solve(tad_batch* b, double* x_h, int n_iters, double proj_eps,
+                                          double* f_hist_h);
+TAD_API tad_status tad_batch_newton_solve_d(tad_batch* b, double* x_d, int n_iters, double proj_eps,
+                                            double* f_hist_h);
+/* times candidate (block rows per chunk, threads per block) pairs on the
+   batch at x_d and keeps the fastest; best3 = [rows, threads, ms] */
+TAD_API tad_status tad_batch_autotune(tad_batch* b, const double* x_d, double proj_eps, double* best3);
+/* the underlying concatenated problem (for evaluations, stats, the stream) */
+TAD_API tad_status tad_batch_problem(tad_batch* b, tad_problem** p);
+TAD_API tad_status tad_batch_destroy(tad_batch* b);
+
 /* Time the main kernels once each at x_d (device), averaged over reps
    launches with CUDA events on the problem's stream: ms5 = [element Hessian
    kernels, gradient + Hessian assembly, one PCG SpMV, one PCG vector update,

@@ -1,0 +1,44 @@
+"""Batched Projected Newton (tad_batch_*): meshes of uneven sizes solved in
+one problem, one launch per stage, one CUDA graph per iteration.  Each mesh
+must reach the energy of its own single-problem solve and of the oracle."""
+import numpy as np
+import pytest
+
+from tinyad_gb300 import meshes
+
+pytestmark = pytest.mark.gpu
+
+
+def _meshes():
+    return [meshes.disk_param(g, seed=100 + i) for i, g in enumerate((8, 14, 20, 11, 24))]
+
+
+@pytest.mark.parametrize("precision,tol", [(0, 1e-10), (1, 1e-5)])
+def test_batch_matches_single_solves(tad, oracle, precision, tol):
+    ws = _meshes()
+    b = tad.Batch(ws, precision=precision, pcg_rel_tol=tol, pcg_max_iters=400)
+    x, fh = b.newton_solve(b.x0(), 40)
+    assert fh.shape == (41, len(ws))
+    assert np.all(np.isfinite(fh))
+    for m, (w, xm) in enumerate(zip(ws, b.split(x))):
+        p = oracle.Problem.from_workload(w)
+        xo, fho, _ = p.newton(w.x0, 40)
+        f_batch = p.eval(xm)
+        assert abs(fh[-1, m] - f_batch) <= 1e-10 * abs(f_batch)
+        assert abs(f_batch - fho[-1]) <= 1e-8 * abs(fho[-1]), (m, f_batch, fho[-1])
+        assert np.all(np.diff(fh[:, m]) <= 1e-12 * fh[0, m])    # monotone per mesh
+
+
+def test_batch_deterministic_and_autotune(tad):
+    import torch
+    ws = _meshes()
+    b = tad.Batch(ws, precision=1, pcg_rel_tol=1e-3, pcg_max_iters=64)
+    x1, f1 = b.newton_solve(b.x0(), 5)
+    x2, f2 = b.newton_solve(b.x0(), 5)
+    assert np.array_equal(x1, x2) and np.array_equal(f1, f2)
+    xd = torch.from_numpy(b.x0()).cuda()
+    best = b.autotune(xd.data_ptr())
+    assert best["chunk_rows"] in (256, 512, 1024, 2048, 4096) and best["threads"] in (128, 256)
+    assert best["ms_per_iteration"] > 0
+    x3, f3 = b.newton_solve(b.x0(), 5)          # results do not depend on the tuned launch shape
+    assert np.allclose(f3, f1, rtol=1e-6, atol=0)

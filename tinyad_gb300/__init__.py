@@ -66,6 +66,8 @@ EXPORTS = [
     "tad_line_search", "tad_newton_solve", "tad_newton_solve_d", "tad_last_solve_stats", "tad_debug_scalar_op",
     "tad_get_stream", "tad_measure_fma_peak", "tad_profile_kernels",
     "tad_launch_count", "tad_adjoint_rest_gradient", "tad_eval_symmetric_dirichlet_tri_noalloc",
+    "tad_batch_create", "tad_batch_add_elements", "tad_batch_newton_solve", "tad_batch_newton_solve_d",
+    "tad_batch_autotune", "tad_batch_problem", "tad_batch_destroy",
 ]
 
 
@@ -111,6 +113,13 @@ def load(build_if_missing: bool = True):
     L.tad_measure_fma_peak.argtypes = [ctypes.c_int, _dp]
     L.tad_profile_kernels.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, _dp]
     L.tad_launch_count.argtypes = [ctypes.c_void_p, _i64p]
+    L.tad_batch_create.argtypes = [ctypes.c_int, ctypes.c_int, _i64p, ctypes.POINTER(Settings), ctypes.POINTER(ctypes.c_void_p)]
+    L.tad_batch_add_elements.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _i64p, _ip, _dp, ctypes.c_int]
+    L.tad_batch_newton_solve.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_double, _dp]
+    L.tad_batch_newton_solve_d.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_double, _dp]
+    L.tad_batch_autotune.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, _dp]
+    L.tad_batch_problem.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]
+    L.tad_batch_destroy.argtypes = [ctypes.c_void_p]
     L.tad_eval_symmetric_dirichlet_tri_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                            ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]
     L.tad_adjoint_rest_gradient.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, ctypes.c_int, ctypes.c_double, _dp, _dp,
@@ -379,6 +388,83 @@ def debug_scalar_op(op: int, a, b=(0.0, 0.0, 0.0), precision: int = PREC_FP64) -
     if rc != TAD_OK:
         raise TinyADError(rc, L.tad_last_error_message().decode())
     return out
+
+
+class Batch:
+    """Many independent meshes solved together (tad_batch_* in include/tad.h).
+
+    workloads: list of meshes.Workload with the same var_dim and term energies
+    (one term per energy, in the same order)."""
+
+    def __init__(self, workloads, settings: Settings | None = None, **kw):
+        self.L = load()
+        self.ws = workloads
+        self.var_dim = workloads[0].var_dim
+        self.n_meshes = len(workloads)
+        self.settings = settings if settings is not None else default_settings(**kw)
+        nh = np.array([w.n_handles for w in workloads], np.int64)
+        self.offsets = np.concatenate([[0], np.cumsum(nh)]) * self.var_dim
+        self.n_vars = int(self.offsets[-1])
+        h = ctypes.c_void_p()
+        self._check(self.L.tad_batch_create(self.var_dim, self.n_meshes, nh.ctypes.data_as(_i64p),
+                                            ctypes.byref(self.settings), ctypes.byref(h)))
+        self.h = h
+        for t in range(len(workloads[0].terms)):
+            terms = [w.terms[t] for w in workloads]
+            cnt = np.array([tt.handles.shape[0] for tt in terms], np.int64)
+            handles = np.ascontiguousarray(np.concatenate([tt.handles for tt in terms]), np.int32)
+            params = np.ascontiguousarray(np.concatenate([tt.params for tt in terms]))
+            self._check(self.L.tad_batch_add_elements(self.h, terms[0].energy, terms[0].valence,
+                                                      cnt.ctypes.data_as(_i64p), handles.ctypes.data_as(_ip),
+                                                      _d(params), params.shape[1]))
+
+    def _check(self, rc, allow=()):
+        if rc != TAD_OK and rc not in allow:
+            raise TinyADError(rc, self.L.tad_last_error_message().decode())
+        return rc
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.tad_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def x0(self) -> np.ndarray:
+        return np.concatenate([w.x0 for w in self.ws])
+
+    def split(self, x):
+        return [x[self.offsets[m]:self.offsets[m + 1]] for m in range(self.n_meshes)]
+
+    def newton_solve(self, x, n_iters: int, projection_eps: float = default_hessian_projection_eps):
+        x = _f64(x).copy()
+        fh = np.zeros((n_iters + 1, self.n_meshes))
+        self._check(self.L.tad_batch_newton_solve(self.h, _d(x), n_iters, projection_eps, _d(fh)))
+        return x, fh
+
+    def newton_solve_device(self, x_ptr: int, n_iters: int, projection_eps: float = default_hessian_projection_eps,
+                            history: bool = False):
+        fh = np.zeros((n_iters + 1, self.n_meshes)) if history else None
+        self._check(self.L.tad_batch_newton_solve_d(self.h, ctypes.c_void_p(x_ptr), n_iters, projection_eps,
+                                                    _d(fh) if history else None))
+        return fh
+
+    def autotune(self, x_ptr: int, projection_eps: float = default_hessian_projection_eps) -> dict:
+        out = np.zeros(3)
+        self._check(self.L.tad_batch_autotune(self.h, ctypes.c_void_p(x_ptr), projection_eps, _d(out)))
+        return {"chunk_rows": int(out[0]), "threads": int(out[1]), "ms_per_iteration": float(out[2])}
+
+    @property
+    def stream_ptr(self) -> int:
+        p = ctypes.c_void_p()
+        self._check(self.L.tad_batch_problem(self.h, ctypes.byref(p)))
+        s = ctypes.c_void_p()
+        self._check(self.L.tad_get_stream(p, ctypes.byref(s)))
+        return int(s.value or 0)
 
 
 def measure_fma_peak(precision: int) -> float:

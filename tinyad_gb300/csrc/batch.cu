@@ -1,0 +1,804 @@
+/*
+ * Batched Projected Newton: many independent meshes of uneven sizes solved
+ * together.  No reference counterpart (TinyAD solves one ScalarFunction at a
+ * time); each mesh follows exactly the single-problem algorithm.
+ *
+ * Layout: the meshes are concatenated into one block-diagonal problem
+ * (handles offset per mesh), so the element kernels, the assembly and the
+ * BSR SpMV run unchanged -- one launch per stage for all meshes.  Everything
+ * that is per mesh -- energies, dot products, PCG alpha/beta/convergence,
+ * the Armijo choice and step -- is computed over "chunks": contiguous ranges
+ * of block rows (or elements) that each belong to one mesh.  A kernel walks
+ * the chunk list with a fixed grid (grid-stride over chunks); the last
+ * chunk of a mesh to finish sums that mesh's chunk partials in chunk order,
+ * so every per-mesh reduction is deterministic.
+ *
+ * One Newton iteration (elements -> f -> assembly -> PCG with a fixed number
+ * of iterations, each mesh stopping at its own tolerance -> two batches of 8
+ * line-search trials -> per-mesh step) has a fixed launch sequence and is
+ * captured once as a CUDA graph; the host replays one graph per iteration.
+ * A small autotuner times candidate chunk sizes / block sizes on the batch
+ * itself and keeps the fastest.
+ */
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <vector>
+
+#include "internal.hh"
+
+namespace tadlib {
+
+struct Chunk
+{
+    int32_t mesh, begin, end;
+};
+
+struct BatchScalars
+{
+    double* f;        // [m] energy
+    double* ftr;      // [m][16] trial energies
+    double* gg;       // [m]
+    double* dg;       // [m]
+    double* rz;       // [m]
+    double* bb;
+    double* tol2;
+    double* alpha;
+    double* beta;
+    double* rr;
+    int32_t* done;    // [m]
+    int32_t* iters;   // [m]
+    int32_t* choice;  // [m] accepted trial, -1 none
+    double* step;     // [m]
+};
+
+constexpr int LS_TRIALS = 16;
+
+__device__ __forceinline__ double bw_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <int NV>
+__device__ __forceinline__ void bblock_sum(double (&v)[NV], double (*sh)[32])
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) v[i] = bw_sum(v[i]);
+    if (lane == 0)
+#pragma unroll
+        for (int i = 0; i < NV; ++i) sh[i][w] = v[i];
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NV; ++i)
+    {
+        v[i] = 0.0;
+        if (w == 0)
+        {
+            v[i] = lane < (int)(blockDim.x >> 5) ? sh[i][lane] : 0.0;
+            v[i] = bw_sum(v[i]);
+        }
+    }
+    __syncthreads();
+}
+
+/* Block-level chunk reduction + per-mesh completion.  Returns true in the
+   block that completed mesh m (totals in tot, all threads). */
+template <int NV>
+__device__ bool seg_finish(int ci, int m, double (&v)[NV], double* partials, int n_chunks, unsigned* counters,
+                           const int32_t* mc_begin, const int32_t* mc_end, double (&tot)[NV])
+{
+    __shared__ double sh[NV][32];
+    __shared__ bool last;
+    __shared__ double res[NV];
+    bblock_sum<NV>(v, sh);
+    if (threadIdx.x == 0)
+    {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) partials[(int64_t)i * n_chunks + ci] = v[i];
+        __threadfence();
+        const unsigned cnt = (unsigned)(mc_end[m] - mc_begin[m]);
+        last = atomicAdd(&counters[m], 1u) == cnt - 1;
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double s[NV];
+#pragma unroll
+    for (int i = 0; i < NV; ++i)
+    {
+        s[i] = 0.0;
+        for (int c = mc_begin[m] + threadIdx.x; c < mc_end[m]; c += blockDim.x)
+            s[i] += __ldcg(&partials[(int64_t)i * n_chunks + c]);
+    }
+    bblock_sum<NV>(s, sh);
+    if (threadIdx.x == 0)
+    {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) res[i] = s[i];
+        counters[m] = 0u;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NV; ++i) tot[i] = res[i];
+    return true;
+}
+
+/* per-mesh sums of element-energy rows: out[m * stride_out + row] */
+__global__ void k_b_reduce_rows(const Chunk* ch, int n_chunks, const int32_t* mcb, const int32_t* mce, const double* ef,
+                                int64_t row_stride, double* partials, unsigned* counters, double* out, int out_stride)
+{
+    const int row = blockIdx.y;
+    for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x)
+    {
+        const Chunk c = ch[ci];
+        double v[1] = {0.0};
+        for (int i = c.begin + threadIdx.x; i < c.end; i += blockDim.x) v[0] += ef[row * row_stride + i];
+        double tot[1];
+        if (seg_finish<1>(ci, c.mesh, v, partials + (int64_t)row * n_chunks, n_chunks, counters + row * 4096, mcb, mce, tot) &&
+            threadIdx.x == 0)
+            out[(int64_t)c.mesh * out_stride + row] = tot[0];
+    }
+}
+
+/* per-mesh a.b over block-row chunks (d values per row) */
+template <int d>
+__global__ void k_b_dot(const Chunk* ch, int n_chunks, const int32_t* mcb, const int32_t* mce, const double* a,
+                        const double* b, double* partials, unsigned* counters, double* out)
+{
+    for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x)
+    {
+        const Chunk c = ch[ci];
+        double v[1] = {0.0};
+        for (int64_t i = (int64_t)c.begin * d + threadIdx.x; i < (int64_t)c.end * d; i += blockDim.x) v[0] += a[i] * b[i];
+        double tot[1];
+        if (seg_finish<1>(ci, c.mesh, v, partials, n_chunks, counters, mcb, mce, tot) && threadIdx.x == 0)
+            out[c.mesh] = tot[0];
+    }
+}
+
+template <int d, typename T>
+__device__ __forceinline__ void bapply_dinv(const T* dinv, int64_t u, const T (&r)[d], T (&z)[d])
+{
+#pragma unroll
+    for (int i = 0; i < d; ++i)
+    {
+        T acc = T(0);
+#pragma unroll
+        for (int j = 0; j < d; ++j) acc += dinv[u * d * d + i * d + j] * r[j];
+        z[i] = acc;
+    }
+}
+
+template <int d, typename T>
+__global__ void k_b_pcg_init(const Chunk* ch, int n_chunks, const int32_t* mcb, const int32_t* mce, const double* b,
+                             T* x, T* r, T* z, T* p, const T* dinv, double* partials, unsigned* counters,
+                             BatchScalars S, double rel_tol)
+{
+    for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x)
+    {
+        const Chunk c = ch[ci];
+        double v[2] = {0.0, 0.0};
+        for (int64_t u = c.begin + threadIdx.x; u < c.end; u += blockDim.x)
+        {
+            T rv[d], zv[d];
+#pragma unroll
+            for (int i = 0; i < d; ++i) { rv[i] = (T)b[u * d + i]; x[u * d + i] = T(0); r[u * d + i] = rv[i]; }
+            bapply_dinv<d, T>(dinv, u, rv, zv);
+#pragma unroll
+            for (int i = 0; i < d; ++i)
+            {
+                z[u * d + i] = zv[i];
+                p[u * d + i] = zv[i];
+                v[0] += (double)rv[i] * (double)zv[i];
+                v[1] += b[u * d + i] * b[u * d + i];
+            }
+        }
+        double tot[2];
+        if (seg_finish<2>(ci, c.mesh, v, partials, n_chunks, counters, mcb, mce, tot) && threadIdx.x == 0)
+        {
+            const int m = c.mesh;
+            S.rz[m] = tot[0];
+            S.bb[m] = tot[1];
+            S.rr[m] = tot[1];
+            S.tol2[m] = rel_tol * rel_tol * tot[1];
+            S.iters[m] = 0;
+            S.done[m] = tot[1] == 0.0 ? 1 : 0;
+        }
+    }
+}
+
+template <int d, typename T>
+__global__ void k_b_spmv(const Chunk* ch, int n_chunks, const int32_t* mcb, const int32_t* mce, const int32_t* bptr,
+                         const int32_t* bcol, const T* H, const T* p, T* Ap, double* partials, unsigned* counters,
+                         BatchScalars S)
+{
+    for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x)
+    {
+        const Chunk c = ch[ci];
+        if (S.done[c.mesh]) continue;
+        double v[1] = {0.0};
+        for (int64_t u = c.begin + threadIdx.x; u < c.end; u += blockDim.x)
+        {
+            T y[d];
+#pragma unroll
+            for (int i = 0; i < d; ++i) y[i] = T(0);
+            for (int32_t bb = bptr[u]; bb < bptr[u + 1]; ++bb)
+            {
+                const int64_t w = bcol[bb];
+                const T* B = H + (int64_t)bb * d * d;
+#pragma unroll
+                for (int i = 0; i < d; ++i)
+#pragma unroll
+                    for (int j = 0; j < d; ++j) y[i] += B[i * d + j] * p[w * d + j];
+            }
+#pragma unroll
+            for (int i = 0; i < d; ++i) { Ap[u * d + i] = y[i]; v[0] += (double)(p[u * d + i] * y[i]); }
+        }
+        double tot[1];
+        if (seg_finish<1>(ci, c.mesh, v, partials, n_chunks, counters, mcb, mce, tot) && threadIdx.x == 0)
+        {
+            const int m = c.mesh;
+            if (!(tot[0] > 0.0) || !isfinite(tot[0])) { S.done[m] = 1; S.alpha[m] = 0.0; }
+            else S.alpha[m] = S.rz[m] / tot[0];
+        }
+    }
+}
+
+template <int d, typename T>
+__global__ void k_b_update(const Chunk* ch, int n_chunks, const int32_t* mcb, const int32_t* mce, T* x, T* r, T* z,
+                           const T* p, const T* Ap, const T* dinv, double* partials, unsigned* counters, BatchScalars S,
+                           int max_iters)
+{
+    for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x)
+    {
+        const Chunk c = ch[ci];
+        if (S.done[c.mesh]) continue;
+        const T alpha = (T)S.alpha[c.mesh];
+        double v[2] = {0.0, 0.0};
+        for (int64_t u = c.begin + threadIdx.x; u < c.end; u += blockDim.x)
+        {
+            T rv[d], zv[d];
+#pragma unroll
+            for (int i = 0; i < d; ++i)
+            {
+                x[u * d + i] += alpha * p[u * d + i];
+                rv[i] = r[u * d + i] - alpha * Ap[u * d + i];
+                r[u * d + i] = rv[i];
+            }
+            bapply_dinv<d, T>(dinv, u, rv, zv);
+#pragma unroll
+            for (int i = 0; i < d; ++i)
+            {
+                z[u * d + i] = zv[i];
+                v[0] += (double)(rv[i] * zv[i]);
+                v[1] += (double)(rv[i] * rv[i]);
+            }
+        }
+        double tot[2];
+        if (seg_finish<2>(ci, c.mesh, v, partials, n_chunks, counters, mcb, mce, tot) && threadIdx.x == 0)
+        {
+            const int m = c.mesh;
+            S.beta[m] = tot[0] / S.rz[m];
+            S.rz[m] = tot[0];
+            S.rr[m] = tot[1];
+            S.iters[m] += 1;
+            if (tot[1] <= S.tol2[m] || S.iters[m] >= max_iters || !isfinite(tot[1])) S.done[m] = 2;
+        }
+    }
+}
+
+/* p = z + beta p for meshes still iterating (done == 0); a mesh that finished
+   in this iteration's update (done == 2) keeps p, then is marked 1 */
+template <int d, typename T>
+__global__ void k_b_pupdate(const Chunk* ch, int n_chunks, const T* z, T* p, BatchScalars S)
+{
+    for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x)
+    {
+        const Chunk c = ch[ci];
+        if (S.done[c.mesh]) continue;
+        const T beta = (T)S.beta[c.mesh];
+        for (int64_t i = (int64_t)c.begin * d + threadIdx.x; i < (int64_t)c.end * d; i += blockDim.x) p[i] = z[i] + beta * p[i];
+    }
+}
+
+__global__ void k_b_settle(int n_meshes, BatchScalars S)
+{
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m < n_meshes && S.done[m] == 2) S.done[m] = 1;
+}
+
+template <typename T>
+__global__ void k_b_to_double(int64_t n, const T* a, double* out)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (double)a[i];
+}
+
+__global__ void k_b_neg(int64_t n, const double* a, double* out)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = -a[i];
+}
+
+/* per-mesh Armijo choice among trials [t0, t0 + nt) (LineSearch.hh:14-24) */
+__global__ void k_b_ls_select(int n_meshes, int t0, int nt, const double* steps, double c_armijo, BatchScalars S)
+{
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n_meshes) return;
+    if (t0 == 0) S.choice[m] = -1;
+    if (S.choice[m] >= 0) return;
+    for (int j = 0; j < nt; ++j)
+    {
+        const double fn = S.ftr[m * LS_TRIALS + t0 + j];
+        if (fn <= S.f[m] + c_armijo * steps[t0 + j] * S.dg[m])
+        {
+            S.choice[m] = t0 + j;
+            S.step[m] = steps[t0 + j];
+            return;
+        }
+    }
+}
+
+template <int d>
+__global__ void k_b_axpy(const Chunk* ch, int n_chunks, double* x, const double* dx, BatchScalars S, int apply_all)
+{
+    for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x)
+    {
+        const Chunk c = ch[ci];
+        if (S.choice[c.mesh] < 0) continue;
+        const double s = S.step[c.mesh];
+        for (int64_t i = (int64_t)c.begin * d + threadIdx.x; i < (int64_t)c.end * d; i += blockDim.x) x[i] += s * dx[i];
+    }
+}
+
+/* line-search trial energies of meshes that have not accepted a step yet are
+   computed for all meshes (one launch); k_b_ls_select ignores the rest */
+
+struct Batch
+{
+    tad_problem* P = nullptr;
+    int n_meshes = 0;
+    std::vector<int64_t> vert_off;           // per mesh handle offset (n_meshes + 1)
+    std::vector<std::vector<int64_t>> elem_cnt; // per term, per mesh element counts (built while adding)
+    int chunk_rows = 1024, threads = 256, grid = 608;
+    // device
+    Chunk *vch = nullptr, *ech = nullptr;
+    int n_vch = 0, n_ech = 0;
+    int32_t *vmcb = nullptr, *vmce = nullptr, *emcb = nullptr, *emce = nullptr;
+    double* partials = nullptr;
+    unsigned* counters = nullptr;   // [LS_TRIALS * 4096]
+    double* scal = nullptr;
+    int32_t* iscal = nullptr;
+    BatchScalars S{};
+    double* steps = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    int graph_iters = 0;
+    double* fh = nullptr;           // pinned [n_meshes]
+    double* x = nullptr;            // device state
+    int pcg_iters = 64;
+    double pcg_tol = 1e-2;
+};
+
+static std::vector<Chunk> make_chunks(const std::vector<int64_t>& off, int rows, std::vector<int32_t>& mcb, std::vector<int32_t>& mce)
+{
+    std::vector<Chunk> out;
+    const int nm = (int)off.size() - 1;
+    mcb.assign(nm, 0);
+    mce.assign(nm, 0);
+    for (int m = 0; m < nm; ++m)
+    {
+        mcb[m] = (int32_t)out.size();
+        for (int64_t b = off[m]; b < off[m + 1]; b += rows)
+            out.push_back({m, (int32_t)b, (int32_t)std::min<int64_t>(off[m + 1], b + rows)});
+        mce[m] = (int32_t)out.size();
+    }
+    return out;
+}
+
+static tad_status batch_fail(tad_status s, const char* m) { set_error(m); return s; }
+
+template <typename X>
+static cudaError_t upload(X** d, const std::vector<X>& h)
+{
+    cudaError_t e = cudaMalloc((void**)d, std::max<size_t>(h.size(), 1) * sizeof(X));
+    if (e != cudaSuccess) return e;
+    return h.empty() ? cudaSuccess : cudaMemcpy(*d, h.data(), h.size() * sizeof(X), cudaMemcpyHostToDevice);
+}
+
+static tad_status batch_setup_chunks(Batch& B)
+{
+    Problem& P = *B.P;
+    if (B.vch) { cudaFree(B.vch); cudaFree(B.ech); cudaFree(B.vmcb); cudaFree(B.vmce); cudaFree(B.emcb); cudaFree(B.emce); }
+    std::vector<int32_t> vmcb, vmce, emcb, emce;
+    std::vector<Chunk> vch = make_chunks(B.vert_off, B.chunk_rows, vmcb, vmce);
+    // element chunks: per mesh, over every term (elements of a mesh are contiguous within a term)
+    std::vector<Chunk> ech;
+    emcb.assign(B.n_meshes, 0);
+    emce.assign(B.n_meshes, 0);
+    for (int m = 0; m < B.n_meshes; ++m)
+    {
+        emcb[m] = (int32_t)ech.size();
+        for (size_t t = 0; t < P.terms.size(); ++t)
+        {
+            int64_t beg = P.terms[t].elem_off;
+            for (int mm = 0; mm < m; ++mm) beg += B.elem_cnt[t][mm];
+            const int64_t end = beg + B.elem_cnt[t][m];
+            for (int64_t b = beg; b < end; b += 4 * B.chunk_rows)
+                ech.push_back({m, (int32_t)b, (int32_t)std::min<int64_t>(end, b + 4 * B.chunk_rows)});
+        }
+        emce[m] = (int32_t)ech.size();
+        if (emce[m] == emcb[m]) ech.push_back({m, 0, 0}), emce[m] = (int32_t)ech.size();
+    }
+    B.n_vch = (int)vch.size();
+    B.n_ech = (int)ech.size();
+    TAD_CUDA_TRY(upload(&B.vch, vch));
+    TAD_CUDA_TRY(upload(&B.ech, ech));
+    TAD_CUDA_TRY(upload(&B.vmcb, vmcb));
+    TAD_CUDA_TRY(upload(&B.vmce, vmce));
+    TAD_CUDA_TRY(upload(&B.emcb, emcb));
+    TAD_CUDA_TRY(upload(&B.emce, emce));
+    if (B.partials) cudaFree(B.partials);
+    TAD_CUDA_TRY(cudaMalloc(&B.partials, (size_t)std::max(B.n_vch, B.n_ech) * LS_TRIALS * 2 * sizeof(double)));
+    return TAD_OK;
+}
+
+void launch_diag_inv(Problem& P, int prec, cudaStream_t s);
+
+/* record one batched Newton iteration on the problem's stream (captured) */
+template <int d, typename T>
+static tad_status record_iteration(Batch& B, int prec, double eps)
+{
+    Problem& P = *B.P;
+    cudaStream_t s = P.stream;
+    const int G = B.grid, TH = B.threads;
+    const int64_t n = P.n_vars, nh = P.n_handles;
+    T* H = (T*)P.H;
+    T *r, *z, *p, *Ap, *xs, *dinv;
+    if (prec == TAD_PREC_MIXED) { r = (T*)P.r32; z = (T*)P.z32; p = (T*)P.p32; Ap = (T*)P.Ap32; xs = (T*)P.dx32; dinv = (T*)P.dinv32; }
+    else { r = (T*)P.r; z = (T*)P.z; p = (T*)P.p; Ap = (T*)P.Ap; xs = (T*)P.dx; dinv = (T*)P.dinv; }
+    // 1. element Hessians (all meshes, one launch per term), f per mesh, assembly
+    tad_status st = eval_elements(P, TAD_MODE_HESSIAN_PROJ, B.x, eps, prec);
+    if (st != TAD_OK) return st;
+    k_b_reduce_rows<<<dim3(G, 1), TH, 0, s>>>(B.ech, B.n_ech, B.emcb, B.emce, P.ef, P.n_elem_total, B.partials, B.counters, B.S.f, 1);
+    launch_assemble_grad(P);
+    launch_assemble_hess(P, prec);
+    k_b_neg<<<G, TH, 0, s>>>(n, P.g, P.rhs);
+    // 2. PCG, per-mesh tolerance
+    launch_diag_inv(P, prec, s);
+    k_b_pcg_init<d, T><<<G, TH, 0, s>>>(B.vch, B.n_vch, B.vmcb, B.vmce, P.rhs, xs, r, z, p, dinv, B.partials,
+                                        B.counters, B.S, B.pcg_tol);
+    for (int it = 0; it < B.pcg_iters; ++it)
+    {
+        k_b_spmv<d, T><<<G, TH, 0, s>>>(B.vch, B.n_vch, B.vmcb, B.vmce, P.bptr, P.bcol, H, p, Ap, B.partials,
+                                        B.counters, B.S);
+        k_b_update<d, T><<<G, TH, 0, s>>>(B.vch, B.n_vch, B.vmcb, B.vmce, xs, r, z, p, Ap, dinv, B.partials,
+                                          B.counters, B.S, B.pcg_iters);
+        k_b_pupdate<d, T><<<G, TH, 0, s>>>(B.vch, B.n_vch, z, p, B.S);
+        k_b_settle<<<(B.n_meshes + 255) / 256, 256, 0, s>>>(B.n_meshes, B.S);
+    }
+    k_b_to_double<T><<<G, TH, 0, s>>>(n, xs, P.dx);
+    // 3. line search: d.g per mesh, 2 batches of 8 trials, per-mesh choice and step
+    k_b_dot<d><<<G, TH, 0, s>>>(B.vch, B.n_vch, B.vmcb, B.vmce, P.dx, P.g, B.partials, B.counters, B.S.dg);
+    for (int t0 = 0; t0 < LS_TRIALS; t0 += LS_BATCH)
+    {
+        double* save = P.steps;
+        P.steps = B.steps + t0;
+        st = eval_elements(P, TAD_MODE_LINESEARCH, B.x, 0.0, TAD_PREC_FP64, P.dx, LS_BATCH);
+        P.steps = save;
+        if (st != TAD_OK) return st;
+        k_b_reduce_rows<<<dim3(G, LS_BATCH), TH, 0, s>>>(B.ech, B.n_ech, B.emcb, B.emce, P.ef, P.n_elem_total,
+                                                         B.partials, B.counters, B.S.ftr + t0, LS_TRIALS);
+        k_b_ls_select<<<(B.n_meshes + 255) / 256, 256, 0, s>>>(B.n_meshes, t0, LS_BATCH, B.steps, P.settings.ls_armijo, B.S);
+    }
+    k_b_axpy<d><<<G, TH, 0, s>>>(B.vch, B.n_vch, B.x, P.dx, B.S, 0);
+    (void)nh;
+    TAD_CUDA_TRY(cudaGetLastError());
+    return TAD_OK;
+}
+
+template <int d>
+static tad_status capture(Batch& B, int prec, double eps)
+{
+    Problem& P = *B.P;
+    if (B.graph) { cudaGraphExecDestroy(B.graph); B.graph = nullptr; }
+    cudaGraph_t g;
+    TAD_CUDA_TRY(cudaStreamBeginCapture(P.stream, cudaStreamCaptureModeThreadLocal));
+    tad_status st = prec == TAD_PREC_MIXED ? record_iteration<d, float>(B, prec, eps) : record_iteration<d, double>(B, prec, eps);
+    cudaGraph_t tmp;
+    cudaError_t e = cudaStreamEndCapture(P.stream, &tmp);
+    if (st != TAD_OK) { if (e == cudaSuccess) cudaGraphDestroy(tmp); return st; }
+    TAD_CUDA_TRY(e);
+    g = tmp;
+    TAD_CUDA_TRY(cudaGraphInstantiate(&B.graph, g, 0));
+    cudaGraphDestroy(g);
+    return TAD_OK;
+}
+
+static tad_status batch_capture(Batch& B, double eps)
+{
+    switch (B.P->d)
+    {
+    case 1: return capture<1>(B, B.P->precision, eps);
+    case 2: return capture<2>(B, B.P->precision, eps);
+    default: return capture<3>(B, B.P->precision, eps);
+    }
+}
+
+} // namespace tadlib
+
+using namespace tadlib;
+
+struct tad_batch : public tadlib::Batch {};
+
+namespace tadlib {
+// diag inverse with the single-problem kernels (defined in solver.cu)
+template <int d, typename T>
+__global__ void k_diag_inv_b(int64_t nh, const int32_t* __restrict__ diag, const T* __restrict__ H, T* __restrict__ dinv)
+{
+    for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < nh; u += (int64_t)gridDim.x * blockDim.x)
+    {
+        double A[d * d], I[d * d];
+        const int32_t b = diag[u];
+#pragma unroll
+        for (int i = 0; i < d * d; ++i) A[i] = b >= 0 ? (double)H[(int64_t)b * d * d + i] : 0.0;
+        double det;
+        if (d == 1) { det = A[0]; I[0] = 1.0 / A[0]; }
+        else if (d == 2)
+        {
+            det = A[0] * A[3] - A[1] * A[2];
+            const double id = 1.0 / det;
+            I[0] = A[3] * id; I[1] = -A[1] * id; I[2] = -A[2] * id; I[3] = A[0] * id;
+        }
+        else
+        {
+            const double c00 = A[4] * A[8] - A[5] * A[7], c01 = A[5] * A[6] - A[3] * A[8], c02 = A[3] * A[7] - A[4] * A[6];
+            det = A[0] * c00 + A[1] * c01 + A[2] * c02;
+            const double id = 1.0 / det;
+            I[0] = c00 * id; I[3] = c01 * id; I[6] = c02 * id;
+            I[1] = (A[2] * A[7] - A[1] * A[8]) * id; I[4] = (A[0] * A[8] - A[2] * A[6]) * id; I[7] = (A[1] * A[6] - A[0] * A[7]) * id;
+            I[2] = (A[1] * A[5] - A[2] * A[4]) * id; I[5] = (A[2] * A[3] - A[0] * A[5]) * id; I[8] = (A[0] * A[4] - A[1] * A[3]) * id;
+        }
+        const bool ok = det > 0.0 && isfinite(det);
+#pragma unroll
+        for (int i = 0; i < d; ++i)
+#pragma unroll
+            for (int j = 0; j < d; ++j)
+                dinv[u * d * d + i * d + j] = (T)(ok ? I[i * d + j] : (i == j ? (A[i * d + i] > 0.0 ? 1.0 / A[i * d + i] : 1.0) : 0.0));
+    }
+}
+
+void launch_diag_inv(Problem& P, int prec, cudaStream_t s)
+{
+#define TAD_DI(D)                                                                                          \
+    if (prec == TAD_PREC_MIXED) k_diag_inv_b<D, float><<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_handles, P.diag, (const float*)P.H, P.dinv32); \
+    else k_diag_inv_b<D, double><<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_handles, P.diag, (const double*)P.H, P.dinv);
+    switch (P.d)
+    {
+    case 1: TAD_DI(1); break;
+    case 2: TAD_DI(2); break;
+    default: TAD_DI(3); break;
+    }
+#undef TAD_DI
+}
+} // namespace tadlib
+
+extern "C" {
+
+TAD_API tad_status tad_batch_create(int var_dim, int n_meshes, const int64_t* n_handles, const tad_settings* settings,
+                                    tad_batch** out)
+{
+    if (!out || !n_handles || n_meshes < 1 || n_meshes > 4096) return batch_fail(TAD_ERR_ARG, "bad batch arguments (1..4096 meshes)");
+    *out = nullptr;
+    tad_batch* B = new tad_batch();
+    B->n_meshes = n_meshes;
+    B->vert_off.assign(n_meshes + 1, 0);
+    for (int m = 0; m < n_meshes; ++m)
+    {
+        if (n_handles[m] <= 0) { delete B; return batch_fail(TAD_ERR_ARG, "every mesh needs at least one handle"); }
+        B->vert_off[m + 1] = B->vert_off[m] + n_handles[m];
+    }
+    tad_status s = tad_problem_create(var_dim, B->vert_off[n_meshes], settings, &B->P);
+    if (s != TAD_OK) { delete B; return s; }
+    *out = B;
+    return TAD_OK;
+}
+
+TAD_API tad_status tad_batch_add_elements(tad_batch* B, int energy, int valence, const int64_t* n_elem_per_mesh,
+                                          const int32_t* handles_h, const double* params_h, int n_params)
+{
+    if (!B || !n_elem_per_mesh) return batch_fail(TAD_ERR_ARG, "NULL argument");
+    int64_t total = 0;
+    for (int m = 0; m < B->n_meshes; ++m) total += n_elem_per_mesh[m];
+    std::vector<int32_t> h(handles_h, handles_h + total * valence);
+    int64_t e = 0;
+    for (int m = 0; m < B->n_meshes; ++m)
+        for (int64_t k = 0; k < n_elem_per_mesh[m]; ++k, ++e)
+            for (int a = 0; a < valence; ++a)
+            {
+                int32_t& v = h[e * valence + a];
+                if (v < 0 || v >= B->vert_off[m + 1] - B->vert_off[m]) return batch_fail(TAD_ERR_ARG, "mesh-local handle out of range");
+                v += (int32_t)B->vert_off[m];
+            }
+    tad_status s = tad_add_elements(B->P, energy, valence, total, h.data(), params_h, n_params);
+    if (s != TAD_OK) return s;
+    B->elem_cnt.emplace_back(n_elem_per_mesh, n_elem_per_mesh + B->n_meshes);
+    return TAD_OK;
+}
+
+static tad_status batch_prepare(tad_batch* B)
+{
+    tad_status s = ensure_finalized(*B->P);
+    if (s != TAD_OK) return s;
+    if (!B->counters)
+    {
+        TAD_CUDA_TRY(cudaMalloc(&B->counters, (size_t)LS_TRIALS * 4096 * sizeof(unsigned)));
+        TAD_CUDA_TRY(cudaMemset(B->counters, 0, (size_t)LS_TRIALS * 4096 * sizeof(unsigned)));
+        const int nm = B->n_meshes;
+        TAD_CUDA_TRY(cudaMalloc(&B->scal, (size_t)nm * (LS_TRIALS + 12) * sizeof(double)));
+        TAD_CUDA_TRY(cudaMemset(B->scal, 0, (size_t)nm * (LS_TRIALS + 12) * sizeof(double)));
+        TAD_CUDA_TRY(cudaMalloc(&B->iscal, (size_t)nm * 4 * sizeof(int32_t)));
+        TAD_CUDA_TRY(cudaMemset(B->iscal, 0, (size_t)nm * 4 * sizeof(int32_t)));
+        double* q = B->scal;
+        B->S.f = q; q += nm;
+        B->S.ftr = q; q += (size_t)nm * LS_TRIALS;
+        B->S.gg = q; q += nm;
+        B->S.dg = q; q += nm;
+        B->S.rz = q; q += nm;
+        B->S.bb = q; q += nm;
+        B->S.tol2 = q; q += nm;
+        B->S.alpha = q; q += nm;
+        B->S.beta = q; q += nm;
+        B->S.rr = q; q += nm;
+        B->S.step = q; q += nm;
+        B->S.done = B->iscal;
+        B->S.iters = B->iscal + nm;
+        B->S.choice = B->iscal + 2 * nm;
+        TAD_CUDA_TRY(cudaMalloc(&B->steps, LS_TRIALS * sizeof(double)));
+        std::vector<double> st(LS_TRIALS);
+        double sv = 1.0;
+        for (int j = 0; j < LS_TRIALS; ++j) { st[j] = sv; sv *= B->P->settings.ls_shrink; }
+        TAD_CUDA_TRY(cudaMemcpy(B->steps, st.data(), LS_TRIALS * sizeof(double), cudaMemcpyHostToDevice));
+        TAD_CUDA_TRY(cudaMallocHost(&B->fh, (size_t)nm * sizeof(double)));
+        TAD_CUDA_TRY(cudaMalloc(&B->x, B->P->n_vars * sizeof(double)));
+        s = batch_setup_chunks(*B);
+        if (s != TAD_OK) return s;
+    }
+    return TAD_OK;
+}
+
+/* n_iters batched Newton iterations on device x (x_d, concatenated meshes).
+   f_hist_h (optional): [n_iters + 1][n_meshes] energies. */
+TAD_API tad_status tad_batch_newton_solve_d(tad_batch* B, double* x_d, int n_iters, double eps, double* f_hist_h)
+{
+    if (!B || !x_d) return batch_fail(TAD_ERR_ARG, "NULL argument");
+    TAD_CUDA_TRY(cudaSetDevice(B->P->device));
+    tad_status s = batch_prepare(B);
+    if (s != TAD_OK) return s;
+    Problem& P = *B->P;
+    const int nm = B->n_meshes;
+    B->pcg_iters = std::max(1, std::min(P.settings.pcg_max_iters, 4096));
+    B->pcg_tol = P.settings.pcg_rel_tol;
+    TAD_CUDA_TRY(cudaMemcpyAsync(B->x, x_d, P.n_vars * 8, cudaMemcpyDeviceToDevice, P.stream));
+    if (!B->graph)
+    {
+        s = batch_capture(*B, eps);
+        if (s != TAD_OK) return s;
+    }
+    for (int it = 0; it < n_iters; ++it)
+    {
+        TAD_CUDA_TRY(cudaGraphLaunch(B->graph, P.stream));
+        P.n_launches += 1;
+        if (f_hist_h)
+        {
+            TAD_CUDA_TRY(cudaMemcpyAsync(B->fh, B->S.f, nm * 8, cudaMemcpyDeviceToHost, P.stream));
+            TAD_CUDA_TRY(cudaStreamSynchronize(P.stream));
+            std::copy(B->fh, B->fh + nm, f_hist_h + (size_t)it * nm);
+        }
+    }
+    if (f_hist_h)
+    {
+        // energy at the final x
+        s = eval_elements(P, TAD_MODE_VALUE, B->x, 0.0, TAD_PREC_FP64);
+        if (s != TAD_OK) return s;
+        k_b_reduce_rows<<<dim3(B->grid, 1), B->threads, 0, P.stream>>>(B->ech, B->n_ech, B->emcb, B->emce, P.ef,
+                                                                      P.n_elem_total, B->partials, B->counters, B->S.f, 1);
+        TAD_CUDA_TRY(cudaMemcpyAsync(B->fh, B->S.f, nm * 8, cudaMemcpyDeviceToHost, P.stream));
+        TAD_CUDA_TRY(cudaStreamSynchronize(P.stream));
+        std::copy(B->fh, B->fh + nm, f_hist_h + (size_t)n_iters * nm);
+    }
+    TAD_CUDA_TRY(cudaMemcpyAsync(x_d, B->x, P.n_vars * 8, cudaMemcpyDeviceToDevice, P.stream));
+    TAD_CUDA_TRY(cudaStreamSynchronize(P.stream));
+    return check_device_error(P);
+}
+
+TAD_API tad_status tad_batch_newton_solve(tad_batch* B, double* x_h, int n_iters, double eps, double* f_hist_h)
+{
+    if (!B || !x_h) return batch_fail(TAD_ERR_ARG, "NULL argument");
+    TAD_CUDA_TRY(cudaSetDevice(B->P->device));
+    tad_status s = batch_prepare(B);
+    if (s != TAD_OK) return s;
+    Problem& P = *B->P;
+    TAD_CUDA_TRY(cudaMemcpyAsync(P.x, x_h, P.n_vars * 8, cudaMemcpyHostToDevice, P.stream));
+    s = tad_batch_newton_solve_d(B, P.x, n_iters, eps, f_hist_h);
+    if (s != TAD_OK) return s;
+    TAD_CUDA_TRY(cudaMemcpyAsync(x_h, P.x, P.n_vars * 8, cudaMemcpyDeviceToHost, P.stream));
+    TAD_CUDA_TRY(cudaStreamSynchronize(P.stream));
+    return TAD_OK;
+}
+
+/* Autotuner: times one captured batched Newton iteration for each candidate
+   (block rows per chunk x threads per block) on the batch's current x and
+   keeps the fastest.  Candidates are measured after one warm replay, with
+   CUDA events on the batch's stream; the state x is restored afterwards.
+   best3 (optional): [chunk_rows, threads, ms]. */
+TAD_API tad_status tad_batch_autotune(tad_batch* B, const double* x_d, double eps, double* best3)
+{
+    if (!B || !x_d) return batch_fail(TAD_ERR_ARG, "NULL argument");
+    TAD_CUDA_TRY(cudaSetDevice(B->P->device));
+    tad_status s = batch_prepare(B);
+    if (s != TAD_OK) return s;
+    Problem& P = *B->P;
+    B->pcg_iters = std::max(1, std::min(P.settings.pcg_max_iters, 4096));
+    B->pcg_tol = P.settings.pcg_rel_tol;
+    const int rows_c[] = {256, 512, 1024, 2048, 4096};
+    const int thr_c[] = {128, 256};
+    double best = 1e30;
+    int br = B->chunk_rows, bt = B->threads;
+    for (int rows : rows_c)
+        for (int thr : thr_c)
+        {
+            B->chunk_rows = rows;
+            B->threads = thr;
+            B->grid = 4 * 152;
+            s = batch_setup_chunks(*B);
+            if (s != TAD_OK) return s;
+            s = batch_capture(*B, eps);
+            if (s != TAD_OK) return s;
+            float ms = 0.f;
+            TAD_CUDA_TRY(cudaMemcpyAsync(B->x, x_d, P.n_vars * 8, cudaMemcpyDeviceToDevice, P.stream));
+            TAD_CUDA_TRY(cudaGraphLaunch(B->graph, P.stream));
+            TAD_CUDA_TRY(cudaMemcpyAsync(B->x, x_d, P.n_vars * 8, cudaMemcpyDeviceToDevice, P.stream));
+            cudaEventRecord(P.ev[5], P.stream);
+            TAD_CUDA_TRY(cudaGraphLaunch(B->graph, P.stream));
+            cudaEventRecord(P.ev[6], P.stream);
+            TAD_CUDA_TRY(cudaEventSynchronize(P.ev[6]));
+            cudaEventElapsedTime(&ms, P.ev[5], P.ev[6]);
+            if (ms < best) { best = ms; br = rows; bt = thr; }
+        }
+    B->chunk_rows = br;
+    B->threads = bt;
+    s = batch_setup_chunks(*B);
+    if (s != TAD_OK) return s;
+    s = batch_capture(*B, eps);
+    if (s != TAD_OK) return s;
+    TAD_CUDA_TRY(cudaMemcpyAsync(B->x, x_d, P.n_vars * 8, cudaMemcpyDeviceToDevice, P.stream));
+    TAD_CUDA_TRY(cudaStreamSynchronize(P.stream));
+    if (best3) { best3[0] = br; best3[1] = bt; best3[2] = best; }
+    return TAD_OK;
+}
+
+TAD_API tad_status tad_batch_problem(tad_batch* B, tad_problem** p)
+{
+    if (!B || !p) return batch_fail(TAD_ERR_ARG, "NULL argument");
+    *p = B->P;
+    return TAD_OK;
+}
+
+TAD_API tad_status tad_batch_destroy(tad_batch* B)
+{
+    if (!B) return TAD_OK;
+    if (B->P) cudaStreamSynchronize(B->P->stream);
+    if (B->graph) cudaGraphExecDestroy(B->graph);
+    void* bufs[] = {B->vch, B->ech, B->vmcb, B->vmce, B->emcb, B->emce, B->partials, B->counters, B->scal, B->iscal,
+                    B->steps, B->x};
+    for (void* b : bufs) if (b) cudaFree(b);
+    if (B->fh) cudaFreeHost(B->fh);
+    tad_problem_destroy(B->P);
+    delete B;
+    return TAD_OK;
+}
+
+} // extern "C"
