@@ -32,6 +32,10 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 METRIC = "Newton iters/s & element-Hessians/s, mixed vs FP64 GPU at 1e-8 energy err"
+# Algorithmic flops per element (value, gradient, full Hessian of the reference's
+# dense Double<k> symmetric Dirichlet + cyclic-Jacobi projection at 5 / 6
+# sweeps), counted by oracle/flop_count.sh with an op-counting passive type.
+ELEM_FLOPS = {6: 15562, 12: 174837}
 UNIT = "Newton iters/s"
 
 
@@ -48,6 +52,21 @@ def parse():
     ap.add_argument("--kernels-only", action="store_true",
                     help="profile the main kernels once at the initial state (for ncu captures) and exit")
     return ap.parse_args()
+
+
+def reduce_max(v: float, dist, device) -> float:
+    """Max over ranks (timings: the slowest rank defines the step time)."""
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_rate(world: int, steps: int, seconds: float) -> float:
+    """Whole-job rate for weak scaling: every rank runs its own mesh replica."""
+    return world * steps / seconds
 
 
 def make_workload(name: str, rank: int = 0):
@@ -130,12 +149,18 @@ class ClockSampler:
 CPU_SAMPLE = "disk512"
 
 
+def cpu_sample_name(full_name: str) -> str:
+    return "tet24" if full_name.startswith("tet") else CPU_SAMPLE
+
+
 def cpu_baseline(full_w, threads: int | None = None) -> dict:
     """One oracle Projected-Newton iteration (OpenMP element eval, serial
-    scatter + triplet sort, sparse LDL^T, Armijo) on the 512-grid disk of the
-    same family, scaled to the benchmark mesh by face count."""
+    scatter + triplet sort, sparse LDL^T, Armijo) on a smaller mesh of the
+    same family (512-grid disk / 24^3 tet cube), scaled to the benchmark mesh
+    by element count."""
     from oracle import pyoracle
-    w = make_workload(CPU_SAMPLE)
+    CPU = cpu_sample_name(full_w.name)
+    w = make_workload(CPU)
     nthreads = threads if threads else -1
     p = pyoracle.Problem.from_workload(w, n_threads=nthreads)
     t0 = time.perf_counter()
@@ -144,8 +169,8 @@ def cpu_baseline(full_w, threads: int | None = None) -> dict:
     scale = w.n_elements / full_w.n_elements
     return {"value": (1.0 / dt) * scale, "unit": UNIT, "cores": p.n_threads, "kind": "port",
             "sample": (f"1 Projected-Newton iteration of the oracle (CPU restatement of the reference path: OpenMP "
-                       f"element eval + projection, serial triplet assembly, sparse LDL^T, Armijo) on {CPU_SAMPLE} "
-                       f"({w.n_elements} faces) = {dt:.2f} s, scaled by faces to {full_w.n_elements} faces "
+                       f"element eval + projection, serial triplet assembly, sparse LDL^T, Armijo) on {CPU} "
+                       f"({w.n_elements} elements) = {dt:.2f} s, scaled by elements to {full_w.n_elements} "
                        f"(linear scaling; the LDL^T grows faster, so this favours the CPU)"),
             "stage_s": {"eval_assemble": times[0], "ldlt": times[1], "line_search": times[2]}}
 
@@ -158,7 +183,7 @@ def run_reference(args):
         return
     from oracle import pyoracle
     full = make_workload(args.workload)
-    w = make_workload(CPU_SAMPLE) if args.workload.startswith("disk") else full
+    w = make_workload(cpu_sample_name(args.workload))
     threads = os.cpu_count() or 1
     p = pyoracle.Problem.from_workload(w, n_threads=threads)
     x = w.x0.copy()
@@ -275,7 +300,9 @@ def main():
     t_gen = time.perf_counter()
     w = make_workload(args.workload, rank)
     t_gen = time.perf_counter() - t_gen
-    settings = dict(pcg_rel_tol=1e-6, pcg_max_iters=2000, forcing=1, refine_max_iters=3, refine_rel_tol=1e-8)
+    # the same inexact-Newton policy for both precisions: PCG to 1e-2 relative
+    # residual (<= 2000 iterations), the fastest-converging mixed policy measured
+    settings = dict(pcg_rel_tol=1e-2, pcg_max_iters=2000, forcing=0, refine_max_iters=3, refine_rel_tol=1e-8)
 
     def make_fn(p):
         fn = tad.ScalarFunction.from_workload(w, precision=p, **settings)
@@ -291,16 +318,16 @@ def main():
             print(json.dumps({"kernels_ms_per_launch": prof, "workload": workload_desc(w), "precision": args.precision}))
         return
 
-    # warm-up
-    fn.newton_solve_device(x.data_ptr(), args.warmup)
-    torch.cuda.synchronize()
-    barrier()
-
-    # timed region: K Newton iterations on the device-resident state
-    launches0 = fn.launch_count
     stage = {"ms_eval": 0.0, "ms_assemble": 0.0, "ms_pcg": 0.0, "ms_linesearch": 0.0, "pcg_iters": 0, "ls_trials": 0}
     fh = []
     with ClockSampler(local) as clk:
+        # warm-up
+        fn.newton_solve_device(x.data_ptr(), args.warmup)
+        torch.cuda.synchronize()
+        x_warm = x.clone()
+        barrier()
+        # timed region: K Newton iterations on the device-resident state
+        launches0 = fn.launch_count
         torch.cuda.synchronize()
         barrier()
         e0 = torch.cuda.Event(enable_timing=True)
@@ -314,22 +341,34 @@ def main():
         e1.record(stream)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
-    launches = fn.launch_count - launches0
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * args.steps / (ms / 1e3)
+        launches = fn.launch_count - launches0
+    ms = reduce_max(ms, dist, "cuda")
+    value = aggregate_rate(world, args.steps, ms / 1e3)
     ms_elem_stage = stage["ms_eval"] + stage["ms_assemble"]
     elem_hess_per_s = world * w.n_elements * args.steps / (ms_elem_stage / 1e3) if ms_elem_stage > 0 else None
+
+    # end to end through the C ABI with host buffers (pinned), the same K
+    # iterations from the same post-warm-up state, one call per step
+    n = w.n_vars
+    xh = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    xh.copy_(x_warm.cpu())
+    xh_np = xh.numpy()
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        fn.newton_solve_inplace(xh_np, 1)
+    t_e2e = time.perf_counter() - t0
+    t_e2e = reduce_max(t_e2e, dist, "cuda")
+    e2e = {"value": aggregate_rate(world, args.steps, t_e2e), "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n + 8,
+           "path": "tad_newton_solve (C ABI) with pinned host x in and out every step, same iterations as the timed region"}
 
     # kernel figures at the final state (CUDA events on the library stream)
     prof = fn.profile_kernels(x.data_ptr(), reps=5)
     nb = fn.hessian_pattern()[1].size // (w.var_dim ** 2)
-    n = w.n_vars
     vb = 4 if prec == tad.PREC_MIXED else 8
-    spmv_bytes = nb * (w.var_dim ** 2 * vb + 4) + (w.n_handles + 1) * 4 + 3 * n * vb
-    pcg_ms = stage["pcg_iters"] * (prof["spmv"] + prof["pcg_update"])
+    # fused SpMV: H blocks + column ids + row pointers + z gathered once + Ap, p read and written
+    spmv_bytes = nb * (w.var_dim ** 2 * vb + 4) + (w.n_handles + 1) * 4 + 5 * n * vb
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -338,31 +377,26 @@ def main():
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     hbm_src = "measured" if "hbm_gbs" in peaks else "fallback"
     spmv_gbs = spmv_bytes / (prof["spmv"] * 1e-3) / 1e9
-    roofline = {"bound": "hbm", "kernel": "k_pcg_spmv (BSR SpMV fused with p.Ap)", "achieved": spmv_gbs,
-                "peak": hbm, "unit": "GB/s", "frac": spmv_gbs / hbm, "traffic": None,
-                "peak_source": f"{hbm_src} copy bandwidth (MEASURED_PEAKS.json hbm_gbs)",
-                "algorithmic_bytes_per_launch": spmv_bytes,
-                "ms_per_launch": prof["spmv"],
-                "share_of_step_est": pcg_ms * prof["spmv"] / max(prof["spmv"] + prof["pcg_update"], 1e-12) / ms}
+    share = {"spmv": stage["pcg_iters"] * prof["spmv"] / ms, "pcg_update": stage["pcg_iters"] * prof["pcg_update"] / ms,
+             "elem_hessian": args.steps * prof["elem_hessian"] / ms,
+             "ls_energy": stage["ls_trials"] * prof["ls_energy"] / ms, "assemble": args.steps * prof["assemble"] / ms}
+    roof_spmv = {"bound": "hbm", "kernel": "k_pcg_spmv_fused (BSR SpMV + p update + p.Ap)", "achieved": spmv_gbs,
+                 "peak": hbm, "unit": "GB/s", "frac": spmv_gbs / hbm, "traffic": None,
+                 "peak_source": f"{hbm_src} copy bandwidth (MEASURED_PEAKS.json hbm_gbs)",
+                 "algorithmic_bytes_per_launch": spmv_bytes, "ms_per_launch": prof["spmv"]}
     fp_peak = tad.measure_fma_peak(prec)
+    k_elem = w.var_dim * w.terms[0].valence
+    elem_flops = ELEM_FLOPS.get(k_elem, 0) * w.terms[0].handles.shape[0]
+    elem_tf = elem_flops / (prof["elem_hessian"] * 1e-3) / 1e12
+    roof_elem = {"bound": "fp32 CUDA-core pipe" if prec == tad.PREC_MIXED else "fp64 CUDA-core pipe",
+                 "kernel": "k_elem_hessian (Double<k> eval + fused PSD projection)", "achieved": elem_tf,
+                 "peak": fp_peak, "unit": "TFLOP/s", "frac": elem_tf / fp_peak, "traffic": None,
+                 "peak_source": "measured FMA throughput (tad_measure_fma_peak, this GPU)",
+                 "algorithmic_flops_per_launch": elem_flops,
+                 "flops_per_element": ELEM_FLOPS.get(k_elem, 0), "ms_per_launch": prof["elem_hessian"]}
+    roofline = dict(roof_elem if share["elem_hessian"] >= share["spmv"] else roof_spmv)
+    roofline["share_of_timed_region_est"] = share
     kernels = {k: round(v, 5) for k, v in prof.items()}
-
-    # end to end through the C ABI with host buffers (pinned), one step per call
-    xh = torch.empty(n, dtype=torch.float64, pin_memory=True)
-    xh.copy_(x.cpu())
-    xh_np = xh.numpy()
-    torch.cuda.synchronize()
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        fn.newton_solve_inplace(xh_np, 1)
-    t_e2e = time.perf_counter() - t0
-    if dist is not None:
-        t = torch.tensor([t_e2e], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_e2e = float(t.item())
-    e2e = {"value": world * args.steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n + 8,
-           "path": "tad_newton_solve (C ABI) with pinned host x in and out every step"}
 
     # FP64 plain path on the same workload (the drop-in), same protocol
     fp64 = None
@@ -370,20 +404,55 @@ def main():
         fd = make_fn(tad.PREC_FP64)
         xd = torch.from_numpy(w.x0.copy()).cuda()
         fd.newton_solve_device(xd.data_ptr(), args.warmup)
-        k64 = max(2, min(args.steps, 4))
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        fd.newton_solve_device(xd.data_ptr(), k64)
+        sd = torch.cuda.ExternalStream(fd.stream_ptr)
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        st64 = {"ms_eval": 0.0, "ms_assemble": 0.0, "pcg_iters": 0}
+        a0.record(sd)
+        for _ in range(args.steps):
+            fd.newton_solve_device(xd.data_ptr(), 1)
+            s2 = fd.last_solve_stats()
+            for k in st64:
+                st64[k] += s2[k]
+        a1.record(sd)
         torch.cuda.synchronize()
-        t64 = time.perf_counter() - t0
-        st64 = fd.last_solve_stats()
+        t64 = a0.elapsed_time(a1) / 1e3
         prof64 = fd.profile_kernels(xd.data_ptr(), reps=2)
-        fp64 = {"value": k64 / t64, "unit": UNIT, "steps": k64,
-                "element_hessians_per_s": w.n_elements * k64 / ((st64["ms_eval"] + st64["ms_assemble"]) / 1e3),
-                "pcg_iters_per_step": st64["pcg_iters"] / k64,
+        fp64 = {"value": args.steps / t64, "unit": UNIT, "steps": args.steps,
+                "element_hessians_per_s": w.n_elements * args.steps / ((st64["ms_eval"] + st64["ms_assemble"]) / 1e3),
+                "pcg_iters_per_step": st64["pcg_iters"] / args.steps,
                 "kernels_ms": {k: round(v, 5) for k, v in prof64.items()},
                 "fp64_fma_peak_tflops": tad.measure_fma_peak(tad.PREC_FP64)}
         del fd
+
+    # solve to 1e-8 energy error: mixed and FP64 from the initial state until the
+    # energy is within 1e-8 of the converged FP64 energy
+    solve = None
+    if not args.no_fp64 and prec == tad.PREC_MIXED and rank == 0:
+        def run_to_convergence(p, max_iter=200, max_s=40.0):
+            f_ = make_fn(p)
+            xx = torch.from_numpy(w.x0.copy()).cuda()
+            hist = []
+            t_start = time.perf_counter()
+            while len(hist) < max_iter and time.perf_counter() - t_start < max_s:
+                fh_ = f_.newton_solve_device(xx.data_ptr(), 1)
+                torch.cuda.synchronize()
+                hist.append((time.perf_counter() - t_start, float(fh_[-1])))
+                if len(hist) > 3 and abs(hist[-1][1] - hist[-3][1]) <= 1e-12 * abs(hist[-1][1]):
+                    break
+            return hist
+        h64 = run_to_convergence(tad.PREC_FP64)
+        hmx = run_to_convergence(tad.PREC_MIXED)
+        fstar = min(h64[-1][1], hmx[-1][1])
+
+        def reach(hist):
+            for i, (t_, f_) in enumerate(hist):
+                if f_ <= fstar * (1 + 1e-8):
+                    return {"iters": i + 1, "seconds": t_}
+            return None
+        solve = {"f_converged_fp64": h64[-1][1], "f_converged_mixed": hmx[-1][1],
+                 "final_energy_rel_err_mixed_vs_fp64": abs(hmx[-1][1] - h64[-1][1]) / abs(h64[-1][1]),
+                 "to_1e-8_fp64": reach(h64), "to_1e-8_mixed": reach(hmx)}
 
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
@@ -396,19 +465,23 @@ def main():
         "data": "synthetic (seeded generator)",
         "config": {"workload": workload_desc(w), "precision": args.precision,
                    "n_vars": n, "n_elements": w.n_elements, "hessian_nnz": int(nb * w.var_dim ** 2),
-                   "newton": "projected Newton, eps=1e-9, inexact PCG (block Jacobi, tol_k = max(1e-6, "
-                             "min(0.5, sqrt(|g_k|/|g_0|))), <= 2000 iters), Armijo line search (0.8, 1e-4, 64)",
+                   "newton": "projected Newton, eps=1e-9, block-Jacobi PCG to 1e-2 relative residual (<= 2000 "
+                             "iterations), Armijo line search (0.8, 1e-4, 64); steps W+1..W+K from the initial state",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                   "l2": "working set per step (element blocks, BSR Hessian, vectors) larger than L2",
+                   "l2": "inputs larger than L2: per-step working set (element blocks 157 MB, BSR Hessian, vectors) > 126 MB",
                    "mesh_generation_s": round(t_gen, 2)},
         "element_hessians_per_s": elem_hess_per_s,
-        "stages_ms_per_step": {k: (v / args.steps if k.startswith("ms") else v / args.steps) for k, v in stage.items()},
+        "stages_ms_per_step": {k: v / args.steps for k, v in stage.items()},
         "kernels_ms_per_launch": kernels,
         "fp_pipe_peak_tflops": fp_peak,
         "f_history": [float(a[0]) for a in fh] + [float(fh[-1][-1])],
         "roofline": roofline,
+        "roofline_spmv": roof_spmv,
+        "roofline_elem": roof_elem,
         "e2e": e2e,
         "fp64_path": fp64,
+        "mixed_vs_fp64_iters_per_s": (value / fp64["value"]) if fp64 else None,
+        "solve": solve,
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
         "gpu_launches": int(launches),

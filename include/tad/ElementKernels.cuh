@@ -18,6 +18,7 @@
  */
 #pragma once
 #include <stdint.h>
+#include <type_traits>
 #include "Scalar.cuh"
 #include "Element.cuh"
 #include "Projection.cuh"
@@ -105,14 +106,21 @@ __global__ void __launch_bounds__(128) k_elem_gradient(ElemLaunch L, Energy ener
     if (!fin) report_error(L.err, DEVERR_NONFINITE);
 }
 
+/* gradient type of the second-order kernel: FP64 for the plain path; for the
+   mixed path double-float up to k = 8 and FP64 beyond (for k = 12 the kernel
+   is bound by register spills of the 78-entry Hessians, not by the gradient's
+   pipe, and the double-float code would only grow the kernel) */
+template <typename T, int K> struct GradOf { using type = double; };
+template <int K> struct GradOf<float, K> { using type = std::conditional_t<(K <= 8), DoubleFloat, double>; };
+
 /* second-order evaluation with the Hessian in T: double (plain Double<k>), or
-   float with FP64 value and gradient (mixed, tad::Mixed<k>). */
+   float with FP64 value and double-float gradient (mixed, tad::Mixed<k>). */
 template <int d, int N, typename T, typename Energy>
 __global__ void __launch_bounds__(128) k_elem_hessian(ElemLaunch L, Energy energy)
 {
     constexpr int k = d * N;
     constexpr int NP = N * (N + 1) / 2;
-    using S = Scalar<k, T, true, double, double>;
+    using S = Scalar<k, T, true, double, typename GradOf<T, k>::type>;
     const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (e >= L.n_elem) return;
     ActiveElement<d, N, S> el;
@@ -127,7 +135,7 @@ __global__ void __launch_bounds__(128) k_elem_hessian(ElemLaunch L, Energy energ
     bool fin = true;
     double* g = (double*)L.out_g + e * k;
 #pragma unroll
-    for (int i = 0; i < k; ++i) { g[i] = (double)r.grad[i]; fin = fin && finite_val(r.grad[i]); }
+    for (int i = 0; i < k; ++i) { const double gi = (double)r.grad[i]; g[i] = gi; fin = fin && finite_val(gi); }
     T* Hb = (T*)L.out_H + e * (NP * d * d);
 #pragma unroll
     for (int a = 0; a < N; ++a)
@@ -172,9 +180,18 @@ inline ElemLaunch make_launch(const tad_term_eval_args& a)
     return L;
 }
 
-/* Launch the kernel for `mode` (tad_eval_mode values) on stream s. */
+/* Second-order kernels (modes 2, 3) in precision T; split from the others
+   so a translation unit can instantiate them alone. */
+template <int d, int N, typename T, typename Energy>
+inline void launch_elements_hessian(const ElemLaunch& L, const Energy& energy, cudaStream_t s)
+{
+    if (L.n_elem <= 0) return;
+    k_elem_hessian<d, N, T, Energy><<<elem_grid(L.n_elem), 128, 0, s>>>(L, energy);
+}
+
+/* Value, gradient, line-search and record kernels (modes 0, 1, 4, 5). */
 template <int d, int N, typename Energy>
-inline void launch_elements(int mode, int precision, const ElemLaunch& L, const Energy& energy, cudaStream_t s)
+inline void launch_elements_first_order(int mode, const ElemLaunch& L, const Energy& energy, cudaStream_t s)
 {
     if (L.n_elem <= 0) return;
     const unsigned g = elem_grid(L.n_elem);
@@ -182,14 +199,21 @@ inline void launch_elements(int mode, int precision, const ElemLaunch& L, const 
     {
     case 0: k_elem_value<d, N, Energy><<<g, 128, 0, s>>>(L, energy); break;
     case 1: k_elem_gradient<d, N, Energy><<<g, 128, 0, s>>>(L, energy); break;
-    case 2:
-    case 3:
-        if (precision == 1) k_elem_hessian<d, N, float, Energy><<<g, 128, 0, s>>>(L, energy);
-        else k_elem_hessian<d, N, double, Energy><<<g, 128, 0, s>>>(L, energy);
-        break;
     case 4: k_elem_linesearch<d, N, Energy><<<g, 128, 0, s>>>(L, energy); break;
     case 5: k_elem_record<d, N, Energy><<<g, 128, 0, s>>>(L, energy); break;
     }
+}
+
+/* Launch the kernel for `mode` (tad_eval_mode values) on stream s. */
+template <int d, int N, typename Energy>
+inline void launch_elements(int mode, int precision, const ElemLaunch& L, const Energy& energy, cudaStream_t s)
+{
+    if (mode == 2 || mode == 3)
+    {
+        if (precision == 1) launch_elements_hessian<d, N, float>(L, energy, s);
+        else launch_elements_hessian<d, N, double>(L, energy, s);
+    }
+    else launch_elements_first_order<d, N>(mode, L, energy, s);
 }
 
 } // namespace tad

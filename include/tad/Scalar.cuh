@@ -17,12 +17,13 @@
  *
  * Precision split: Scalar<k, T, with_hessian, V, G> keeps the value in V,
  * the gradient in G and the Hessian in T.  Mixed<k> = Scalar<k, float, true,
- * double, double> is the mixed-precision scalar: values (edge vectors,
- * Jacobian determinants and inverses, the energy) and the O(k) gradient are
- * FP64, the O(k^2) Hessian arithmetic is FP32.  An FP64 gradient keeps the
- * Newton fixed point, and the gradient's components along (near-)null
- * directions of the Hessian such as rigid motions, at FP64 accuracy.  With
- * V = G = T it is the reference's plain scalar.
+ * double, DoubleFloat> is the mixed-precision scalar: values (edge vectors,
+ * Jacobian determinants and inverses, the energy) are FP64, the O(k)
+ * gradient is double-float (two FP32 words, ~1e-14 relative), and the
+ * O(k^2) Hessian arithmetic is FP32.  A near-FP64 gradient keeps the Newton
+ * fixed point, and the gradient's components along (near-)null directions of
+ * the Hessian such as rigid motions, accurate; an FP32 gradient does not.
+ * With V = G = T it is the reference's plain scalar.
  *
  * All functions are __host__ __device__ so element functors can be written
  * once and run on either side.
@@ -42,6 +43,54 @@ namespace tad {
 
 /* index of (i, j), i <= j, in the packed upper triangle of a k x k matrix */
 TAD_HD constexpr int packed_index(int i, int j, int k) { return i * k - (i * (i - 1)) / 2 + (j - i); }
+
+/* ---------------------------------------------------------------------------
+ * DoubleFloat: an unevaluated sum hi + lo of two floats (~48-bit mantissa),
+ * the gradient type of the mixed-precision scalar.  On GB300 a float FMA
+ * issues at 70x the rate of a double one, so these few-FMA sequences carry
+ * the gradient at near-FP64 accuracy (relative ~1e-14) for a fraction of an
+ * FP64 instruction's cost.  Published algorithms: two-sum (Knuth, TAOCP vol.
+ * 2, 4.2.2), the FMA two-product and Dekker's double-length arithmetic
+ * (T. J. Dekker, "A floating-point technique for extending the available
+ * precision", Numer. Math. 18, 1971).
+ * ------------------------------------------------------------------------ */
+struct DoubleFloat
+{
+    float hi, lo;
+    TAD_HD DoubleFloat() : hi(0.f), lo(0.f) {}
+    TAD_HD DoubleFloat(double x) : hi((float)x), lo((float)(x - (double)(float)x)) {}
+    TAD_HD DoubleFloat(float h, float l) : hi(h), lo(l) {}
+    TAD_HD explicit operator double() const { return (double)hi + (double)lo; }
+    TAD_HD explicit operator float() const { return hi + lo; }
+};
+
+TAD_HD DoubleFloat df_quick_two_sum(float a, float b)
+{
+    const float s = a + b;
+    return DoubleFloat(s, b - (s - a));
+}
+TAD_HD DoubleFloat operator+(DoubleFloat a, DoubleFloat b)
+{
+    const float s = a.hi + b.hi;
+    const float bb = s - a.hi;
+    const float e = (a.hi - (s - bb)) + (b.hi - bb);     // two-sum error
+    return df_quick_two_sum(s, e + a.lo + b.lo);
+}
+TAD_HD DoubleFloat operator-(DoubleFloat a) { return DoubleFloat(-a.hi, -a.lo); }
+TAD_HD DoubleFloat operator-(DoubleFloat a, DoubleFloat b) { return a + (-b); }
+TAD_HD DoubleFloat operator*(DoubleFloat a, DoubleFloat b)
+{
+    const float p = a.hi * b.hi;
+#if defined(__CUDA_ARCH__)
+    float e = __fmaf_rn(a.hi, b.hi, -p);                 // exact product error
+#else
+    float e = std::fma(a.hi, b.hi, -p);
+#endif
+    e += a.hi * b.lo + a.lo * b.hi;
+    return df_quick_two_sum(p, e);
+}
+TAD_HD DoubleFloat& operator+=(DoubleFloat& a, DoubleFloat b) { a = a + b; return a; }
+TAD_HD bool isfinite(DoubleFloat a) { using std::isfinite; return isfinite(a.hi) && isfinite(a.lo); }
 
 template <int K, typename T, bool WithHessian = true, typename V = T, typename G = V>
 struct Scalar
@@ -126,8 +175,8 @@ struct Scalar
 
 template <int K, bool WithHessian = true> using Double = Scalar<K, double, WithHessian>;
 template <int K, bool WithHessian = true> using Float = Scalar<K, float, WithHessian>;
-/* mixed precision: FP64 value and gradient, FP32 Hessian */
-template <int K, bool WithHessian = true> using Mixed = Scalar<K, float, WithHessian, double, double>;
+/* mixed precision: FP64 value, double-float gradient, FP32 Hessian */
+template <int K, bool WithHessian = true> using Mixed = Scalar<K, float, WithHessian, double, DoubleFloat>;
 
 template <typename S> struct is_scalar : std::false_type {};
 template <int K, typename T, bool H, typename V, typename G> struct is_scalar<Scalar<K, T, H, V, G>> : std::true_type {};

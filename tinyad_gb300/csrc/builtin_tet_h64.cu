@@ -1,0 +1,13 @@
+/* Second-order kernel of the built-in tet energy (k = 12), fp64. */
+#include "internal.hh"
+#include "../../include/tad/ElementKernels.cuh"
+#include "../../include/tad/Energies.cuh"
+
+namespace tadlib {
+
+void tet_hessian_fp64(const tad::ElemLaunch& L, const tad::SymmetricDirichletTet& e, cudaStream_t s)
+{
+    tad::launch_elements_hessian<3, 4, double>(L, e, s);
+}
+
+} // namespace tadlib

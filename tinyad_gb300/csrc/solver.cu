@@ -7,14 +7,14 @@
  * Linear solve.  The reference factorises H with Eigen's SimplicialLDLT; a
  * serial sparse factorisation has no good GB300 mapping, so d = -(H + wI)^-1 g
  * is solved by preconditioned conjugate gradients with a block-Jacobi
- * preconditioner (inverted d x d diagonal blocks).  One iteration is three
+ * preconditioner (inverted d x d diagonal blocks).  One iteration is two
  * kernels over a fixed grid (RED_BLOCKS x RED_THREADS, grid-stride):
- *   k_pcg_spmv    Ap = H p (BSR) fused with the p.Ap reduction; the last
- *                 block computes alpha on the device
- *   k_pcg_update  x += alpha p, r -= alpha Ap, z = M^-1 r fused with the r.z
- *                 and r.r reductions; the last block computes beta and sets
- *                 the convergence flag (|r| <= tol |b|) or the iteration cap
- *   k_pcg_pupdate p = z + beta p
+ *   k_pcg_spmv_fused  Ap = H z + beta Ap and p = z + beta p (BSR, one thread
+ *                     per block row), fused with the p.Ap reduction; the last
+ *                     block computes alpha on the device
+ *   k_pcg_update      x += alpha p, r -= alpha Ap, z = M^-1 r fused with the
+ *                     r.z and r.r reductions; the last block computes beta and
+ *                     sets the convergence flag (|r| <= tol |b|) or the cap
  * Scalars never leave the device; every kernel returns at once when the flag
  * is set, so chunks of iterations are captured once in a CUDA graph and
  * replayed, with one host check per replay.  Reductions have a fixed order
@@ -168,10 +168,11 @@ __device__ __forceinline__ void apply_dinv(const T* __restrict__ dinv, int64_t u
     }
 }
 
-/* x = 0, r = b, z = M^-1 r, p = z; rz = r.z, bb = b.b */
+/* x = 0, r = b, z = M^-1 r, p = Ap = 0, beta = 0 (the first fused SpMV then
+   forms p = z, Ap = A z); rz = r.z, bb = b.b */
 template <int d, typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_pcg_init(int64_t nh, const double* __restrict__ b, T* x, T* r, T* z, T* p,
-                                                          const T* __restrict__ dinv, double* partials, unsigned* counter,
+                                                          T* Ap, const T* __restrict__ dinv, double* partials, unsigned* counter,
                                                           DevScalars* ds, double rel_tol, int max_iters)
 {
     double part[2] = {0.0, 0.0};
@@ -185,7 +186,8 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_init(int64_t nh, const doub
         for (int i = 0; i < d; ++i)
         {
             z[u * d + i] = zv[i];
-            p[u * d + i] = zv[i];
+            p[u * d + i] = T(0);
+            Ap[u * d + i] = T(0);
             part[0] += (double)rv[i] * (double)zv[i];
             part[1] += b[u * d + i] * b[u * d + i];
         }
@@ -197,6 +199,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_init(int64_t nh, const doub
         ds->rz = tot[0];
         ds->bb = tot[1];
         ds->rr = tot[1];
+        ds->beta = 0.0;
         ds->tol2 = rel_tol * rel_tol * tot[1];
         ds->iters = 0;
         ds->breakdown = 0;
@@ -251,6 +254,108 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_spmv(int64_t nh, const int3
         else ds->alpha = ds->rz / tot[0];
     }
 }
+
+/* one d x d block of H into registers (16-byte vector loads where the
+   block size allows) */
+template <int d, typename T>
+__device__ __forceinline__ void load_block(const T* __restrict__ B, T (&v)[d * d])
+{
+    if constexpr (d == 2 && sizeof(T) == 4)
+    {
+        const float4 q = __ldg(reinterpret_cast<const float4*>(B));
+        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    }
+    else if constexpr (d == 2 && sizeof(T) == 8)
+    {
+        const double2 q0 = __ldg(reinterpret_cast<const double2*>(B));
+        const double2 q1 = __ldg(reinterpret_cast<const double2*>(B) + 1);
+        v[0] = q0.x; v[1] = q0.y; v[2] = q1.x; v[3] = q1.y;
+    }
+    else
+    {
+#pragma unroll
+        for (int i = 0; i < d * d; ++i) v[i] = __ldg(B + i);
+    }
+}
+
+/* SpMV fused with the p update and the p.Ap reduction:
+     Ap = A z + beta Ap,  p = z + beta p  (A p_new = A z + beta A p_old),
+   so p is never gathered and the separate p = z + beta p pass disappears.
+   One thread per block row; the block loop is unrolled four ways so four
+   column ids, four blocks and four z gathers are in flight at once (the
+   row-at-a-time loop was latency-bound on the bcol -> z dependency). */
+template <int d, typename T, int G>
+__global__ void __launch_bounds__(RED_THREADS) k_pcg_spmv_fused(int64_t nh, const int32_t* __restrict__ bptr,
+                                                                const int32_t* __restrict__ bcol, const T* __restrict__ H,
+                                                                const T* __restrict__ z, T* __restrict__ p, T* __restrict__ Ap,
+                                                                double* partials, unsigned* counter, DevScalars* ds)
+{
+    if (*(volatile int32_t*)&ds->done) return;
+    const T beta = (T)ds->beta;
+    T part = T(0);
+    GRID_STRIDE(u, nh)
+    {
+        T y[d];
+#pragma unroll
+        for (int i = 0; i < d; ++i) y[i] = T(0);
+        int32_t b = bptr[u];
+        const int32_t b1 = bptr[u + 1];
+        for (; b + 4 <= b1; b += 4)
+        {
+            int64_t v[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) v[k] = __ldg(bcol + b + k);
+            T B[4][d * d], zv[4][d];
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+            {
+                load_block<d, T>(H + (int64_t)(b + k) * d * d, B[k]);
+#pragma unroll
+                for (int j = 0; j < d; ++j) zv[k][j] = z[v[k] * d + j];
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+#pragma unroll
+                for (int i = 0; i < d; ++i)
+#pragma unroll
+                    for (int j = 0; j < d; ++j) y[i] += B[k][i * d + j] * zv[k][j];
+        }
+        for (; b < b1; ++b)
+        {
+            const int64_t v = __ldg(bcol + b);
+            T B[d * d];
+            load_block<d, T>(H + (int64_t)b * d * d, B);
+#pragma unroll
+            for (int i = 0; i < d; ++i)
+#pragma unroll
+                for (int j = 0; j < d; ++j) y[i] += B[i * d + j] * z[v * d + j];
+        }
+#pragma unroll
+        for (int i = 0; i < d; ++i)
+        {
+            const T apn = y[i] + beta * Ap[u * d + i];
+            const T pn = z[u * d + i] + beta * p[u * d + i];
+            Ap[u * d + i] = apn;
+            p[u * d + i] = pn;
+            part += pn * apn;
+        }
+    }
+    double v[1] = {(double)part}, tot[1];
+    if (!grid_sum<1>(v, partials, counter, tot)) return;
+    if (threadIdx.x == 0)
+    {
+        ds->pAp = tot[0];
+        if (!(tot[0] > 0.0) || !isfinite(tot[0]))
+        {
+            ds->breakdown = 1;
+            ds->done = 1;
+            ds->alpha = 0.0;
+        }
+        else ds->alpha = ds->rz / tot[0];
+    }
+}
+
+template <int d> struct SpmvGroup { static constexpr int value = d == 3 ? 16 : 8; };
 
 template <int d, typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_pcg_update(int64_t nh, T* x, T* r, T* z, const T* __restrict__ p, const T* __restrict__ Ap,
@@ -400,7 +505,7 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
     const int64_t nh = P.n_handles, n = P.n_vars;
     cudaStream_t s = P.stream;
     k_diag_inv<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, P.diag, H, w, dinv);
-    k_pcg_init<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, b, xs, r, z, p, dinv, P.partials, P.counters, P.ds, rel_tol, max_iters);
+    k_pcg_init<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, b, xs, r, z, p, Ap, dinv, P.partials, P.counters, P.ds, rel_tol, max_iters);
     P.n_launches += 2;
     TAD_CUDA_TRY(cudaGetLastError());
     // CHUNK iterations captured once per (precision, solution buffer)
@@ -412,9 +517,9 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
         TAD_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         for (int it = 0; it < CHUNK; ++it)
         {
-            k_pcg_spmv<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, P.bptr, P.bcol, H, p, Ap, P.partials, P.counters + 1, P.ds);
+            k_pcg_spmv_fused<d, T, SpmvGroup<d>::value><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, P.bptr, P.bcol, H, z, p, Ap,
+                                                                                      P.partials, P.counters + 1, P.ds);
             k_pcg_update<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, xs, r, z, p, Ap, dinv, P.partials, P.counters + 2, P.ds);
-            k_pcg_pupdate<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, z, p, P.ds);
         }
         TAD_CUDA_TRY(cudaStreamEndCapture(s, &graph));
         TAD_CUDA_TRY(cudaGraphInstantiate(&P.pcg_graph, graph, 0));
@@ -427,7 +532,7 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
     for (;;)
     {
         for (int k = 0; k < replays_between_checks; ++k) TAD_CUDA_TRY(cudaGraphLaunch(P.pcg_graph, s));
-        P.n_launches += 3 * CHUNK * replays_between_checks;
+        P.n_launches += 2 * CHUNK * replays_between_checks;
         TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
         TAD_CUDA_TRY(cudaStreamSynchronize(s));
         if (P.hs->done) break;
@@ -703,20 +808,22 @@ TAD_API tad_status tad_profile_kernels(tad_problem* P, const double* x_d, int re
     if (prec == TAD_PREC_MIXED)                                                                                     \
     {                                                                                                               \
         k_diag_inv<D, float><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.diag, (const float*)Q.H, 0.0, Q.dinv32);     \
-        k_pcg_init<D, float><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.rhs, Q.dx32, Q.r32, Q.z32, Q.p32, Q.dinv32,  \
-                                                                 Q.partials, Q.counters, Q.ds, 1e-30, 1 << 30);     \
-        ms5[2] = timed([&] { k_pcg_spmv<D, float><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.bptr, Q.bcol,          \
-                               (const float*)Q.H, Q.p32, Q.Ap32, Q.partials, Q.counters + 1, Q.ds); });               \
+        k_pcg_init<D, float><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.rhs, Q.dx32, Q.r32, Q.z32, Q.p32, Q.Ap32,    \
+                                                                 Q.dinv32, Q.partials, Q.counters, Q.ds, 1e-30, 1 << 30); \
+        ms5[2] = timed([&] { k_pcg_spmv_fused<D, float, SpmvGroup<D>::value><<<RED_BLOCKS, RED_THREADS, 0, st>>>(   \
+                               nh, Q.bptr, Q.bcol, (const float*)Q.H, Q.z32, Q.p32, Q.Ap32, Q.partials,              \
+                               Q.counters + 1, Q.ds); });                                                             \
         ms5[3] = timed([&] { k_pcg_update<D, float><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.dx32, Q.r32, Q.z32,  \
                                Q.p32, Q.Ap32, Q.dinv32, Q.partials, Q.counters + 2, Q.ds); });                       \
     }                                                                                                               \
     else                                                                                                            \
     {                                                                                                               \
         k_diag_inv<D, double><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.diag, (const double*)Q.H, 0.0, Q.dinv);     \
-        k_pcg_init<D, double><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.rhs, Q.dx, Q.r, Q.z, Q.p, Q.dinv,           \
+        k_pcg_init<D, double><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.rhs, Q.dx, Q.r, Q.z, Q.p, Q.Ap, Q.dinv,     \
                                                                   Q.partials, Q.counters, Q.ds, 1e-30, 1 << 30);    \
-        ms5[2] = timed([&] { k_pcg_spmv<D, double><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.bptr, Q.bcol,         \
-                               (const double*)Q.H, Q.p, Q.Ap, Q.partials, Q.counters + 1, Q.ds); });                  \
+        ms5[2] = timed([&] { k_pcg_spmv_fused<D, double, SpmvGroup<D>::value><<<RED_BLOCKS, RED_THREADS, 0, st>>>(  \
+                               nh, Q.bptr, Q.bcol, (const double*)Q.H, Q.z, Q.p, Q.Ap, Q.partials,                   \
+                               Q.counters + 1, Q.ds); });                                                             \
         ms5[3] = timed([&] { k_pcg_update<D, double><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.dx, Q.r, Q.z,       \
                                Q.p, Q.Ap, Q.dinv, Q.partials, Q.counters + 2, Q.ds); });                             \
     }
