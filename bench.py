@@ -90,57 +90,129 @@ def workload_desc(w) -> str:
 
 # ---------------------------------------------------------------------------
 # clocks sampled during the timed region
-# ---------------------------------------------------------------------------
+# NVML clock-event reason bits (nvml.h, nvmlClocksEventReason*)
+_NVML_REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+                 0x80: "hw_power_brake_slowdown"}
+
+
 class ClockSampler:
-    def __init__(self, index: int = 0):
+    """Samples the SM clock and the clock-event reasons of this process's GPU
+    every ~2 ms through NVML (read-only queries), so that even a timed region
+    of a few tens of milliseconds gets samples; mark() / unmark() bracket the
+    timed region.  Falls back to `nvidia-smi -lms 100` when NVML cannot be
+    loaded."""
+
+    def __init__(self, cuda_index: int = 0, period_s: float = 0.002):
+        self.cuda_index = cuda_index
+        self.period = period_s
+        self.samples = []          # (t, sm_mhz, reasons_mask, in_region)
+        self.max_mhz = None
+        self.in_region = False
+        self.stop = threading.Event()
         self.proc = None
-        self.lines = []
-        self.index = index
+        self.source = None
+
+    def _nvml_handle(self):
+        import ctypes
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        h = ctypes.c_void_p()
+        ok = False
+        try:
+            import torch
+            uuid = str(torch.cuda.get_device_properties(self.cuda_index).uuid)
+            ok = lib.nvmlDeviceGetHandleByUUID(("GPU-" + uuid).encode(), ctypes.byref(h)) == 0
+        except Exception:
+            ok = False
+        if not ok:
+            vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+            ids = [v for v in vis.split(",") if v.strip()]
+            idx = int(ids[self.cuda_index]) if ids and ids[self.cuda_index].strip().isdigit() else self.cuda_index
+            if lib.nvmlDeviceGetHandleByIndex_v2(idx, ctypes.byref(h)) != 0:
+                raise OSError("no NVML handle")
+        return lib, h
+
+    def _run_nvml(self, lib, h):
+        import ctypes
+        clk = ctypes.c_uint()
+        mask = ctypes.c_ulonglong()
+        get_reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        while not self.stop.is_set():
+            if lib.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(clk)) == 0:   # NVML_CLOCK_SM
+                r = get_reasons(h, ctypes.byref(mask))
+                self.samples.append((time.perf_counter(), float(clk.value), int(mask.value) if r == 0 else 0,
+                                     self.in_region))
+            time.sleep(self.period)
 
     def __enter__(self):
-        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
-             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+        try:
+            import ctypes
+            lib, h = self._nvml_handle()
+            mx = ctypes.c_uint()
+            if lib.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0:
+                self.max_mhz = float(mx.value)
+            self.source = "nvml (2 ms polling)"
+            self.t = threading.Thread(target=self._run_nvml, args=(lib, h), daemon=True)
+            self.t.start()
+        except Exception:
+            self._start_smi()
+        return self
+
+    def _start_smi(self):
+        q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        bits = [0x8, 0x40, 0x20, 0x4]
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
-                                          "-i", str(self.index), "-lms", "200"],
+                                          "-i", str(self.cuda_index), "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.t = threading.Thread(target=self._read, daemon=True)
+            self.source = "nvidia-smi -lms 100"
+
+            def read():
+                for line in self.proc.stdout:
+                    parts = [x.strip() for x in line.split(",")]
+                    try:
+                        sm, mx = float(parts[0]), float(parts[1])
+                    except (ValueError, IndexError):
+                        continue
+                    self.max_mhz = mx
+                    m = sum(b for b, v in zip(bits, parts[2:6]) if v.lower() in ("active", "1", "yes"))
+                    self.samples.append((time.perf_counter(), sm, m, self.in_region))
+            self.t = threading.Thread(target=read, daemon=True)
             self.t.start()
         except Exception:
             self.proc = None
-        return self
 
-    def _read(self):
-        for line in self.proc.stdout:
-            self.lines.append(line.strip())
+    def mark(self):
+        self.in_region = True
+
+    def unmark(self):
+        self.in_region = False
 
     def __exit__(self, *a):
+        self.stop.set()
         if self.proc:
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
             except Exception:
                 self.proc.kill()
+        elif getattr(self, "t", None) is not None:
+            self.t.join(timeout=1)
 
     def summary(self) -> dict:
-        sm, mx, reasons = [], None, set()
-        for ln in self.lines:
-            parts = [p.strip() for p in ln.split(",")]
-            if len(parts) < 9:
-                continue
-            try:
-                sm.append(float(parts[1]))
-                mx = float(parts[2])
-            except ValueError:
-                continue
-            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-            for nm, v in zip(names, parts[5:9]):
-                if v.lower() in ("active", "1", "yes"):
-                    reasons.add(nm)
-        sm.sort()
-        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        region = [s for s in self.samples if s[3]]
+        use = region if region else self.samples
+        sm = sorted(s[1] for s in use)
+        mask = 0
+        for s in use:
+            mask |= s[2]
+        reasons = sorted(nm for bit, nm in _NVML_REASONS.items() if mask & bit)
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": self.max_mhz, "reasons": reasons,
+                "samples": len(sm), "window": "timed region" if region else "whole run (no sample inside the region)",
+                "source": self.source}
 
 
 # ---------------------------------------------------------------------------
@@ -221,6 +293,7 @@ def run_batch(args, rank: int):
     t_gen = time.perf_counter() - t0
     n_faces = sum(w.n_elements for w in ws)
     res = {}
+    clk = ClockSampler(torch.cuda.current_device()).__enter__()
     for name, prec in (("mixed", tad.PREC_MIXED), ("fp64", tad.PREC_FP64)):
         b = tad.Batch(ws, precision=prec, pcg_rel_tol=1e-2, pcg_max_iters=64)
         x = torch.from_numpy(b.x0()).cuda()
@@ -229,10 +302,13 @@ def run_batch(args, rank: int):
         stream = torch.cuda.ExternalStream(b.stream_ptr)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if name == "mixed":
+            clk.mark()
         e0.record(stream)
         b.newton_solve_device(x.data_ptr(), args.steps)
         e1.record(stream)
         torch.cuda.synchronize()
+        clk.unmark()
         ms = e0.elapsed_time(e1)
         fh = b.newton_solve_device(x.data_ptr(), 1, history=True)
         res[name] = {"batch_iters_per_s": args.steps / (ms / 1e3), "mesh_iters_per_s": n_meshes * args.steps / (ms / 1e3),
@@ -265,6 +341,8 @@ def run_batch(args, rank: int):
             "mixed_vs_fp64": res["mixed"]["batch_iters_per_s"] / res["fp64"]["batch_iters_per_s"],
             "sequential_single_problem_ms_per_iteration": t_seq * 1e3,
             "batched_vs_sequential": t_seq * 1e3 / res["mixed"]["ms_per_iteration"]}
+    clk.__exit__(None, None, None)
+    line["clocks"] = clk.summary()
     print(json.dumps(line), flush=True)
 
 
@@ -332,6 +410,7 @@ def main():
         barrier()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
+        clk.mark()
         e0.record(stream)
         for _ in range(args.steps):
             fh.append(fn.newton_solve_device(x.data_ptr(), 1))
@@ -340,6 +419,7 @@ def main():
                 stage[k] += st[k]
         e1.record(stream)
         torch.cuda.synchronize()
+        clk.unmark()
         ms = e0.elapsed_time(e1)
         launches = fn.launch_count - launches0
     ms = reduce_max(ms, dist, "cuda")

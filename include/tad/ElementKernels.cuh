@@ -113,6 +113,18 @@ __global__ void __launch_bounds__(128) k_elem_gradient(ElemLaunch L, Energy ener
 template <typename T, int K> struct GradOf { using type = double; };
 template <int K> struct GradOf<float, K> { using type = std::conditional_t<(K <= 8), DoubleFloat, double>; };
 
+/* For k <= 8 the PSD projection runs in its own kernel (k_project_blocks)
+   over the element blocks the evaluation kernel wrote: the evaluation needs
+   ~250 registers a thread for the live Scalar<k> intermediates, the k = 6
+   projection (packed matrix + eigenvectors) under 100, so apart it runs at
+   about three times the occupancy for the price of re-reading and
+   re-writing the blocks once (measured on the 1.64M-face disk, FP32:
+   1.34 ms fused, 1.17 ms split).  At k = 12 the projection alone (78 + 144
+   entries) exceeds the register file of a thread either way and the second
+   pass only adds traffic (13.6 ms fused, 18.4 ms split on 663,552 tets), so
+   it stays fused. */
+template <int k> struct FusedProjection { static constexpr bool value = k > 8; };
+
 /* second-order evaluation with the Hessian in T: double (plain Double<k>), or
    float with FP64 value and double-float gradient (mixed, tad::Mixed<k>). */
 template <int d, int N, typename T, typename Energy>
@@ -130,7 +142,7 @@ __global__ void __launch_bounds__(128) k_elem_hessian(ElemLaunch L, Energy energ
 #pragma unroll
     for (int i = 0; i < N; ++i) el.vh[i] = L.rec[e * N + i];
     S r = energy(el);
-    if (L.project) project_positive_definite<k, T>(r.hess, (T)L.eps);
+    if (FusedProjection<k>::value && L.project) project_positive_definite<k, T>(r.hess, (T)L.eps);
     L.out_f[e] = (double)r.val;
     bool fin = true;
     double* g = (double*)L.out_g + e * k;
@@ -155,6 +167,45 @@ __global__ void __launch_bounds__(128) k_elem_hessian(ElemLaunch L, Energy energ
                 }
         }
     if (!fin) report_error(L.err, DEVERR_NONFINITE);
+}
+
+/* Projection of the element blocks (layout of k_elem_hessian: NP vertex-pair
+   blocks of d x d, row-major) in place, one element per thread. */
+template <int d, int N, typename T>
+__global__ void __launch_bounds__(128) k_project_blocks(int64_t n_elem, T* __restrict__ Hblocks, T eps)
+{
+    constexpr int k = d * N;
+    constexpr int NP = N * (N + 1) / 2;
+    constexpr int BS = NP * d * d;
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= n_elem) return;
+    T* Hb = Hblocks + e * BS;
+    T h[k * (k + 1) / 2];
+#pragma unroll
+    for (int a = 0; a < N; ++a)
+#pragma unroll
+        for (int b = a; b < N; ++b)
+#pragma unroll
+            for (int p = 0; p < d; ++p)
+#pragma unroll
+                for (int q = 0; q < d; ++q)
+                {
+                    const int i = a * d + p, j = b * d + q;
+                    if (i <= j) h[packed_index(i, j, k)] = Hb[packed_index(a, b, N) * d * d + p * d + q];
+                }
+    if (!project_positive_definite<k, T>(h, eps)) return;
+#pragma unroll
+    for (int a = 0; a < N; ++a)
+#pragma unroll
+        for (int b = a; b < N; ++b)
+#pragma unroll
+            for (int p = 0; p < d; ++p)
+#pragma unroll
+                for (int q = 0; q < d; ++q)
+                {
+                    const int i = a * d + p, j = b * d + q;
+                    Hb[packed_index(a, b, N) * d * d + p * d + q] = (i <= j) ? h[packed_index(i, j, k)] : h[packed_index(j, i, k)];
+                }
 }
 
 inline unsigned elem_grid(int64_t n) { return (unsigned)((n + 127) / 128); }
@@ -187,6 +238,9 @@ inline void launch_elements_hessian(const ElemLaunch& L, const Energy& energy, c
 {
     if (L.n_elem <= 0) return;
     k_elem_hessian<d, N, T, Energy><<<elem_grid(L.n_elem), 128, 0, s>>>(L, energy);
+    if constexpr (!FusedProjection<d * N>::value)
+        if (L.project)
+        k_project_blocks<d, N, T><<<elem_grid(L.n_elem), 128, 0, s>>>(L.n_elem, (T*)L.out_H, (T)L.eps);
 }
 
 /* Value, gradient, line-search and record kernels (modes 0, 1, 4, 5). */
