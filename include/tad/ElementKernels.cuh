@@ -106,10 +106,13 @@ __global__ void __launch_bounds__(128) k_elem_gradient(ElemLaunch L, Energy ener
     if (!fin) report_error(L.err, DEVERR_NONFINITE);
 }
 
-/* gradient type of the second-order kernel: FP64 for the plain path; for the
-   mixed path double-float up to k = 8 and FP64 beyond (for k = 12 the kernel
-   is bound by register spills of the 78-entry Hessians, not by the gradient's
-   pipe, and the double-float code would only grow the kernel) */
+/* value and gradient types of the second-order kernel: FP64 for the plain
+   path; for the mixed path double-float (FP32-pipe arithmetic, ~48-bit
+   significand) up to k = 8 and FP64 beyond (for k = 12 the kernel is bound
+   by register spills of the 78-entry Hessians, and the double-float code
+   would only grow it) */
+template <typename T, int K> struct ValOf { using type = double; };
+template <int K> struct ValOf<float, K> { using type = std::conditional_t<(K <= 8), DoubleFloatValue, double>; };
 template <typename T, int K> struct GradOf { using type = double; };
 template <int K> struct GradOf<float, K> { using type = std::conditional_t<(K <= 8), DoubleFloat, double>; };
 
@@ -132,7 +135,7 @@ __global__ void __launch_bounds__(128) k_elem_hessian(ElemLaunch L, Energy energ
 {
     constexpr int k = d * N;
     constexpr int NP = N * (N + 1) / 2;
-    using S = Scalar<k, T, true, double, typename GradOf<T, k>::type>;
+    using S = Scalar<k, T, true, typename ValOf<T, k>::type, typename GradOf<T, k>::type>;
     const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (e >= L.n_elem) return;
     ActiveElement<d, N, S> el;

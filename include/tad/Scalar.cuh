@@ -92,6 +92,137 @@ TAD_HD DoubleFloat operator*(DoubleFloat a, DoubleFloat b)
 TAD_HD DoubleFloat& operator+=(DoubleFloat& a, DoubleFloat b) { a = a + b; return a; }
 TAD_HD bool isfinite(DoubleFloat a) { using std::isfinite; return isfinite(a.hi) && isfinite(a.lo); }
 
+/* Value channel of the mixed-precision scalar: the unevaluated sum hi + lo of
+   two floats (a ~48-bit significand) computed on the FP32 pipe, so that no
+   FP64 instruction or double <-> float conversion is left inside the
+   per-operation work of a mixed element kernel.  Unlike the gradient's
+   DoubleFloat it carries the full passive semantics element functors rely
+   on: accurate addition (two-sum on both parts, so differences such as
+   determinants keep their relative accuracy), division and square root (the
+   float quotient / root plus one Newton correction computed from the exact
+   FMA residual), comparisons, the elementary functions (evaluated in double
+   and split back; rare in energies), and IEEE propagation of infinities and
+   NaNs (a non-finite hi part travels with lo = 0).  Methods: Knuth's
+   two-sum, Dekker's product (here via FMA) and the double-double division
+   and square root of Hida, Li and Bailey (2001), in float. */
+struct DoubleFloatValue
+{
+    float hi, lo;
+    TAD_HD DoubleFloatValue() : hi(0.f), lo(0.f) {}
+    TAD_HD DoubleFloatValue(double x) : hi((float)x), lo(0.f)
+    {
+        using std::isfinite;
+        if (isfinite(hi)) lo = (float)(x - (double)hi);
+    }
+    TAD_HD DoubleFloatValue(float x) : hi(x), lo(0.f) {}
+    template <typename I, typename = std::enable_if_t<std::is_integral<I>::value>>
+    TAD_HD DoubleFloatValue(I x) : DoubleFloatValue((double)x) {}
+    TAD_HD DoubleFloatValue(float h, float l) : hi(h), lo(l) {}
+    TAD_HD explicit operator double() const { return (double)hi + (double)lo; }
+    TAD_HD explicit operator float() const { return hi + lo; }
+    TAD_HD explicit operator DoubleFloat() const { return DoubleFloat(hi, lo); }
+};
+
+TAD_HD float dfv_fma(float a, float b, float c)
+{
+#if defined(__CUDA_ARCH__)
+    return __fmaf_rn(a, b, c);
+#else
+    return std::fma(a, b, c);
+#endif
+}
+TAD_HD bool dfv_finite(float v) { using std::isfinite; return isfinite(v); }
+TAD_HD DoubleFloatValue dfv_quick(float s, float e)
+{
+    const float t = s + e;
+    return DoubleFloatValue(t, e - (t - s));
+}
+TAD_HD DoubleFloatValue operator+(DoubleFloatValue a, DoubleFloatValue b)
+{
+    const float s = a.hi + b.hi;
+    if (!dfv_finite(s)) return DoubleFloatValue(s, 0.f);
+    const float v = s - a.hi;
+    float e = (a.hi - (s - v)) + (b.hi - v);
+    const float t = a.lo + b.lo;
+    const float w = t - a.lo;
+    const float f = (a.lo - (t - w)) + (b.lo - w);
+    // full two-sum here: when the hi parts cancel, e + t can exceed s
+    e += t;
+    const float r = s + e;
+    const float z = r - s;
+    const float rl = (s - (r - z)) + (e - z);
+    return dfv_quick(r, rl + f);
+}
+TAD_HD DoubleFloatValue operator-(DoubleFloatValue a) { return DoubleFloatValue(-a.hi, -a.lo); }
+TAD_HD DoubleFloatValue operator-(DoubleFloatValue a, DoubleFloatValue b) { return a + (-b); }
+TAD_HD DoubleFloatValue operator*(DoubleFloatValue a, DoubleFloatValue b)
+{
+    const float p = a.hi * b.hi;
+    if (!dfv_finite(p)) return DoubleFloatValue(p, 0.f);
+    float e = dfv_fma(a.hi, b.hi, -p);
+    e = dfv_fma(a.hi, b.lo, e);
+    e = dfv_fma(a.lo, b.hi, e);
+    return dfv_quick(p, e);
+}
+TAD_HD DoubleFloatValue operator/(DoubleFloatValue a, DoubleFloatValue b)
+{
+    const float q1 = a.hi / b.hi;
+    if (!dfv_finite(q1) || !dfv_finite(b.hi) || q1 == 0.f) return DoubleFloatValue(q1, 0.f);
+    // a - q1 b, with q1 b.hi exact through the FMA residual
+    const float ph = q1 * b.hi;
+    const float pl = dfv_fma(q1, b.lo, dfv_fma(q1, b.hi, -ph));
+    const float r = ((a.hi - ph) - pl) + a.lo;
+    return dfv_quick(q1, r / b.hi);
+}
+TAD_HD DoubleFloatValue& operator+=(DoubleFloatValue& a, DoubleFloatValue b) { a = a + b; return a; }
+TAD_HD DoubleFloatValue& operator-=(DoubleFloatValue& a, DoubleFloatValue b) { a = a - b; return a; }
+TAD_HD DoubleFloatValue& operator*=(DoubleFloatValue& a, DoubleFloatValue b) { a = a * b; return a; }
+TAD_HD DoubleFloatValue& operator/=(DoubleFloatValue& a, DoubleFloatValue b) { a = a / b; return a; }
+TAD_HD bool operator<(DoubleFloatValue a, DoubleFloatValue b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+TAD_HD bool operator>(DoubleFloatValue a, DoubleFloatValue b) { return b < a; }
+TAD_HD bool operator<=(DoubleFloatValue a, DoubleFloatValue b) { return a.hi < b.hi || (a.hi == b.hi && a.lo <= b.lo); }
+TAD_HD bool operator>=(DoubleFloatValue a, DoubleFloatValue b) { return b <= a; }
+TAD_HD bool operator==(DoubleFloatValue a, DoubleFloatValue b) { return a.hi == b.hi && a.lo == b.lo; }
+TAD_HD bool operator!=(DoubleFloatValue a, DoubleFloatValue b) { return !(a == b); }
+TAD_HD DoubleFloatValue sqrt(DoubleFloatValue a)
+{
+    using std::sqrt;
+    const float y = sqrt(a.hi);
+    if (!(a.hi > 0.f) || !dfv_finite(a.hi)) return DoubleFloatValue(y, 0.f);
+    // a - y^2 from the exact square (FMA residual), then y + (a - y^2) / (2y)
+    const float yy = y * y;
+    const float r = ((a.hi - yy) - dfv_fma(y, y, -yy)) + a.lo;
+    return dfv_quick(y, r / (2.f * y));
+}
+TAD_HD DoubleFloatValue fabs(DoubleFloatValue a) { return a.hi < 0.f ? -a : a; }
+TAD_HD DoubleFloatValue abs(DoubleFloatValue a) { return fabs(a); }
+TAD_HD DoubleFloatValue sqr(DoubleFloatValue a) { return a * a; }
+TAD_HD bool isfinite(DoubleFloatValue a) { return dfv_finite(a.hi); }
+TAD_HD bool isnan(DoubleFloatValue a) { using std::isnan; return isnan(a.hi); }
+TAD_HD bool isinf(DoubleFloatValue a) { using std::isinf; return isinf(a.hi); }
+#define TAD_DFV_VIA_DOUBLE(F)                                                                              \
+    TAD_HD DoubleFloatValue F(DoubleFloatValue a) { using std::F; return DoubleFloatValue(F((double)a)); }
+TAD_DFV_VIA_DOUBLE(exp)
+TAD_DFV_VIA_DOUBLE(log)
+TAD_DFV_VIA_DOUBLE(log2)
+TAD_DFV_VIA_DOUBLE(log10)
+TAD_DFV_VIA_DOUBLE(sin)
+TAD_DFV_VIA_DOUBLE(cos)
+TAD_DFV_VIA_DOUBLE(tan)
+TAD_DFV_VIA_DOUBLE(asin)
+TAD_DFV_VIA_DOUBLE(acos)
+TAD_DFV_VIA_DOUBLE(atan)
+TAD_DFV_VIA_DOUBLE(sinh)
+TAD_DFV_VIA_DOUBLE(cosh)
+TAD_DFV_VIA_DOUBLE(tanh)
+TAD_DFV_VIA_DOUBLE(asinh)
+TAD_DFV_VIA_DOUBLE(acosh)
+TAD_DFV_VIA_DOUBLE(atanh)
+#undef TAD_DFV_VIA_DOUBLE
+TAD_HD DoubleFloatValue atan2(DoubleFloatValue y, DoubleFloatValue x) { using std::atan2; return DoubleFloatValue(atan2((double)y, (double)x)); }
+TAD_HD DoubleFloatValue pow(DoubleFloatValue a, DoubleFloatValue e) { using std::pow; return DoubleFloatValue(pow((double)a, (double)e)); }
+TAD_HD DoubleFloatValue pow(DoubleFloatValue a, int e) { using std::pow; return DoubleFloatValue(pow((double)a, e)); }
+
 template <int K, typename T, bool WithHessian = true, typename V = T, typename G = V>
 struct Scalar
 {
@@ -175,8 +306,8 @@ struct Scalar
 
 template <int K, bool WithHessian = true> using Double = Scalar<K, double, WithHessian>;
 template <int K, bool WithHessian = true> using Float = Scalar<K, float, WithHessian>;
-/* mixed precision: FP64 value, double-float gradient, FP32 Hessian */
-template <int K, bool WithHessian = true> using Mixed = Scalar<K, float, WithHessian, double, DoubleFloat>;
+/* mixed precision: double-float value and gradient, FP32 Hessian */
+template <int K, bool WithHessian = true> using Mixed = Scalar<K, float, WithHessian, DoubleFloatValue, DoubleFloat>;
 
 template <typename S> struct is_scalar : std::false_type {};
 template <int K, typename T, bool H, typename V, typename G> struct is_scalar<Scalar<K, T, H, V, G>> : std::true_type {};
@@ -189,7 +320,7 @@ TAD_HD V to_passive(const Scalar<K, T, H, V, G>& a) { return a.val; }
 
 #define TAD_S Scalar<K, T, H, V, G>
 #define TAD_TPL template <int K, typename T, bool H, typename V, typename G>
-#define TAD_TPLU template <int K, typename T, bool H, typename V, typename G, typename U, typename = std::enable_if_t<std::is_arithmetic<U>::value>>
+#define TAD_TPLU template <int K, typename T, bool H, typename V, typename G, typename U, typename = std::enable_if_t<std::is_arithmetic<U>::value || std::is_same<U, V>::value>>
 
 /* ---- unary -------------------------------------------------------------- */
 TAD_TPL TAD_HD TAD_S operator-(const TAD_S& a)                              // Scalar.hh:220-234
@@ -245,7 +376,7 @@ TAD_TPL TAD_HD TAD_S pow(const TAD_S& a, int e)                              // 
     return TAD_S::chain(f1 * a.val, V(e) * f1, V(e * (e - 1)) * f2, a);
 }
 
-template <int K, typename T, bool H, typename V, typename G, typename U, typename = std::enable_if_t<std::is_floating_point<U>::value>>
+template <int K, typename T, bool H, typename V, typename G, typename U, typename = std::enable_if_t<std::is_floating_point<U>::value || std::is_same<U, V>::value>>
 TAD_HD TAD_S pow(const TAD_S& a, U eu)                                       // Scalar.hh:291-307
 {
     using std::pow;

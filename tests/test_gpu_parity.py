@@ -229,11 +229,11 @@ def test_newton_direction_api(tad, oracle):
 
 
 def test_mixed_precision(tad, oracle):
-    """Mixed mode: FP32 element Hessians, projection and PCG; FP64 values
-    (edge vectors, determinant, inverse, energy), gradient, line-search
-    energy and refinement residuals.  f and g match the FP64 oracle, H carries
-    FP32 rounding, and the Newton loop reaches the FP64 final energy within
-    1e-8 relative."""
+    """Mixed mode: FP32 element Hessians, projection and PCG; double-float
+    (~48-bit) values (edge vectors, determinant, inverse, energy) and
+    gradient in the element kernel; FP64 line-search energy and refinement
+    residuals.  f and g match the FP64 oracle, H carries FP32 rounding, and
+    the Newton loop reaches the FP64 final energy within 1e-8 relative."""
     w = meshes.disk_param(64, seed=0)
     fm = tad.ScalarFunction.from_workload(w, precision=tad.PREC_MIXED, pcg_rel_tol=1e-8, pcg_max_iters=2000)
     p = oracle.Problem.from_workload(w)

@@ -31,6 +31,11 @@ namespace tadlib {
 
 constexpr int LS_BATCH = 8;        // trial step sizes evaluated per launch
 constexpr int RED_BLOCKS = 608;    // 4 x 152 SMs: fixed grid of the reductions
+/* grid of the PCG SpMV: 8 x 152 SMs x 256 threads = 2048 threads per SM,
+   full occupancy at <= 32 registers, so each SM keeps as many block-row
+   gathers in flight as it can (the vector-update kernel stays on the
+   reduction grid: measured faster there) */
+constexpr int PCG_BLOCKS = 1216;
 constexpr int RED_THREADS = 256;
 
 void set_error(const std::string& msg);

@@ -371,6 +371,7 @@ TAD_API tad_status tad_problem_create(int var_dim, int64_t n_handles, const tad_
     TAD_CUDA_TRY(cudaMallocHost(&P->err_h, sizeof(int32_t)));
     TAD_CUDA_TRY(cudaMalloc(&P->counters, 64 * sizeof(unsigned)));
     TAD_CUDA_TRY(cudaMemset(P->counters, 0, 64 * sizeof(unsigned)));
+    static_assert(PCG_BLOCKS * 3 <= RED_BLOCKS * LS_BATCH * 4, "PCG grid sums must fit the partials buffer");
     TAD_CUDA_TRY(cudaMalloc(&P->partials, (size_t)RED_BLOCKS * LS_BATCH * 4 * sizeof(double)));
     TAD_CUDA_TRY(cudaMalloc(&P->steps, 64 * sizeof(double)));
     TAD_CUDA_TRY(cudaMalloc(&P->x, P->n_vars * sizeof(double)));

@@ -514,7 +514,7 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
     // replays between host checks doubling up to 8.
     constexpr int CHUNK = 8;
     auto launch_iteration = [&]() {
-        k_pcg_spmv_fused<d, T, SpmvGroup<d>::value><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, P.bptr, P.bcol, H, z, p, Ap,
+        k_pcg_spmv_fused<d, T, SpmvGroup<d>::value><<<PCG_BLOCKS, RED_THREADS, 0, s>>>(nh, P.bptr, P.bcol, H, z, p, Ap,
                                                                                   P.partials, P.counters + 1, P.ds);
         k_pcg_update<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, xs, r, z, p, Ap, dinv, P.partials, P.counters + 2, P.ds);
     };
@@ -830,7 +830,7 @@ TAD_API tad_status tad_profile_kernels(tad_problem* P, const double* x_d, int re
         k_diag_inv<D, float><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.diag, (const float*)Q.H, 0.0, Q.dinv32);     \
         k_pcg_init<D, float><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.rhs, Q.dx32, Q.r32, Q.z32, Q.p32, Q.Ap32,    \
                                                                  Q.dinv32, Q.partials, Q.counters, Q.ds, 1e-30, 1 << 30); \
-        ms5[2] = timed([&] { k_pcg_spmv_fused<D, float, SpmvGroup<D>::value><<<RED_BLOCKS, RED_THREADS, 0, st>>>(   \
+        ms5[2] = timed([&] { k_pcg_spmv_fused<D, float, SpmvGroup<D>::value><<<PCG_BLOCKS, RED_THREADS, 0, st>>>(   \
                                nh, Q.bptr, Q.bcol, (const float*)Q.H, Q.z32, Q.p32, Q.Ap32, Q.partials,              \
                                Q.counters + 1, Q.ds); });                                                             \
         ms5[3] = timed([&] { k_pcg_update<D, float><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.dx32, Q.r32, Q.z32,  \
@@ -841,7 +841,7 @@ TAD_API tad_status tad_profile_kernels(tad_problem* P, const double* x_d, int re
         k_diag_inv<D, double><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.diag, (const double*)Q.H, 0.0, Q.dinv);     \
         k_pcg_init<D, double><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.rhs, Q.dx, Q.r, Q.z, Q.p, Q.Ap, Q.dinv,     \
                                                                   Q.partials, Q.counters, Q.ds, 1e-30, 1 << 30);    \
-        ms5[2] = timed([&] { k_pcg_spmv_fused<D, double, SpmvGroup<D>::value><<<RED_BLOCKS, RED_THREADS, 0, st>>>(  \
+        ms5[2] = timed([&] { k_pcg_spmv_fused<D, double, SpmvGroup<D>::value><<<PCG_BLOCKS, RED_THREADS, 0, st>>>(  \
                                nh, Q.bptr, Q.bcol, (const double*)Q.H, Q.z, Q.p, Q.Ap, Q.partials,                   \
                                Q.counters + 1, Q.ds); });                                                             \
         ms5[3] = timed([&] { k_pcg_update<D, double><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.dx, Q.r, Q.z,       \
