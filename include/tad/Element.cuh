@@ -93,25 +93,27 @@ struct PassiveElement
     TAD_HD T variable(int v) const { return variables(v)[0]; }
 };
 
-template <int d, int N>
+template <int d, int N, typename P = double>
 struct LineSearchElement
 {
-    using scalar_type = double;
-    using passive_type = double;
+    using scalar_type = P;
+    using passive_type = P;
     static constexpr bool active_mode = false;
     int64_t handle;
     const double* x;
     const double* dir;
-    double s;
+    P s;
 
-    TAD_HD Vec<double, d> variables(int v) const
+    /* trial point x + s dir in the passive type P (double, or the
+       double-float of mixed mode, where it is formed without FP64 work) */
+    TAD_HD Vec<P, d> variables(int v) const
     {
-        Vec<double, d> r;
+        Vec<P, d> r;
 #pragma unroll
-        for (int i = 0; i < d; ++i) r[i] = x[(int64_t)d * v + i] + s * dir[(int64_t)d * v + i];
+        for (int i = 0; i < d; ++i) r[i] = P(x[(int64_t)d * v + i]) + s * P(dir[(int64_t)d * v + i]);
         return r;
     }
-    TAD_HD double variable(int v) const { return variables(v)[0]; }
+    TAD_HD P variable(int v) const { return variables(v)[0]; }
 };
 
 template <int d, int N>

@@ -55,15 +55,16 @@ __global__ void __launch_bounds__(128) k_elem_value(ElemLaunch L, Energy energy)
     L.out_f[e] = (double)energy(el);
 }
 
-/* f at x + s_j dir for the n_steps trial step sizes */
-template <int d, int N, typename Energy>
+/* f at x + s_j dir for the n_steps trial step sizes, evaluated in the passive
+   type P (double; the double-float of mixed mode for k <= 8) */
+template <int d, int N, typename Energy, typename P = double>
 __global__ void __launch_bounds__(128) k_elem_linesearch(ElemLaunch L, Energy energy)
 {
     const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (e >= L.n_elem) return;
     for (int j = 0; j < L.n_steps; ++j)
     {
-        LineSearchElement<d, N> el{e, L.x, L.dir, L.steps[j]};
+        LineSearchElement<d, N, P> el{e, L.x, L.dir, P(L.steps[j])};
         L.out_f[(int64_t)j * L.f_stride + e] = (double)energy(el);
     }
 }
@@ -246,17 +247,25 @@ inline void launch_elements_hessian(const ElemLaunch& L, const Energy& energy, c
         k_project_blocks<d, N, T><<<elem_grid(L.n_elem), 128, 0, s>>>(L.n_elem, (T*)L.out_H, (T)L.eps);
 }
 
-/* Value, gradient, line-search and record kernels (modes 0, 1, 4, 5). */
+/* Value, gradient, line-search and record kernels (modes 0, 1, 4, 5).  The
+   line-search energies of mixed precision (precision 1) use the value type
+   of the mixed second-order kernel, so that the Armijo test compares f(x)
+   and f(x + s d) computed alike. */
 template <int d, int N, typename Energy>
-inline void launch_elements_first_order(int mode, const ElemLaunch& L, const Energy& energy, cudaStream_t s)
+inline void launch_elements_first_order(int mode, const ElemLaunch& L, const Energy& energy, cudaStream_t s,
+                                        int precision = 0)
 {
     if (L.n_elem <= 0) return;
     const unsigned g = elem_grid(L.n_elem);
+    using PMixed = typename ValOf<float, d * N>::type;
     switch (mode)
     {
     case 0: k_elem_value<d, N, Energy><<<g, 128, 0, s>>>(L, energy); break;
     case 1: k_elem_gradient<d, N, Energy><<<g, 128, 0, s>>>(L, energy); break;
-    case 4: k_elem_linesearch<d, N, Energy><<<g, 128, 0, s>>>(L, energy); break;
+    case 4:
+        if (precision == 1) k_elem_linesearch<d, N, Energy, PMixed><<<g, 128, 0, s>>>(L, energy);
+        else k_elem_linesearch<d, N, Energy, double><<<g, 128, 0, s>>>(L, energy);
+        break;
     case 5: k_elem_record<d, N, Energy><<<g, 128, 0, s>>>(L, energy); break;
     }
 }
@@ -270,7 +279,7 @@ inline void launch_elements(int mode, int precision, const ElemLaunch& L, const 
         if (precision == 1) launch_elements_hessian<d, N, float>(L, energy, s);
         else launch_elements_hessian<d, N, double>(L, energy, s);
     }
-    else launch_elements_first_order<d, N>(mode, L, energy, s);
+    else launch_elements_first_order<d, N>(mode, L, energy, s, precision);
 }
 
 } // namespace tad

@@ -35,6 +35,32 @@ def test_known_answers_device(tad):
         np.testing.assert_allclose(got, exp, rtol=0, atol=max(c["tol"], 2e-6) * scale, err_msg=c["name"])
 
 
+def test_mixed_value_conversions(tad):
+    """The mixed scalar's double-float value channel: double -> hi + lo on the
+    device is a bit-level split (no FP64 instruction) for exponents where
+    both parts are normal floats, and the rounding conversion elsewhere.  A
+    round trip through `a + 0` (op 29) must return the input within 2^-47
+    relative, keep signed zero, and propagate inf / NaN."""
+    rng = np.random.default_rng(5)
+    vals = list(np.ldexp(rng.uniform(-1, 1, 200), rng.integers(-70, 70, 200)))
+    vals += [1.0, -1.0, 0.1, 1.0 / 3.0, 2.0 ** -74, 2.0 ** -75, 1e-30, -1e-40, 1e-300, 3.0e38, -3.4e38, 1e39,
+             1e300, np.nextafter(1.0, 2.0), 5e-324]
+    for v in vals:
+        got = tad.debug_scalar_op(29, (v, 1.0, 0.0), (0.0, 0.0, 0.0), tad.PREC_MIXED)[0]
+        if abs(v) < 1e-38 or abs(v) > 3.4e38:
+            # outside the normal float range the double-float cannot hold the value;
+            # the conversion rounds through float (flush to zero / infinity)
+            with np.errstate(over="ignore"):
+                as_float = np.float64(np.float32(v))
+            assert got == as_float or abs(got - v) <= 2.0 ** -47 * abs(v), (v, got)
+        else:
+            assert abs(got - v) <= 2.0 ** -47 * abs(v), (v, got)
+    z = tad.debug_scalar_op(0, (0.0, 1.0, 0.0), (0.0, 0.0, 0.0), tad.PREC_MIXED)[0]   # -(+0) = -0
+    assert z == 0.0 and np.signbit(z)
+    assert tad.debug_scalar_op(29, (np.inf, 1.0, 0.0), (0.0, 0.0, 0.0), tad.PREC_MIXED)[0] == np.inf
+    assert np.isnan(tad.debug_scalar_op(29, (np.nan, 1.0, 0.0), (0.0, 0.0, 0.0), tad.PREC_MIXED)[0])
+
+
 def _quad(A, b, c):
     return np.concatenate([np.asarray(A, float).ravel(), np.asarray(b, float), [c]])[None, :]
 

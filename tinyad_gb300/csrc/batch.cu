@@ -486,7 +486,7 @@ static tad_status record_iteration(Batch& B, int prec, double eps)
     {
         double* save = P.steps;
         P.steps = B.steps + t0;
-        st = eval_elements(P, TAD_MODE_LINESEARCH, B.x, 0.0, TAD_PREC_FP64, P.dx, LS_BATCH);
+        st = eval_elements(P, TAD_MODE_LINESEARCH, B.x, 0.0, P.precision, P.dx, LS_BATCH);
         P.steps = save;
         if (st != TAD_OK) return st;
         k_b_reduce_rows<<<dim3(G, LS_BATCH), TH, 0, s>>>(B.ech, B.n_ech, B.emcb, B.emce, P.ef, P.n_elem_total,

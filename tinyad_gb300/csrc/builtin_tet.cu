@@ -24,7 +24,7 @@ tad_status launch_builtin_tet(Problem& P, Term& T, const tad_term_eval_args& a)
         if (a.precision == TAD_PREC_MIXED) tet_hessian_mixed(L, energy, s);
         else tet_hessian_fp64(L, energy, s);
     }
-    else tad::launch_elements_first_order<3, 4>(a.mode, L, energy, s);
+    else tad::launch_elements_first_order<3, 4>(a.mode, L, energy, s, a.precision);
     return TAD_OK;
 }
 

@@ -118,39 +118,41 @@ __global__ void k_diag_inv(int64_t nh, const int32_t* __restrict__ diag, const T
 {
     GRID_STRIDE(u, nh)
     {
-        double A[d * d];
+        // in the PCG's precision: FP32 blocks are inverted in FP32 (no FP64
+        // instructions in the mixed path)
+        T A[d * d];
         const int32_t b = diag[u];
 #pragma unroll
-        for (int i = 0; i < d * d; ++i) A[i] = b >= 0 ? (double)H[(int64_t)b * d * d + i] : 0.0;
+        for (int i = 0; i < d * d; ++i) A[i] = b >= 0 ? H[(int64_t)b * d * d + i] : T(0);
 #pragma unroll
-        for (int i = 0; i < d; ++i) A[i * d + i] += w;
-        double I[d * d];
-        double det;
-        if (d == 1) { det = A[0]; I[0] = 1.0 / A[0]; }
+        for (int i = 0; i < d; ++i) A[i * d + i] += (T)w;
+        T I[d * d];
+        T det;
+        if (d == 1) { det = A[0]; I[0] = T(1) / A[0]; }
         else if (d == 2)
         {
             det = A[0] * A[3] - A[1] * A[2];
-            const double id = 1.0 / det;
+            const T id = T(1) / det;
             I[0] = A[3] * id; I[1] = -A[1] * id; I[2] = -A[2] * id; I[3] = A[0] * id;
         }
         else
         {
-            const double c00 = A[4] * A[8] - A[5] * A[7], c01 = A[5] * A[6] - A[3] * A[8], c02 = A[3] * A[7] - A[4] * A[6];
+            const T c00 = A[4] * A[8] - A[5] * A[7], c01 = A[5] * A[6] - A[3] * A[8], c02 = A[3] * A[7] - A[4] * A[6];
             det = A[0] * c00 + A[1] * c01 + A[2] * c02;
-            const double id = 1.0 / det;
+            const T id = T(1) / det;
             I[0] = c00 * id; I[3] = c01 * id; I[6] = c02 * id;
             I[1] = (A[2] * A[7] - A[1] * A[8]) * id; I[4] = (A[0] * A[8] - A[2] * A[6]) * id; I[7] = (A[1] * A[6] - A[0] * A[7]) * id;
             I[2] = (A[1] * A[5] - A[2] * A[4]) * id; I[5] = (A[2] * A[3] - A[0] * A[5]) * id; I[8] = (A[0] * A[4] - A[1] * A[3]) * id;
         }
-        const bool ok = det > 0.0 && isfinite(det);
+        const bool ok = det > T(0) && isfinite(det);
 #pragma unroll
         for (int i = 0; i < d; ++i)
 #pragma unroll
             for (int j = 0; j < d; ++j)
             {
-                double v = I[i * d + j];
-                if (!ok) v = (i == j && A[i * d + i] > 0.0) ? 1.0 / A[i * d + i] : (i == j ? 1.0 : 0.0);
-                dinv[u * d * d + i * d + j] = (T)v;
+                T v = I[i * d + j];
+                if (!ok) v = (i == j && A[i * d + i] > T(0)) ? T(1) / A[i * d + i] : (i == j ? T(1) : T(0));
+                dinv[u * d * d + i * d + j] = v;
             }
     }
 }
@@ -175,7 +177,8 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_init(int64_t nh, const doub
                                                           T* Ap, const T* __restrict__ dinv, double* partials, unsigned* counter,
                                                           DevScalars* ds, double rel_tol, int max_iters)
 {
-    double part[2] = {0.0, 0.0};
+    // per-thread partials in the PCG's precision (a few rows each), combined in FP64
+    T acc_rz = T(0), acc_bb = T(0);
     GRID_STRIDE(u, nh)
     {
         T rv[d], zv[d];
@@ -188,10 +191,11 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_init(int64_t nh, const doub
             z[u * d + i] = zv[i];
             p[u * d + i] = T(0);
             Ap[u * d + i] = T(0);
-            part[0] += (double)rv[i] * (double)zv[i];
-            part[1] += b[u * d + i] * b[u * d + i];
+            acc_rz += rv[i] * zv[i];
+            acc_bb += rv[i] * rv[i];
         }
     }
+    double part[2] = {(double)acc_rz, (double)acc_bb};
     double tot[2];
     if (!grid_sum<2>(part, partials, counter, tot)) return;
     if (threadIdx.x == 0)
@@ -649,7 +653,7 @@ tad_status line_search_device(Problem& P, double* x, const double* d, double f, 
     {
         const int nb = std::min(batch, max_iters - t0);
         TAD_CUDA_TRY(cudaMemcpyAsync(P.steps, seq.data() + t0, nb * sizeof(double), cudaMemcpyHostToDevice, s));
-        tad_status st = eval_elements(P, TAD_MODE_LINESEARCH, x, 0.0, TAD_PREC_FP64, d, nb);
+        tad_status st = eval_elements(P, TAD_MODE_LINESEARCH, x, 0.0, P.precision, d, nb);
         if (st != TAD_OK) return st;
         launch_reduce_f(P, nb, P.ds->f_trial);
         k_ls_select<<<1, 32, 0, s>>>(nb, P.steps, P.settings.ls_armijo, P.ds);
@@ -857,7 +861,7 @@ TAD_API tad_status tad_profile_kernels(tad_problem* P, const double* x_d, int re
     // keep the PCG kernels from early-exiting: done was cleared by k_pcg_init with an unreachable tolerance
     const double one = 1.0;
     TAD_CUDA_TRY(cudaMemcpyAsync(Q.steps, &one, sizeof(double), cudaMemcpyHostToDevice, st));
-    ms5[4] = timed([&] { eval_elements(Q, TAD_MODE_LINESEARCH, x_d, 0.0, TAD_PREC_FP64, Q.rhs, 1); });
+    ms5[4] = timed([&] { eval_elements(Q, TAD_MODE_LINESEARCH, x_d, 0.0, Q.precision, Q.rhs, 1); });
     TAD_CUDA_TRY(cudaStreamSynchronize(st));
     TAD_CUDA_TRY(cudaGetLastError());
     return check_device_error(Q);
