@@ -22,6 +22,7 @@
 #include "Scalar.cuh"
 #include "Element.cuh"
 #include "Projection.cuh"
+#include "RowIO.cuh"
 #include "../tad.h"
 
 namespace tad {
@@ -149,10 +150,11 @@ __global__ void __launch_bounds__(128) k_elem_hessian(ElemLaunch L, Energy energ
     if (FusedProjection<k>::value && L.project) project_positive_definite<k, T>(r.hess, (T)L.eps);
     L.out_f[e] = (double)r.val;
     bool fin = true;
-    double* g = (double*)L.out_g + e * k;
+    double gv[k];
 #pragma unroll
-    for (int i = 0; i < k; ++i) { const double gi = (double)r.grad[i]; g[i] = gi; fin = fin && finite_val(gi); }
-    T* Hb = (T*)L.out_H + e * (NP * d * d);
+    for (int i = 0; i < k; ++i) { gv[i] = (double)r.grad[i]; fin = fin && finite_val(gv[i]); }
+    store_row<double, k>((double*)L.out_g, e, gv);
+    T hb[NP * d * d];
 #pragma unroll
     for (int a = 0; a < N; ++a)
 #pragma unroll
@@ -167,9 +169,10 @@ __global__ void __launch_bounds__(128) k_elem_hessian(ElemLaunch L, Energy energ
                     const int i = a * d + p, j = b * d + q;
                     const T v = (i <= j) ? r.hess[packed_index(i, j, k)] : r.hess[packed_index(j, i, k)];
                     fin = fin && finite_val(v);
-                    Hb[pr * d * d + p * d + q] = v;
+                    hb[pr * d * d + p * d + q] = v;
                 }
         }
+    store_row<T, NP * d * d>((T*)L.out_H, e, hb);
     if (!fin) report_error(L.err, DEVERR_NONFINITE);
 }
 
@@ -183,7 +186,8 @@ __global__ void __launch_bounds__(128) k_project_blocks(int64_t n_elem, T* __res
     constexpr int BS = NP * d * d;
     const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (e >= n_elem) return;
-    T* Hb = Hblocks + e * BS;
+    T hb[BS];
+    load_row<T, BS>(Hblocks, e, hb);
     T h[k * (k + 1) / 2];
 #pragma unroll
     for (int a = 0; a < N; ++a)
@@ -195,7 +199,7 @@ __global__ void __launch_bounds__(128) k_project_blocks(int64_t n_elem, T* __res
                 for (int q = 0; q < d; ++q)
                 {
                     const int i = a * d + p, j = b * d + q;
-                    if (i <= j) h[packed_index(i, j, k)] = Hb[packed_index(a, b, N) * d * d + p * d + q];
+                    if (i <= j) h[packed_index(i, j, k)] = hb[packed_index(a, b, N) * d * d + p * d + q];
                 }
     if (!project_positive_definite<k, T>(h, eps)) return;
 #pragma unroll
@@ -208,8 +212,9 @@ __global__ void __launch_bounds__(128) k_project_blocks(int64_t n_elem, T* __res
                 for (int q = 0; q < d; ++q)
                 {
                     const int i = a * d + p, j = b * d + q;
-                    Hb[packed_index(a, b, N) * d * d + p * d + q] = (i <= j) ? h[packed_index(i, j, k)] : h[packed_index(j, i, k)];
+                    hb[packed_index(a, b, N) * d * d + p * d + q] = (i <= j) ? h[packed_index(i, j, k)] : h[packed_index(j, i, k)];
                 }
+    store_row<T, BS>(Hblocks, e, hb);
 }
 
 inline unsigned elem_grid(int64_t n) { return (unsigned)((n + 127) / 128); }

@@ -17,6 +17,7 @@
  *                     from the BSR blocks, for the host-facing Hessian.
  */
 #include "internal.hh"
+#include "../../include/tad/RowIO.cuh"
 
 namespace tadlib {
 
@@ -129,10 +130,8 @@ __global__ void k_assemble_hess(int64_t nb, const int32_t* __restrict__ cptr, co
     for (int32_t q = cptr[b]; q < q1; ++q)
     {
         const int32_t c = cidx[q];
-        const T* blk = eH + (int64_t)(c & 0x7fffffff) * (d * d);
         T v[d * d];
-#pragma unroll
-        for (int i = 0; i < d * d; ++i) v[i] = blk[i];
+        tad::load_row<T, d * d>(eH, (int64_t)(c & 0x7fffffff), v);   // one 16-byte load per 2x2 FP32 block
         if (c < 0)
         {
 #pragma unroll
@@ -146,8 +145,7 @@ __global__ void k_assemble_hess(int64_t nb, const int32_t* __restrict__ cptr, co
             for (int i = 0; i < d * d; ++i) acc[i] += v[i];
         }
     }
-#pragma unroll
-    for (int i = 0; i < d * d; ++i) H[b * (d * d) + i] = acc[i];
+    tad::store_row<T, d * d>(H, b, acc);
 }
 
 void launch_assemble_hess(Problem& P, int precision)

@@ -261,6 +261,22 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_spmv(int64_t nh, const int3
 
 /* one d x d block of H into registers (16-byte vector loads where the
    block size allows) */
+/* the d entries of one block row of a vector (one 8-byte load for 2D FP32) */
+template <int d, typename T>
+__device__ __forceinline__ void load_vec(const T* __restrict__ src, T (&v)[d])
+{
+    if constexpr (d == 2 && sizeof(T) == 4)
+    {
+        const float2 q = *reinterpret_cast<const float2*>(src);
+        v[0] = q.x; v[1] = q.y;
+    }
+    else
+    {
+#pragma unroll
+        for (int j = 0; j < d; ++j) v[j] = src[j];
+    }
+}
+
 template <int d, typename T>
 __device__ __forceinline__ void load_block(const T* __restrict__ B, T (&v)[d * d])
 {
@@ -314,8 +330,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_spmv_fused(int64_t nh, cons
             for (int k = 0; k < 4; ++k)
             {
                 load_block<d, T>(H + (int64_t)(b + k) * d * d, B[k]);
-#pragma unroll
-                for (int j = 0; j < d; ++j) zv[k][j] = z[v[k] * d + j];
+                load_vec<d, T>(z + v[k] * d, zv[k]);
             }
 #pragma unroll
             for (int k = 0; k < 4; ++k)
