@@ -27,6 +27,8 @@
  *                             CSR arrays here equal Eigen's CSC arrays)
  *   tad_newton_direction      newton_direction(g, H, solver)
  *                             include/TinyAD/Utils/NewtonDirection.hh:25-65
+ *   tad_newton_direction_reduced_basis  newton_direction_reduced_basis(g, H, B, solver)
+ *                             include/TinyAD/Utils/NewtonDirection.hh:76-123
  *   tad_line_search           line_search(x, d, f, g, func)
  *                             include/TinyAD/Utils/LineSearch.hh:26-65
  *   tad_newton_solve          the Projected-Newton loop users write around the
@@ -173,9 +175,11 @@ typedef enum tad_eval_mode {
 
 typedef int (*tad_term_eval_fn)(void* user, const tad_term_eval_args* args);
 
-/* element_handles_h: n_elem int32 element handles (passed to the functor).
-   The library records each element's access order with one TAD_MODE_RECORD
-   call when the sparsity pattern is built. */
+/* A term of n_elem elements of valence 1..64 evaluated by a caller-supplied
+   device functor (fn launches the element kernels for args->mode; the C++
+   front end instantiates them from a lambda).  The library records each
+   element's access order with one TAD_MODE_RECORD call when the sparsity
+   pattern is built. */
 TAD_API tad_status tad_add_elements_custom(tad_problem* p, int valence,
                                            int64_t n_elem,
                                            tad_term_eval_fn fn, void* user);
@@ -213,6 +217,21 @@ TAD_API tad_status tad_eval_with_hessian_proj_d(tad_problem* p, const double* x_
 TAD_API tad_status tad_newton_direction(tad_problem* p, const double* x_h, int projected,
                                         double proj_eps, double w_identity,
                                         double* d_h, double* f, double* g_h);
+
+/* newton_direction_reduced_basis(g, H_proj, B, solver, w)
+   (include/TinyAD/Utils/NewtonDirection.hh:76-123): with g and the projected
+   Hessian (proj_eps) evaluated at x, returns d = B (B^T H B + w I)^-1 (-B^T g)
+   for the n_vars x m basis B given as CSR (b_outer[n_vars + 1], b_inner and
+   b_values[b_outer[n_vars]], column indices in [0, m)).  The reduced system is
+   solved matrix-free by conjugate gradients with the exact diagonal of
+   B^T H B + w I as preconditioner, to the problem's pcg_rel_tol.  Returns
+   TAD_ERR_PCG_NOCONV (d = the last iterate) if the tolerance is not met or
+   the reduced system shows non-positive curvature (the reference throws
+   "Linear solve failed"). */
+TAD_API tad_status tad_newton_direction_reduced_basis(tad_problem* p, const double* x_h, int64_t m,
+                                                      const int32_t* b_outer, const int32_t* b_inner,
+                                                      const double* b_values, double proj_eps, double w_identity,
+                                                      double* d_h, double* f, double* g_h);
 
 /* Armijo backtracking from x along d: s = s_max, s *= shrink, at most
    max_iters trials; x_out = x + s d for the first s meeting

@@ -29,7 +29,9 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <array>
+#include <map>
 #include <functional>
 #include <memory>
 #include <stdexcept>
@@ -166,7 +168,45 @@ public:
         auto term = std::make_unique<detail::Term<d, N, F>>(detail::HandleMapped<F>{functor, hd});
         check(tad_add_elements_custom(p_, N, (int64_t)h.size(), &detail::term_callback, term.get()));
         terms_.push_back(std::move(term));
+        term_sizes_.push_back((int64_t)h.size());
     }
+
+    /* add_elements_dynamic<V...>(range, functor) (ScalarFunctionImpl.hh:133-214):
+       every element's distinct accessed handles are counted once on the
+       device (the functor run with x = 0, as the reference's recorder
+       element does), the element joins the smallest listed valence that
+       holds it, and one term per non-empty group is added in the order the
+       valences are listed -- so the functor is instantiated once per
+       valence, each group runs its own element kernels. */
+    template <int... Valences, typename Range, typename F>
+    void add_elements_dynamic(const Range& elements, F functor)
+    {
+        static_assert(sizeof...(Valences) >= 1, "At least one element valence has to be passed.");
+        static_assert(((Valences >= 1) && ...), "Element valences must be positive.");
+        constexpr int vmax = std::max({Valences...});
+        std::vector<int> sorted = {Valences...};
+        std::sort(sorted.begin(), sorted.end());
+        if (std::unique(sorted.begin(), sorted.end()) != sorted.end())
+            throw std::runtime_error("Element valences passed to add_elements<..>(..) are not unique. Please pass unique element valences.");
+        std::vector<int32_t> h;
+        for (auto eh : elements) h.push_back((int32_t)eh);
+        const std::vector<int> counts = record_valences<vmax>(h, functor);
+        std::map<int, std::vector<int32_t>> groups;
+        for (size_t i = 0; i < h.size(); ++i)
+        {
+            const auto it = std::lower_bound(sorted.begin(), sorted.end(), counts[i]);
+            if (it == sorted.end())
+                throw std::runtime_error("Element valence " + std::to_string(counts[i]) +
+                                         " Exceeds maximum static valence passed to add_elements<..>(..).");
+            groups[*it].push_back(h[i]);
+        }
+        (add_group<Valences>(groups, functor), ...);
+    }
+
+    /* number of terms and their element counts (the reference's
+       objective_terms[i]->n_elements()) */
+    size_t n_terms() const { return term_sizes_.size(); }
+    int64_t term_n_elements(size_t i) const { return term_sizes_.at(i); }
 
     /* x_from_data / x_to_data (ScalarFunctionImpl.hh:216-254) */
     std::vector<double> x_from_data(const std::function<VecD(int64_t)>& read) const
@@ -216,6 +256,9 @@ public:
 
     SparseCSR eval_hessian(const std::vector<double>& x) const { return std::get<2>(eval_with_derivatives(x)); }
 
+    /* the Hessian at x = 0 (ScalarFunctionImpl.hh:370-376) */
+    SparseCSR eval_hessian_of_quadratic() const { return eval_hessian(std::vector<double>(n_vars(), 0.0)); }
+
     std::tuple<double, std::vector<double>, SparseCSR>
     eval_with_hessian_proj(const std::vector<double>& x, double projection_eps = 1e-9) const
     {
@@ -232,6 +275,23 @@ public:
         std::vector<double> dvec(n_vars()), g(n_vars());
         double f;
         const tad_status s = tad_newton_direction(p_, x.data(), 1, projection_eps, 0.0, dvec.data(), &f, g.data());
+        if (s != TAD_OK && s != TAD_ERR_PCG_NOCONV) check(s);
+        return dvec;
+    }
+
+    /* newton_direction_reduced_basis(g, H_proj, B, solver, w) at x
+       (NewtonDirection.hh:76-123): d = B (B^T H B + w I)^-1 (-B^T g), B the
+       n_vars x m basis in CSR */
+    std::vector<double> newton_direction_reduced_basis(const std::vector<double>& x, const SparseCSR& B, int64_t m,
+                                                       double w_identity = 0.0, double projection_eps = 1e-9) const
+    {
+        if (B.rows != n_vars() || (int64_t)B.outer.size() != n_vars() + 1)
+            throw std::runtime_error("basis must have n_vars rows");
+        std::vector<double> dvec(n_vars()), g(n_vars());
+        double f;
+        const tad_status s = tad_newton_direction_reduced_basis(p_, x.data(), m, B.outer.data(), B.inner.data(),
+                                                                B.values.data(), projection_eps, w_identity,
+                                                                dvec.data(), &f, g.data());
         if (s != TAD_OK && s != TAD_ERR_PCG_NOCONV) check(s);
         return dvec;
     }
@@ -256,6 +316,54 @@ public:
     }
 
 private:
+    /* distinct accessed handles per element, recorded on the device with the
+       functor evaluated at x = 0 and at most vmax handles an element */
+    template <int vmax, typename F>
+    std::vector<int> record_valences(const std::vector<int32_t>& h, F& functor)
+    {
+        const int64_t n = (int64_t)h.size();
+        std::vector<int> counts(n, 0);
+        if (n == 0) return counts;
+        void* sp = nullptr;
+        check(tad_get_stream(p_, &sp));
+        cudaStream_t st = (cudaStream_t)sp;
+        int32_t *hd = nullptr, *rec = nullptr, *err = nullptr;
+        double* xz = nullptr;
+        check_cuda(cudaMalloc(&hd, n * sizeof(int32_t)));
+        check_cuda(cudaMalloc(&rec, n * vmax * sizeof(int32_t)));
+        check_cuda(cudaMalloc(&err, sizeof(int32_t)));
+        check_cuda(cudaMalloc(&xz, std::max<int64_t>(n_vars(), 1) * sizeof(double)));
+        std::vector<int32_t> rec_h(n * vmax);
+        int32_t err_h = 0;
+        check_cuda(cudaMemcpyAsync(hd, h.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+        check_cuda(cudaMemsetAsync(xz, 0, std::max<int64_t>(n_vars(), 1) * sizeof(double), st));
+        check_cuda(cudaMemsetAsync(err, 0, sizeof(int32_t), st));
+        ElemLaunch L{};
+        L.n_elem = n;
+        L.x = xz;
+        L.record = rec;
+        L.err = err;
+        k_elem_record<d, vmax, detail::HandleMapped<F>><<<elem_grid(n), 128, 0, st>>>(L, detail::HandleMapped<F>{functor, hd});
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(rec_h.data(), rec, n * vmax * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&err_h, err, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        cudaFree(hd); cudaFree(rec); cudaFree(err); cudaFree(xz);
+        check_cuda(e);
+        if (err_h & DEVERR_TOO_MANY_VARS)
+            throw std::runtime_error("Element valence exceeds maximum static valence passed to add_elements<..>(..)."
+                                     " Please pass a large-enough static valence as template argument.");
+        for (int64_t i = 0; i < n; ++i)
+            for (int j = 0; j < vmax; ++j) counts[i] += rec_h[i * vmax + j] >= 0 ? 1 : 0;
+        return counts;
+    }
+    template <int V, typename F>
+    void add_group(std::map<int, std::vector<int32_t>>& groups, F& functor)
+    {
+        const auto it = groups.find(V);
+        if (it != groups.end() && !it->second.empty()) add_elements<V>(it->second, functor);
+    }
+
     SparseCSR pattern() const
     {
         int64_t nnz = 0;
@@ -274,12 +382,14 @@ private:
         std::swap(n_handles_, o.n_handles_);
         std::swap(terms_, o.terms_);
         std::swap(handle_bufs_, o.handle_bufs_);
+        std::swap(term_sizes_, o.term_sizes_);
     }
 
     tad_problem* p_ = nullptr;
     int64_t n_handles_ = 0;
     std::vector<std::unique_ptr<detail::TermBase>> terms_;
     std::vector<int32_t*> handle_bufs_;
+    std::vector<int64_t> term_sizes_;
 };
 
 /* scalar_function<d>(range) (ScalarFunctionImpl.hh:418-442) */

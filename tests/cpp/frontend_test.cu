@@ -4,12 +4,18 @@
  *   planar Newton        tests/NewtonTest.cc:12-95 (nnz formula, f -> 4, g -> 0)
  *   quadratics           tests/ScalarFunctionTest.cc:10-151
  *   element variables    tests/ScalarFunctionTest.cc:153-179 (dedup, too many variables)
+ *   reduced basis        tests/SwitchSolverTest.cc:16-36 (Newton step (-1, -1))
+ *   dynamic valences     tests/DynamicElementsTest.cc:9-33 (grouping, term sizes, f/g/H)
+ *   Laplacian            tests/DynamicElementsTest.cc:35-141 (static triangles and dynamic
+ *                        one-ring elements vs the assembled Laplacian, on a closed torus
+ *                        with vertex valences 4 and 8)
  * Prints "frontend ok" and exits 0 on success.
  */
 #include <tad/ScalarFunction.cuh>
 #include <tad/Mat.cuh>
 
 #include <cmath>
+#include <algorithm>
 #include <cstdio>
 #include <vector>
 
@@ -114,6 +120,22 @@ static int quadratics()
     auto [fg, gg] = func.eval_with_gradient(x);
     CHECK(fg == 12.0 && gg[0] == 9.0 && gg[1] == 6.0);
 
+    // SwitchSolverTest.cc:16-36: x^2 + y^2 at (1, 1), B = I: Newton step (-1, -1)
+    auto circ = tad::scalar_function<2>(tad::range(1));
+    circ.add_elements<1>(tad::range(1), [] __device__(auto& element) {
+        const auto v = element.variables(0);
+        return tad::sqr(v[0]) + tad::sqr(v[1]);
+    });
+    tad::SparseCSR B;
+    B.rows = 2;
+    B.outer = {0, 1, 2};
+    B.inner = {0, 1};
+    B.values = {1.0, 1.0};
+    const std::vector<double> dr = circ.newton_direction_reduced_basis({1.0, 1.0}, B, 2);
+    CHECK(std::fabs(dr[0] + 1.0) <= 1e-15 && std::fabs(dr[1] + 1.0) <= 1e-15);
+    const std::vector<double> dn = circ.newton_direction({1.0, 1.0});
+    CHECK(std::fabs(dn[0] + 1.0) <= 1e-15 && std::fabs(dn[1] + 1.0) <= 1e-15);
+
     auto neg = tad::scalar_function<2>(tad::range(1));
     neg.add_elements<1>(tad::range(1), [] __device__(auto& element) {
         const auto v = element.variables(0);
@@ -151,11 +173,138 @@ static int element_variables()
     return 0;
 }
 
+static int dynamic_valences()
+{
+    // element e accesses variables 0..e-1 and returns |sum|^2; valences <3, 1>
+    auto func = tad::scalar_function<2>(tad::range(4));
+    func.add_elements_dynamic<3, 1>(tad::range(4), [] __device__(auto& element) {
+        using T = TAD_SCALAR_TYPE(element);
+        const int e = (int)element.handle;
+        tad::Vec<T, 2> sum;
+        sum[0] = T(0.0);
+        sum[1] = T(0.0);
+        for (int v = 0; v < e; ++v) sum = sum + element.variables(v);
+        return sum.squaredNorm();
+    });
+    CHECK(func.n_terms() == 2);
+    CHECK(func.term_n_elements(0) == 2 && func.term_n_elements(1) == 2);
+    auto [f, g, H] = func.eval_with_hessian_proj(std::vector<double>(8, 1.0));
+    // f = sum_e 2 e^2; g_v = 2 sum_{e > v} (e, e); H(v, w) = 2 (3 - max(v, w)) I for max(v, w) < 3
+    CHECK(f == 28.0);
+    const double gx[4] = {12.0, 10.0, 6.0, 0.0};
+    for (int v = 0; v < 4; ++v) CHECK(g[2 * v] == gx[v] && g[2 * v + 1] == gx[v]);
+    for (int v = 0; v < 3; ++v)
+        for (int w = 0; w < 3; ++w)
+        {
+            const double ex = 2.0 * (3 - std::max(v, w));
+            CHECK(std::fabs(H.coeff(2 * v, 2 * w) - ex) <= 1e-8 && std::fabs(H.coeff(2 * v + 1, 2 * w + 1) - ex) <= 1e-8);
+            CHECK(std::fabs(H.coeff(2 * v, 2 * w + 1)) <= 1e-8);
+        }
+    // a valence above every listed one is an error (ScalarFunctionImpl.hh:185-190)
+    auto small = tad::scalar_function<2>(tad::range(4));
+    bool threw = false;
+    try
+    {
+        small.add_elements_dynamic<2, 1>(tad::range(4), [] __device__(auto& element) {
+            using T = TAD_SCALAR_TYPE(element);
+            const int e = (int)element.handle;
+            T acc = T(0.0);
+            for (int v = 0; v < e; ++v) acc = acc + element.variables(v)[0];
+            return acc * acc;
+        });
+    }
+    catch (const std::runtime_error&) { threw = true; }
+    CHECK(threw);
+    return 0;
+}
+
+static int dynamic_laplacian()
+{
+    // closed torus, nu x nv grid, quads split along alternating diagonals:
+    // vertex valences 4 and 8 (one-ring elements of 5 and 9 handles)
+    const int nu = 8, nv = 6, nV = nu * nv;
+    auto vid = [&](int i, int j) { return ((i + nu) % nu) * nv + (j + nv) % nv; };
+    std::vector<int> F;
+    for (int i = 0; i < nu; ++i)
+        for (int j = 0; j < nv; ++j)
+        {
+            const int a = vid(i, j), b = vid(i + 1, j), c = vid(i + 1, j + 1), dd = vid(i, j + 1);
+            if ((i + j) % 2 == 0) { F.insert(F.end(), {a, b, c, a, c, dd}); }
+            else { F.insert(F.end(), {a, b, dd, b, c, dd}); }
+        }
+    const int nF = (int)F.size() / 3;
+    // reference Laplacian of the directed face edges (DynamicElementsTest.cc:38-55)
+    std::vector<double> L(nV * nV, 0.0);
+    std::vector<std::vector<int>> nbr(nV);
+    for (int f = 0; f < nF; ++f)
+        for (int i = 0; i < 3; ++i)
+        {
+            const int v1 = F[3 * f + i], v2 = F[3 * f + (i + 1) % 3];
+            L[v1 * nV + v1] += 1.0;
+            L[v1 * nV + v2] -= 1.0;
+            nbr[v1].push_back(v2);
+        }
+    std::vector<int> nptr(nV + 1, 0), nidx;
+    for (int v = 0; v < nV; ++v) { nptr[v + 1] = nptr[v] + (int)nbr[v].size(); nidx.insert(nidx.end(), nbr[v].begin(), nbr[v].end()); }
+    const int* Fd = to_device(F);
+    const int* np = to_device(nptr);
+    const int* ni = to_device(nidx);
+    auto dense = [&](const tad::SparseCSR& H) {
+        std::vector<double> D(nV * nV, 0.0);
+        for (int r = 0; r < nV; ++r)
+            for (int q = H.outer[r]; q < H.outer[r + 1]; ++q) D[r * nV + H.inner[q]] += H.values[q];
+        return D;
+    };
+    auto err_to_ref = [&](const std::vector<double>& D) {
+        double e2 = 0.0;
+        for (int i = 0; i < nV * nV; ++i) e2 += (D[i] - 0.5 * (L[i] + L[(i % nV) * nV + i / nV])) * (D[i] - 0.5 * (L[i] + L[(i % nV) * nV + i / nV]));
+        return std::sqrt(e2);
+    };
+    int ref_nnz = 0;
+    for (int i = 0; i < nV * nV; ++i) ref_nnz += (L[i] != 0.0 || L[(i % nV) * nV + i / nV] != 0.0) ? 1 : 0;
+
+    // static triangle elements
+    auto tri = tad::scalar_function<1>(tad::range(nV));
+    tri.add_elements<3>(tad::range(nF), [=] __device__(auto& element) {
+        const int f = (int)element.handle;
+        const auto a = element.variable(Fd[3 * f + 0]);
+        const auto b = element.variable(Fd[3 * f + 1]);
+        const auto c = element.variable(Fd[3 * f + 2]);
+        return 0.25 * (tad::sqr(b - a) + tad::sqr(c - b) + tad::sqr(a - c));
+    });
+    const tad::SparseCSR Ht = tri.eval_hessian_of_quadratic();
+    const double et = err_to_ref(dense(Ht));
+    std::printf("laplacian (triangles): |L - L_ref| = %.3g, nnz %lld vs %d\n", et, (long long)Ht.nonZeros(), ref_nnz);
+    CHECK(et <= 1e-12);
+    CHECK(Ht.nonZeros() == ref_nnz);
+
+    // dynamic one-ring vertex elements: valences 5 and 9 go to the groups 6 and 10
+    auto ring = tad::scalar_function<1>(tad::range(nV));
+    ring.add_elements_dynamic<6, 10>(tad::range(nV), [=] __device__(auto& element) {
+        using T = TAD_SCALAR_TYPE(element);
+        const int v = (int)element.handle;
+        const T vv = element.variable(v);
+        T dirichlet = T(0.0);
+        for (int q = np[v]; q < np[v + 1]; ++q) dirichlet = dirichlet + 0.25 * tad::sqr(vv - element.variable(ni[q]));
+        return dirichlet;
+    });
+    CHECK(ring.n_terms() == 2);
+    int n5 = 0;
+    for (int v = 0; v < nV; ++v) n5 += nbr[v].size() == 4 ? 1 : 0;
+    CHECK(ring.term_n_elements(0) == n5 && ring.term_n_elements(1) == nV - n5);
+    const double er = err_to_ref(dense(ring.eval_hessian_of_quadratic()));
+    std::printf("laplacian (one-ring dynamic): |L - L_ref| = %.3g\n", er);
+    CHECK(er <= 1e-12);
+    return 0;
+}
+
 int main()
 {
     if (planar_newton()) return 1;
     if (quadratics()) return 1;
     if (element_variables()) return 1;
+    if (dynamic_valences()) return 1;
+    if (dynamic_laplacian()) return 1;
     std::printf("frontend ok\n");
     return 0;
 }

@@ -272,3 +272,44 @@ def test_mixed_precision(tad, oracle):
     xm, fhm = fm.newton_solve(w.x0, 25)
     xo, fho, _ = p.newton(w.x0, 25)
     assert abs(fhm[-1] - fho[-1]) <= 1e-8 * abs(fho[-1]), (fhm[-4:], fho[-4:])
+
+
+def test_newton_direction_reduced_basis_switch_solver(tad):
+    """tests/SwitchSolverTest.cc:16-36: x^2 + y^2 at (1, 1) with B = I gives
+    the Newton step (-1, -1)."""
+    import scipy.sparse as sp
+    f1 = tad.ScalarFunction(2, 1)
+    f1.add_elements(meshes.TAD_ENERGY_QUADRATIC, [[0]], _quad([[1.0, 0.0], [0.0, 1.0]], [0.0, 0.0], 0.0))
+    d, f, g = f1.newton_direction_reduced_basis(np.array([1.0, 1.0]), sp.identity(2, format="csr"))
+    assert f == 2.0 and np.all(g == 2.0)
+    assert np.all(np.abs(d + 1.0) <= 1e-15)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-8), ("mixed", 1e-4)])
+@pytest.mark.parametrize("w_identity", [0.0, 0.5])
+def test_newton_direction_reduced_basis_pinned_boundary(tad, oracle, precision, tol, w_identity):
+    """newton_direction_reduced_basis (NewtonDirection.hh:76-123) with B the
+    free (interior) coordinates of a disk parametrisation whose boundary is
+    fixed: d = B (B^T H B + w I)^-1 (-B^T g) against a direct solve of the
+    reduced system assembled from the oracle's projected Hessian."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    w = meshes.disk_param(24, seed=3)
+    prec = tad.PREC_MIXED if precision == "mixed" else tad.PREC_FP64
+    fn = tad.ScalarFunction.from_workload(w, precision=prec, pcg_rel_tol=1e-12, pcg_max_iters=5000)
+    p = oracle.Problem.from_workload(w)
+    x = w.x0
+    F = np.asarray(w.terms[0].handles)
+    edges = np.sort(np.concatenate([F[:, [0, 1]], F[:, [1, 2]], F[:, [2, 0]]]), axis=1)
+    uniq, counts = np.unique(edges, axis=0, return_counts=True)
+    boundary = np.unique(uniq[counts == 1])
+    free_v = np.setdiff1d(np.arange(w.n_handles), boundary)
+    free = np.sort(np.concatenate([2 * free_v, 2 * free_v + 1]))
+    B = sp.csr_matrix((np.ones(free.size), (free, np.arange(free.size))), shape=(w.n_vars, free.size))
+    d, f, g = fn.newton_direction_reduced_basis(x, B, w_identity=w_identity)
+    fo, go, Ho = p.eval_with_hessian_proj(x)
+    Hr = (B.T @ Ho @ B + w_identity * sp.identity(free.size)).tocsc()
+    d_ref = B @ spla.spsolve(Hr, -(B.T @ go))
+    assert rel_err(f, fo) <= 1e-12
+    assert rel_err(d, d_ref) <= tol
+    assert np.all(d[2 * boundary] == 0.0) and np.all(d[2 * boundary + 1] == 0.0)

@@ -59,6 +59,7 @@ _lib = None
 
 # every symbol include/tad.h declares (checked by the CPU tests)
 EXPORTS = [
+    "tad_newton_direction_reduced_basis",
     "tad_settings_default", "tad_last_error_message", "tad_version", "tad_problem_create", "tad_problem_destroy",
     "tad_problem_set_settings", "tad_n_vars", "tad_add_elements", "tad_add_elements_custom", "tad_finalize",
     "tad_hessian_nnz", "tad_hessian_pattern", "tad_eval", "tad_eval_with_gradient", "tad_eval_with_derivatives",
@@ -102,6 +103,8 @@ def load(build_if_missing: bool = True):
     L.tad_eval_with_hessian_proj_d.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, _dp,
                                                ctypes.c_void_p, ctypes.c_void_p]
     L.tad_newton_direction.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_double, ctypes.c_double, _dp, _dp, _dp]
+    L.tad_newton_direction_reduced_basis.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int64, _ip, _ip, _dp, ctypes.c_double,
+                                                     ctypes.c_double, _dp, _dp, _dp]
     L.tad_line_search.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double, _dp, ctypes.c_double, _dp, _dp]
     L.tad_newton_solve.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_double, ctypes.c_double, _dp,
                                    ctypes.POINTER(ctypes.c_int)]
@@ -294,6 +297,29 @@ class ScalarFunction:
         g = np.zeros(self.n_vars)
         f = np.zeros(1)
         self._check(self.L.tad_newton_direction(self.h, _d(x), int(projected), projection_eps, 0.0, _d(d), _d(f), _d(g)),
+                    allow=(TAD_ERR_PCG_NOCONV,))
+        return d, float(f[0]), g
+
+    def newton_direction_reduced_basis(self, x, B, projection_eps: float = default_hessian_projection_eps,
+                                       w_identity: float = 0.0):
+        """newton_direction_reduced_basis(g, H_proj, B, solver, w): d = B (B^T H B
+        + w I)^-1 (-B^T g) with g, H_proj at x and B an (n_vars x m) scipy
+        sparse basis.  Returns (d, f, g)."""
+        import scipy.sparse as sp
+        x = self._x(x)
+        Bc = sp.csr_matrix(B)
+        if Bc.shape[0] != self.n_vars:
+            raise ValueError(f"basis has {Bc.shape[0]} rows, the problem {self.n_vars} variables")
+        Bc.sort_indices()
+        outer = np.ascontiguousarray(Bc.indptr, dtype=np.int32)
+        inner = np.ascontiguousarray(Bc.indices, dtype=np.int32)
+        vals = np.ascontiguousarray(Bc.data, dtype=np.float64)
+        d = np.zeros(self.n_vars)
+        g = np.zeros(self.n_vars)
+        f = np.zeros(1)
+        self._check(self.L.tad_newton_direction_reduced_basis(self.h, _d(x), int(Bc.shape[1]),
+                                                              outer.ctypes.data_as(_ip), inner.ctypes.data_as(_ip),
+                                                              _d(vals), projection_eps, w_identity, _d(d), _d(f), _d(g)),
                     allow=(TAD_ERR_PCG_NOCONV,))
         return d, float(f[0]), g
 

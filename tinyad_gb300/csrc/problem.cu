@@ -454,7 +454,7 @@ TAD_API tad_status tad_add_elements(tad_problem* P, int energy, int valence, int
 TAD_API tad_status tad_add_elements_custom(tad_problem* P, int valence, int64_t n_elem, tad_term_eval_fn fn, void* user)
 {
     if (!P || !fn) return fail(TAD_ERR_ARG, "NULL argument");
-    if (valence < 1 || valence > 8) return fail(TAD_ERR_ARG, "valence must be 1..8");
+    if (valence < 1 || valence > 64) return fail(TAD_ERR_ARG, "valence must be 1..64");
     if (P->finalized) return fail(TAD_ERR_STATE, "elements must be added before the first evaluation");
     Term T;
     T.energy = -1; T.N = valence; T.n_elem = n_elem; T.fn = fn; T.user = user;
