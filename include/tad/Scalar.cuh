@@ -60,8 +60,24 @@ struct DoubleFloat
     TAD_HD DoubleFloat() : hi(0.f), lo(0.f) {}
     TAD_HD DoubleFloat(double x) : hi((float)x), lo((float)(x - (double)(float)x)) {}
     TAD_HD DoubleFloat(float h, float l) : hi(h), lo(l) {}
-    TAD_HD explicit operator double() const { return (double)hi + (double)lo; }
+    TAD_HD explicit operator double() const { return float_to_double(hi) + float_to_double(lo); }
     TAD_HD explicit operator float() const { return hi + lo; }
+
+    /* exact float -> double; on the device by bit construction for normal
+       floats (the conversion instruction runs on the FP64 pipe) */
+    TAD_HD static double float_to_double(float v)
+    {
+#if defined(__CUDA_ARCH__)
+        const unsigned u = (unsigned)__float_as_int(v);
+        const unsigned ex = (u >> 23) & 0xffu;
+        if (ex != 0u && ex != 0xffu)
+            return __longlong_as_double((long long)(((unsigned long long)(u & 0x80000000u) << 32) |
+                                                    ((unsigned long long)(ex + 896u) << 52) |
+                                                    ((unsigned long long)(u & 0x7fffffu) << 29)));
+        if ((u << 1) == 0u) return __longlong_as_double((long long)((unsigned long long)(u & 0x80000000u) << 32));
+#endif
+        return (double)v;
+    }
 };
 
 TAD_HD DoubleFloat df_quick_two_sum(float a, float b)
@@ -112,55 +128,51 @@ struct DoubleFloatValue
     TAD_HD DoubleFloatValue(double x) : hi(0.f), lo(0.f)
     {
 #if defined(__CUDA_ARCH__)
-        // Bit-level split, no FP64 instruction: hi = the sign, exponent and
-        // top 23 stored mantissa bits of x (x truncated to float precision,
-        // exact); lo = the remaining 29 mantissa bits as an integer, rounded
-        // to nearest float (an integer conversion) and scaled by the exact
-        // power of two 2^(e - 1075) (|lo| < ulp(hi); the split is within
-        // 2^-49 |x|, unbiased).  Zero is exact; exponents where hi or the
-        // scale would leave the normal float range, and inf / NaN, take the
-        // rounding conversion below.
+        // Bit-level split with integer and FP32 instructions only (every
+        // branch: a short FP64 fallback would be if-converted and issued for
+        // all threads).  hi = the sign, exponent and top 23 stored mantissa
+        // bits of x (x truncated to float precision, exact); lo = the
+        // remaining 29 mantissa bits rounded to nearest float and scaled by
+        // the exact power of two 2^(e - 1075) (|lo| < ulp(hi); the split is
+        // within 2^-49 |x|).  The 29-bit integer becomes a float without a
+        // conversion instruction: for v < 2^23 the float with bits
+        // 0x4b000000 | v is exactly 2^23 + v, so both halves convert exactly
+        // by one subtraction and one FMA rounds rh 2^23 + rl once.  Below the
+        // normal float range x becomes a signed zero, above it +-inf; NaN
+        // stays NaN.
         const unsigned long long b = (unsigned long long)__double_as_longlong(x);
         const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
         const int e = (int)((b >> 52) & 0x7ff);
-        if ((b << 1) == 0ull) { hi = __int_as_float((int)sign); return; }
-        if (e >= 949 && e <= 1150)
+        if (e >= 897 && e <= 1150)
         {
             hi = __int_as_float((int)(sign | ((unsigned)(e - 896) << 23) | ((unsigned)(b >> 29) & 0x7fffffu)));
             const unsigned r = (unsigned)b & 0x1fffffffu;
-            const float scale = __int_as_float((int)((unsigned)(e - 948) << 23));   // 2^(e - 1075)
-            lo = __uint2float_rn(r) * scale;
+            const float rh = __int_as_float((int)(0x4b000000u | (r >> 23))) - 8388608.0f;
+            const float rl = __int_as_float((int)(0x4b000000u | (r & 0x7fffffu))) - 8388608.0f;
+            const float rf = __fmaf_rn(rh, 8388608.0f, rl);
+            if (e >= 949) lo = rf * __int_as_float((int)((unsigned)(e - 948) << 23));              // 2^(e - 1075)
+            else lo = (rf * __int_as_float((int)((unsigned)(e - 884) << 23))) * 5.42101086242752217e-20f;  // 2^(e - 1011) 2^-64
             if (sign) lo = -lo;
-            return;
         }
-#endif
+        else if (e == 2047)
+            hi = __int_as_float((int)(sign | 0x7f800000u | ((b & 0xfffffffffffffull) ? 0x400000u : 0u)));
+        else if (e > 1150)
+            hi = __int_as_float((int)(sign | 0x7f800000u));
+        else
+            hi = __int_as_float((int)sign);
+#else
         hi = (float)x;
         using std::isfinite;
         if (isfinite(hi)) lo = (float)(x - (double)hi);
+#endif
     }
     TAD_HD DoubleFloatValue(float x) : hi(x), lo(0.f) {}
     template <typename I, typename = std::enable_if_t<std::is_integral<I>::value>>
     TAD_HD DoubleFloatValue(I x) : DoubleFloatValue((double)x) {}
     TAD_HD DoubleFloatValue(float h, float l) : hi(h), lo(l) {}
-    TAD_HD explicit operator double() const { return float_to_double(hi) + float_to_double(lo); }
+    TAD_HD explicit operator double() const { return DoubleFloat::float_to_double(hi) + DoubleFloat::float_to_double(lo); }
     TAD_HD explicit operator float() const { return hi + lo; }
     TAD_HD explicit operator DoubleFloat() const { return DoubleFloat(hi, lo); }
-
-    /* exact float -> double; on the device by bit construction for normal
-       floats (the conversion instruction runs on the FP64 pipe) */
-    TAD_HD static double float_to_double(float v)
-    {
-#if defined(__CUDA_ARCH__)
-        const unsigned u = (unsigned)__float_as_int(v);
-        const unsigned ex = (u >> 23) & 0xffu;
-        if (ex != 0u && ex != 0xffu)
-            return __longlong_as_double((long long)(((unsigned long long)(u & 0x80000000u) << 32) |
-                                                    ((unsigned long long)(ex + 896u) << 52) |
-                                                    ((unsigned long long)(u & 0x7fffffu) << 29)));
-        if ((u << 1) == 0u) return __longlong_as_double((long long)((unsigned long long)(u & 0x80000000u) << 32));
-#endif
-        return (double)v;
-    }
 };
 
 TAD_HD float dfv_fma(float a, float b, float c)

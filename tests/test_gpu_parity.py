@@ -37,19 +37,21 @@ def test_known_answers_device(tad):
 
 def test_mixed_value_conversions(tad):
     """The mixed scalar's double-float value channel: double -> hi + lo on the
-    device is a bit-level split (no FP64 instruction) for exponents where
-    both parts are normal floats, and the rounding conversion elsewhere.  A
-    round trip through `a + 0` (op 29) must return the input within 2^-47
-    relative, keep signed zero, and propagate inf / NaN."""
+    device is a bit-level split without FP64 instructions.  A round trip
+    through `a + 0` (op 29) must return the input within 2^-47 relative in
+    the normal float range, give a signed zero below it and inf above it,
+    keep signed zero, and propagate inf / NaN."""
     rng = np.random.default_rng(5)
     vals = list(np.ldexp(rng.uniform(-1, 1, 200), rng.integers(-70, 70, 200)))
     vals += [1.0, -1.0, 0.1, 1.0 / 3.0, 2.0 ** -74, 2.0 ** -75, 1e-30, -1e-40, 1e-300, 3.0e38, -3.4e38, 1e39,
              1e300, np.nextafter(1.0, 2.0), 5e-324]
     for v in vals:
         got = tad.debug_scalar_op(29, (v, 1.0, 0.0), (0.0, 0.0, 0.0), tad.PREC_MIXED)[0]
-        if abs(v) < 1e-38 or abs(v) > 3.4e38:
-            # outside the normal float range the double-float cannot hold the value;
-            # the conversion rounds through float (flush to zero / infinity)
+        if abs(v) < 2.0 ** -126:
+            # below the normal float range the double-float cannot hold the value
+            # (the conversion gives a signed zero; `+ 0` then yields +0)
+            assert got == 0.0, (v, got)
+        elif abs(v) > 3.4e38:
             with np.errstate(over="ignore"):
                 as_float = np.float64(np.float32(v))
             assert got == as_float or abs(got - v) <= 2.0 ** -47 * abs(v), (v, got)
