@@ -37,6 +37,10 @@ METRIC = "Newton iters/s & element-Hessians/s, mixed vs FP64 GPU at 1e-8 energy 
 # sweeps), counted by oracle/flop_count.sh with an op-counting passive type.
 ELEM_FLOPS = {6: 15562, 12: 174837}
 UNIT = "Newton iters/s"
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one
+# ncu --set full capture of the same workload (profiles/k_elem_hessian_k_project_blocks_mixed_disk1024.md,
+# profiles/k_pcg_spmv_fused_fp32_disk1024.md); workloads without a capture report null
+NCU_TRAFFIC = {("disk1024", "mixed"): {"elem": (131.3e6 + 190.8e6) + (157.5e6 + 92.7e6), "spmv": 138.0e6 + 5.7e6}}
 
 
 def parse():
@@ -460,8 +464,9 @@ def main():
     share = {"spmv": stage["pcg_iters"] * prof["spmv"] / ms, "pcg_update": stage["pcg_iters"] * prof["pcg_update"] / ms,
              "elem_hessian": args.steps * prof["elem_hessian"] / ms,
              "ls_energy": stage["ls_trials"] * prof["ls_energy"] / ms, "assemble": args.steps * prof["assemble"] / ms}
+    traffic = NCU_TRAFFIC.get((args.workload, args.precision), {})
     roof_spmv = {"bound": "hbm", "kernel": "k_pcg_spmv_fused (BSR SpMV + p update + p.Ap)", "achieved": spmv_gbs,
-                 "peak": hbm, "unit": "GB/s", "frac": spmv_gbs / hbm, "traffic": None,
+                 "peak": hbm, "unit": "GB/s", "frac": spmv_gbs / hbm, "traffic": traffic.get("spmv"),
                  "peak_source": f"{hbm_src} copy bandwidth (MEASURED_PEAKS.json hbm_gbs)",
                  "algorithmic_bytes_per_launch": spmv_bytes, "ms_per_launch": prof["spmv"]}
     fp_peak = tad.measure_fma_peak(prec)
@@ -469,8 +474,9 @@ def main():
     elem_flops = ELEM_FLOPS.get(k_elem, 0) * w.terms[0].handles.shape[0]
     elem_tf = elem_flops / (prof["elem_hessian"] * 1e-3) / 1e12
     roof_elem = {"bound": "fp32 CUDA-core pipe" if prec == tad.PREC_MIXED else "fp64 CUDA-core pipe",
-                 "kernel": "k_elem_hessian (Double<k> eval + fused PSD projection)", "achieved": elem_tf,
-                 "peak": fp_peak, "unit": "TFLOP/s", "frac": elem_tf / fp_peak, "traffic": None,
+                 "kernel": "k_elem_hessian + k_project_blocks (Double<k> evaluation + PSD projection)", "achieved": elem_tf,
+                 "peak": fp_peak, "unit": "TFLOP/s", "frac": elem_tf / fp_peak, "traffic": traffic.get("elem"),
+                 "traffic_unit": "bytes per launch (ncu capture)",
                  "peak_source": "measured FMA throughput (tad_measure_fma_peak, this GPU)",
                  "algorithmic_flops_per_launch": elem_flops,
                  "flops_per_element": ELEM_FLOPS.get(k_elem, 0), "ms_per_launch": prof["elem_hessian"]}
