@@ -29,6 +29,11 @@
  *                             include/TinyAD/Utils/NewtonDirection.hh:25-65
  *   tad_newton_direction_reduced_basis  newton_direction_reduced_basis(g, H, B, solver)
  *                             include/TinyAD/Utils/NewtonDirection.hh:76-123
+ *   tad_add_vector_elements*, tad_vec_*, tad_eval_sum_of_squares_with_derivatives
+ *                             VectorFunction (include/TinyAD/VectorFunction.hh,
+ *                             Detail/VectorObjectiveTerm.hh)
+ *   tad_gauss_newton_direction gauss_newton_direction(r, J, solver, w)
+ *                             include/TinyAD/Utils/GaussNewtonDirection.hh:24-64
  *   tad_line_search           line_search(x, d, f, g, func)
  *                             include/TinyAD/Utils/LineSearch.hh:26-65
  *   tad_newton_solve          the Projected-Newton loop users write around the
@@ -90,6 +95,18 @@ typedef enum tad_energy {
     TAD_ENERGY_DIRICHLET_TRI = 4,
     TAD_ENERGY_COUNT_ = 5
 } tad_energy;
+
+/* Built-in residual functors of vector terms (VectorFunction). */
+typedef enum tad_vector_energy {
+    /* d=2, N=3, 8 outputs: params as TAD_ENERGY_SYMMETRIC_DIRICHLET_TRI.
+       r = sqrt(w) [J00 J01 J10 J11 Ji00 Ji01 Ji10 Ji11] with J = M Mr^-1,
+       Ji = Mr M^-1 (+inf residuals if det M <= 0), so sum r^2 is the
+       symmetric Dirichlet energy (tests/GaussNewtonTest.cc:33-66). */
+    TAD_VEC_SYMMETRIC_DIRICHLET_TRI = 0,
+    /* any d, N=1, d outputs: params [target(d) w].  r = sqrt(w) (target - p)
+       (tests/GaussNewtonTest.cc:67-74). */
+    TAD_VEC_POSITION = 1
+} tad_vector_energy;
 
 typedef enum tad_precision {
     TAD_PREC_FP64 = 0,   /* plain drop-in: everything in double */
@@ -162,6 +179,11 @@ typedef struct tad_term_eval_args {
     int32_t* record_d;        /* TAD_MODE_RECORD: write accessed handles here */
     int32_t* error_d;         /* device error word (OR in TAD_DEVERR_* bits) */
     void* stream;             /* cudaStream_t */
+    /* vector terms (VectorFunction) only; 0 / NULL for scalar terms */
+    int n_outputs;            /* residuals per element, M */
+    double* out_r_d;          /* [n_elem][M] residuals, or NULL */
+    double* out_J_d;          /* [n_elem][M][N*d] residual gradients in local slot order, or NULL */
+    double* out_Hv_d;         /* [n_elem][M][k(k+1)/2] packed residual Hessians, k = N*d, or NULL */
 } tad_term_eval_args;
 
 typedef enum tad_eval_mode {
@@ -170,8 +192,14 @@ typedef enum tad_eval_mode {
     TAD_MODE_HESSIAN = 2,     /* f, g, H */
     TAD_MODE_HESSIAN_PROJ = 3,/* f, g, PSD-projected H */
     TAD_MODE_LINESEARCH = 4,  /* f at x + s_j * dir for j < n_steps */
-    TAD_MODE_RECORD = 5       /* record first-access handle order */
+    TAD_MODE_RECORD = 5,      /* record first-access handle order */
+    TAD_MODE_VEC_JACOBIAN = 6,    /* vector terms: residuals and their gradients */
+    TAD_MODE_VEC_DERIVATIVES = 7  /* vector terms: residuals, gradients and Hessians */
 } tad_eval_mode;
+/* For vector terms the scalar modes refer to the sum of squares f = sum_i r_i^2:
+   VALUE and LINESEARCH write f per element, GRADIENT adds g = 2 J^T r, and
+   HESSIAN / HESSIAN_PROJ add the Gauss-Newton blocks 2 J_e^T J_e (PSD, so the
+   projection has nothing to do). */
 
 typedef int (*tad_term_eval_fn)(void* user, const tad_term_eval_args* args);
 
@@ -211,12 +239,53 @@ TAD_API tad_status tad_eval_with_hessian_proj_d(tad_problem* p, const double* x_
 
 /* d = -(H + w I)^-1 g with H the Hessian at x -- PSD-projected with proj_eps
    if `projected` (eval_with_hessian_proj), else exact (eval_with_derivatives)
-   -- solved by block-Jacobi PCG on the device (w_identity must be 0).
+   -- solved by block-Jacobi PCG on the device (w_identity >= 0).
    Returns TAD_ERR_PCG_NOCONV if the tolerance is not met (d then holds the
    last iterate). */
 TAD_API tad_status tad_newton_direction(tad_problem* p, const double* x_h, int projected,
                                         double proj_eps, double w_identity,
                                         double* d_h, double* f, double* g_h);
+
+/* ---- vector functions (include/TinyAD/VectorFunction.hh) -----------------
+   A problem holds either scalar terms (tad_add_elements*) or vector terms
+   (tad_add_vector_elements*), whose functors return n_outputs residuals per
+   element.  On a vector problem the scalar entry points act on the sum of
+   squares f = sum_i r_i^2 (tad_eval = eval_sum_of_squares; gradient 2 J^T r;
+   the Hessian entry points and tad_newton_solve use the Gauss-Newton matrix
+   2 J^T J, so tad_newton_solve runs Gauss-Newton with the Armijo line search
+   on f).  Residuals are numbered term by term, element by element
+   (Detail/VectorObjectiveTerm.hh:160-215). */
+TAD_API tad_status tad_add_vector_elements(tad_problem* p, int energy, int valence, int n_outputs,
+                                           int64_t n_elem, const int32_t* element_vertices_h,
+                                           const double* params_h, int n_params);
+TAD_API tad_status tad_add_vector_elements_custom(tad_problem* p, int valence, int n_outputs, int64_t n_elem,
+                                                  tad_term_eval_fn fn, void* user);
+/* number of residuals (VectorFunction::n_outputs) */
+TAD_API int64_t tad_n_outputs(const tad_problem* p);
+/* VectorFunction::eval: r[n_outputs] */
+TAD_API tad_status tad_vec_eval(tad_problem* p, const double* x_h, double* r_h);
+/* the Jacobian's CSR pattern (n_outputs x n_vars, columns sorted per row):
+   the variables of each residual's element, as the reference's triplets
+   (VectorObjectiveTerm.hh:214-221) */
+TAD_API tad_status tad_vec_jacobian_nnz(tad_problem* p, int64_t* nnz);
+TAD_API tad_status tad_vec_jacobian_pattern(tad_problem* p, int32_t* outer, int32_t* inner);
+/* VectorFunction::eval_with_jacobian: r and the CSR values of J */
+TAD_API tad_status tad_vec_eval_with_jacobian(tad_problem* p, const double* x_h, double* r_h, double* J_values_h);
+/* VectorFunction::eval_with_derivatives: r, J and the residual Hessians as
+   triplets, output i owning [H_ptr[i], H_ptr[i+1]) (tad_vec_hessians_nnz
+   entries in all) */
+TAD_API tad_status tad_vec_hessians_nnz(tad_problem* p, int64_t* nnz);
+TAD_API tad_status tad_vec_eval_with_derivatives(tad_problem* p, const double* x_h, double* r_h, double* J_values_h,
+                                                 int64_t* H_ptr, int32_t* H_row, int32_t* H_col, double* H_val);
+/* VectorFunction::eval_sum_of_squares_with_derivatives: f, g = 2 J^T r, r, J
+   (Detail/VectorFunctionImpl.hh:271-283) */
+TAD_API tad_status tad_eval_sum_of_squares_with_derivatives(tad_problem* p, const double* x_h, double* f,
+                                                            double* g_h, double* r_h, double* J_values_h);
+/* gauss_newton_direction(r, J, solver, w) (Utils/GaussNewtonDirection.hh:24-47)
+   at x: d = -(J^T J + w I)^-1 J^T r, device PCG to pcg_rel_tol; also returns
+   f and g of the sum of squares. */
+TAD_API tad_status tad_gauss_newton_direction(tad_problem* p, const double* x_h, double w_identity, double* d_h,
+                                              double* f, double* g_h);
 
 /* newton_direction_reduced_basis(g, H_proj, B, solver, w)
    (include/TinyAD/Utils/NewtonDirection.hh:76-123): with g and the projected

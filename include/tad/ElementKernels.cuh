@@ -45,6 +45,9 @@ struct ElemLaunch
     void* out_H;
     int32_t* record;         /* record mode output */
     int32_t* err;
+    double* out_r;           /* vector terms: residuals [n_elem][M] */
+    double* out_J;           /* vector terms: residual gradients [n_elem][M][k] */
+    double* out_Hv;          /* vector terms: packed residual Hessians [n_elem][M][k(k+1)/2] */
 };
 
 template <int d, int N, typename Energy>
@@ -237,6 +240,9 @@ inline ElemLaunch make_launch(const tad_term_eval_args& a)
     L.out_H = a.out_H_d;
     L.record = a.record_d;
     L.err = a.error_d;
+    L.out_r = a.out_r_d;
+    L.out_J = a.out_J_d;
+    L.out_Hv = a.out_Hv_d;
     return L;
 }
 
@@ -285,6 +291,164 @@ inline void launch_elements(int mode, int precision, const ElemLaunch& L, const 
         else launch_elements_hessian<d, N, double>(L, energy, s);
     }
     else launch_elements_first_order<d, N>(mode, L, energy, s, precision);
+}
+
+/* ---------------------------------------------------------------------------
+ * Vector functors (VectorFunction, include/TinyAD/Detail/VectorObjectiveTerm.hh):
+ * the functor returns tad::Vec<T, M>, M residuals per element.  The scalar
+ * modes evaluate the sum of squares f_e = sum_o r_o^2 (VALUE, LINESEARCH),
+ * its gradient 2 sum_o r_o grad r_o (GRADIENT) and the Gauss-Newton blocks
+ * 2 sum_o grad r_o grad r_o^T (HESSIAN, HESSIAN_PROJ; PSD, written as the
+ * vertex-pair blocks the assembly of scalar terms reads).  VEC_JACOBIAN adds
+ * the residuals and their gradients in local slot order, VEC_DERIVATIVES also
+ * the packed residual Hessians.  FP64 (the Gauss-Newton blocks are written
+ * in the problem's Hessian precision T).
+ * ------------------------------------------------------------------------ */
+template <int d, int N, int M, typename Energy>
+__global__ void __launch_bounds__(128) k_vec_value(ElemLaunch L, Energy energy)
+{
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= L.n_elem) return;
+    PassiveElement<d, N, double> el{e, L.x};
+    const Vec<double, M> r = energy(el);
+    double f = 0.0;
+#pragma unroll
+    for (int o = 0; o < M; ++o)
+    {
+        f += r[o] * r[o];
+        if (L.out_r) L.out_r[e * M + o] = r[o];
+    }
+    L.out_f[e] = f;
+}
+
+template <int d, int N, int M, typename Energy>
+__global__ void __launch_bounds__(128) k_vec_linesearch(ElemLaunch L, Energy energy)
+{
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= L.n_elem) return;
+    for (int j = 0; j < L.n_steps; ++j)
+    {
+        LineSearchElement<d, N, double> el{e, L.x, L.dir, L.steps[j]};
+        const Vec<double, M> r = energy(el);
+        double f = 0.0;
+#pragma unroll
+        for (int o = 0; o < M; ++o) f += r[o] * r[o];
+        L.out_f[(int64_t)j * L.f_stride + e] = f;
+    }
+}
+
+/* first order: f, g = 2 J^T r, optionally r and J, optionally the
+   Gauss-Newton blocks (gn) in precision T */
+template <int d, int N, int M, typename T, typename Energy>
+__global__ void __launch_bounds__(128) k_vec_first_order(ElemLaunch L, Energy energy, bool gn)
+{
+    constexpr int k = d * N;
+    constexpr int NP = N * (N + 1) / 2;
+    using S = Scalar<k, double, false>;
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= L.n_elem) return;
+    ActiveElement<d, N, S> el;
+    el.handle = e;
+    el.x = L.x;
+    el.err = L.err;
+#pragma unroll
+    for (int i = 0; i < N; ++i) el.vh[i] = L.rec[e * N + i];
+    const Vec<S, M> r = energy(el);
+    double f = 0.0, g[k];
+    bool fin = true;
+#pragma unroll
+    for (int i = 0; i < k; ++i) g[i] = 0.0;
+#pragma unroll
+    for (int o = 0; o < M; ++o)
+    {
+        const double ro = r[o].val;
+        f += ro * ro;
+        if (L.out_r) L.out_r[e * M + o] = ro;
+#pragma unroll
+        for (int i = 0; i < k; ++i)
+        {
+            g[i] += 2.0 * ro * r[o].grad[i];
+            fin = fin && finite_val(r[o].grad[i]);
+            if (L.out_J) L.out_J[(e * M + o) * k + i] = r[o].grad[i];
+        }
+    }
+    L.out_f[e] = f;
+    store_row<double, k>((double*)L.out_g, e, g);
+    if (gn)
+    {
+        T hb[NP * d * d];
+#pragma unroll
+        for (int a = 0; a < N; ++a)
+#pragma unroll
+            for (int b = a; b < N; ++b)
+#pragma unroll
+                for (int p = 0; p < d; ++p)
+#pragma unroll
+                    for (int q = 0; q < d; ++q)
+                    {
+                        const int i = a * d + p, j = b * d + q;
+                        double acc = 0.0;
+#pragma unroll
+                        for (int o = 0; o < M; ++o) acc += r[o].grad[i] * r[o].grad[j];
+                        hb[packed_index(a, b, N) * d * d + p * d + q] = (T)(2.0 * acc);
+                    }
+        store_row<T, NP * d * d>((T*)L.out_H, e, hb);
+    }
+    if (!fin) report_error(L.err, DEVERR_NONFINITE);
+}
+
+/* second order: r, J and the packed residual Hessians */
+template <int d, int N, int M, typename Energy>
+__global__ void __launch_bounds__(128) k_vec_second_order(ElemLaunch L, Energy energy)
+{
+    constexpr int k = d * N;
+    constexpr int NH = k * (k + 1) / 2;
+    using S = Scalar<k, double, true>;
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= L.n_elem) return;
+    ActiveElement<d, N, S> el;
+    el.handle = e;
+    el.x = L.x;
+    el.err = L.err;
+#pragma unroll
+    for (int i = 0; i < N; ++i) el.vh[i] = L.rec[e * N + i];
+    const Vec<S, M> r = energy(el);
+    double f = 0.0;
+#pragma unroll
+    for (int o = 0; o < M; ++o)
+    {
+        f += r[o].val * r[o].val;
+        if (L.out_r) L.out_r[e * M + o] = r[o].val;
+#pragma unroll
+        for (int i = 0; i < k; ++i)
+            if (L.out_J) L.out_J[(e * M + o) * k + i] = r[o].grad[i];
+#pragma unroll
+        for (int q = 0; q < NH; ++q)
+            if (L.out_Hv) L.out_Hv[(e * M + o) * NH + q] = r[o].hess[q];
+    }
+    L.out_f[e] = f;
+}
+
+/* Launch the vector-term kernel for `mode` on stream s. */
+template <int d, int N, int M, typename Energy>
+inline void launch_vector_elements(int mode, int precision, const ElemLaunch& L, const Energy& energy, cudaStream_t s)
+{
+    if (L.n_elem <= 0) return;
+    const unsigned g = elem_grid(L.n_elem);
+    switch (mode)
+    {
+    case 0: k_vec_value<d, N, M, Energy><<<g, 128, 0, s>>>(L, energy); break;
+    case 4: k_vec_linesearch<d, N, M, Energy><<<g, 128, 0, s>>>(L, energy); break;
+    case 5: k_elem_record<d, N, Energy><<<g, 128, 0, s>>>(L, energy); break;
+    case 1:
+    case 6: k_vec_first_order<d, N, M, double, Energy><<<g, 128, 0, s>>>(L, energy, false); break;
+    case 2:
+    case 3:
+        if (precision == 1) k_vec_first_order<d, N, M, float, Energy><<<g, 128, 0, s>>>(L, energy, true);
+        else k_vec_first_order<d, N, M, double, Energy><<<g, 128, 0, s>>>(L, energy, true);
+        break;
+    case 7: k_vec_second_order<d, N, M, Energy><<<g, 128, 0, s>>>(L, energy); break;
+    }
 }
 
 } // namespace tad

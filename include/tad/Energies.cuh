@@ -8,6 +8,9 @@
  *   PositionPenalty        tests/NewtonTest.cc:48-55 (weight per element)
  *   Quadratic              the quadratics of tests/ScalarFunctionTest.cc
  *   DirichletTri           the Laplacian energy of tests/DynamicElementsTest.cc:60-91
+ * and the residual functors of vector terms (VectorFunction):
+ *   SymmetricDirichletTriResiduals  the 8 residuals of tests/GaussNewtonTest.cc:33-66
+ *   PositionResiduals      the 2 residuals of tests/GaussNewtonTest.cc:67-74
  *
  * Each functor reads its element's vertex handles (`vtx`, n_elem x N) and
  * parameters (`prm`, n_elem x P) through element.handle, the way the
@@ -182,5 +185,71 @@ TAD_HD S symmetric_dirichlet_tri_rest(const Vec<S, 2>& a, const Vec<S, 2>& b, co
     if (to_passive(determinant(M)) <= 0.0) return S(INFINITY);
     return ((M * inverse(Mr)).squaredNorm() + (Mr * inverse(M)).squaredNorm()) * (an * 0.5);
 }
+
+/* Residual form of SymmetricDirichletTri: sqrt(w) times the entries of
+   J = M Mr^-1 and of J^-1 = Mr M^-1 (row-major, J first), so the sum of
+   squares is the symmetric Dirichlet energy (tests/GaussNewtonTest.cc:33-66,
+   weight 1/#F there).  Params as SymmetricDirichletTri: Mr (column-major), w. */
+struct SymmetricDirichletTriResiduals
+{
+    static constexpr int d = 2, N = 3, M = 8, n_params = 5;
+    const int32_t* vtx;
+    const double* prm;
+
+    template <typename El>
+    TAD_HD auto operator()(El& element) const -> Vec<TAD_SCALAR_TYPE(element), 8>
+    {
+        using T = TAD_SCALAR_TYPE(element);
+        using P = TAD_PASSIVE_TYPE(element);
+        const int64_t e = element.handle;
+        const double* p = prm + e * n_params;
+        Mat<P, 2, 2> Mr;
+        Mr.m[0] = P(p[0]); Mr.m[1] = P(p[1]); Mr.m[2] = P(p[2]); Mr.m[3] = P(p[3]);
+        const Vec<T, 2> a = element.variables(vtx[e * 3 + 0]);
+        const Vec<T, 2> b = element.variables(vtx[e * 3 + 1]);
+        const Vec<T, 2> c = element.variables(vtx[e * 3 + 2]);
+        const Mat<T, 2, 2> Mt = col_mat(b - a, c - a);
+        Vec<T, 8> E;
+        if (determinant(Mt) <= 0.0)
+        {
+#pragma unroll
+            for (int o = 0; o < 8; ++o) E[o] = T(INFINITY);
+            return E;
+        }
+        const Mat<T, 2, 2> J = Mt * inverse(Mr);
+        const Mat<T, 2, 2> Ji = Mr * inverse(Mt);
+        using std::sqrt;
+        const P s = P(sqrt(p[4]));
+        E[0] = J(0, 0) * s; E[1] = J(0, 1) * s; E[2] = J(1, 0) * s; E[3] = J(1, 1) * s;
+        E[4] = Ji(0, 0) * s; E[5] = Ji(0, 1) * s; E[6] = Ji(1, 0) * s; E[7] = Ji(1, 1) * s;
+        return E;
+    }
+};
+
+/* Residual form of PositionPenalty: sqrt(w) (target - p), D residuals
+   (tests/GaussNewtonTest.cc:67-74).  Params: target (D), w. */
+template <int D>
+struct PositionResiduals
+{
+    static constexpr int d = D, N = 1, M = D, n_params = D + 1;
+    const int32_t* vtx;
+    const double* prm;
+
+    template <typename El>
+    TAD_HD auto operator()(El& element) const -> Vec<TAD_SCALAR_TYPE(element), D>
+    {
+        using T = TAD_SCALAR_TYPE(element);
+        using P = TAD_PASSIVE_TYPE(element);
+        const int64_t e = element.handle;
+        const double* p = prm + e * n_params;
+        using std::sqrt;
+        const P s = P(sqrt(p[D]));
+        const Vec<T, D> x = element.variables(vtx[e]);
+        Vec<T, D> r;
+#pragma unroll
+        for (int i = 0; i < D; ++i) r[i] = (P(p[i]) - x[i]) * s;
+        return r;
+    }
+};
 
 } // namespace tad

@@ -76,6 +76,7 @@ inline IndexRange range(int64_t n) { return {n}; }
 struct SparseCSR
 {
     int64_t rows = 0;
+    int64_t cols = 0;        // 0: square (rows x rows)
     std::vector<int32_t> outer, inner;
     std::vector<double> values;
     int64_t nonZeros() const { return (int64_t)values.size(); }
@@ -120,6 +121,18 @@ struct Term : TermBase
     int launch(const tad_term_eval_args* a) override
     {
         tad::launch_elements<d, N>(a->mode, a->precision, make_launch(*a), fn, (cudaStream_t)a->stream);
+        return cudaGetLastError() == cudaSuccess ? 0 : 1;
+    }
+};
+
+template <int d, int N, int M, typename F>
+struct VecTerm : TermBase
+{
+    HandleMapped<F> fn;
+    explicit VecTerm(HandleMapped<F> f) : fn(std::move(f)) {}
+    int launch(const tad_term_eval_args* a) override
+    {
+        tad::launch_vector_elements<d, N, M>(a->mode, a->precision, make_launch(*a), fn, (cudaStream_t)a->stream);
         return cudaGetLastError() == cudaSuccess ? 0 : 1;
     }
 };
@@ -315,7 +328,16 @@ public:
         return x;
     }
 
-private:
+protected:
+    int32_t* upload_handles(const std::vector<int32_t>& h)
+    {
+        int32_t* hd = nullptr;
+        check_cuda(cudaMalloc(&hd, std::max<size_t>(h.size(), 1) * sizeof(int32_t)));
+        handle_bufs_.push_back(hd);
+        if (!h.empty()) check_cuda(cudaMemcpy(hd, h.data(), h.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+        return hd;
+    }
+
     /* distinct accessed handles per element, recorded on the device with the
        functor evaluated at x = 0 and at most vmax handles an element */
     template <int vmax, typename F>
@@ -391,6 +413,129 @@ private:
     std::vector<int32_t*> handle_bufs_;
     std::vector<int64_t> term_sizes_;
 };
+
+/* VectorFunction<d> (include/TinyAD/VectorFunction.hh): elements return
+   tad::Vec<T, M>, M residuals each, numbered term by term, element by
+   element.  The inherited scalar methods act on the sum of squares |r|^2
+   (eval_with_gradient: g = 2 J^T r; newton_solve: Gauss-Newton iterations
+   with the Armijo line search on |r|^2). */
+template <int d>
+class VectorFunction : public ScalarFunction<d>
+{
+public:
+    explicit VectorFunction(int64_t n_handles, const tad_settings* settings = nullptr) : ScalarFunction<d>(n_handles, settings) {}
+
+    /* add_elements<N, M>(range, functor) (VectorFunction.hh:48-57) */
+    template <int N, int M, typename Range, typename F>
+    void add_elements(const Range& elements, F functor)
+    {
+        std::vector<int32_t> h;
+        for (auto eh : elements) h.push_back((int32_t)eh);
+        int32_t* hd = this->upload_handles(h);
+        auto term = std::make_unique<detail::VecTerm<d, N, M, F>>(detail::HandleMapped<F>{functor, hd});
+        check(tad_add_vector_elements_custom(this->p_, N, M, (int64_t)h.size(), &detail::term_callback, term.get()));
+        this->terms_.push_back(std::move(term));
+        this->term_sizes_.push_back((int64_t)h.size());
+    }
+
+    int64_t n_outputs() const { return tad_n_outputs(this->p_); }
+
+    /* eval(x): the residual vector */
+    std::vector<double> eval(const std::vector<double>& x) const
+    {
+        std::vector<double> r(n_outputs());
+        check(tad_vec_eval(this->p_, x.data(), r.data()));
+        return r;
+    }
+    std::vector<double> operator()(const std::vector<double>& x) const { return eval(x); }
+    double eval_sum_of_squares(const std::vector<double>& x) const { return ScalarFunction<d>::eval(x); }
+
+    std::tuple<std::vector<double>, SparseCSR> eval_with_jacobian(const std::vector<double>& x) const
+    {
+        std::vector<double> r(n_outputs());
+        SparseCSR J = jacobian_pattern();
+        check(tad_vec_eval_with_jacobian(this->p_, x.data(), r.data(), J.values.data()));
+        return {std::move(r), std::move(J)};
+    }
+
+    /* (r, J, H): H[i] the Hessian of residual i (n_vars x n_vars, CSR) */
+    std::tuple<std::vector<double>, SparseCSR, std::vector<SparseCSR>> eval_with_derivatives(const std::vector<double>& x) const
+    {
+        const int64_t m = n_outputs();
+        std::vector<double> r(m);
+        SparseCSR J = jacobian_pattern();
+        int64_t nnz = 0;
+        check(tad_vec_hessians_nnz(this->p_, &nnz));
+        std::vector<int64_t> hp(m + 1);
+        std::vector<int32_t> hr(nnz), hc(nnz);
+        std::vector<double> hv(nnz);
+        check(tad_vec_eval_with_derivatives(this->p_, x.data(), r.data(), J.values.data(), hp.data(), hr.data(), hc.data(),
+                                            hv.data()));
+        std::vector<SparseCSR> H(m);
+        const int64_t n = this->n_vars();
+        for (int64_t i = 0; i < m; ++i)
+        {
+            SparseCSR& Hi = H[i];
+            Hi.rows = n;
+            Hi.outer.assign(n + 1, 0);
+            std::vector<std::tuple<int32_t, int32_t, double>> t;
+            for (int64_t q = hp[i]; q < hp[i + 1]; ++q) t.emplace_back(hr[q], hc[q], hv[q]);
+            std::sort(t.begin(), t.end());
+            for (const auto& e : t)
+            {
+                ++Hi.outer[std::get<0>(e) + 1];
+                Hi.inner.push_back(std::get<1>(e));
+                Hi.values.push_back(std::get<2>(e));
+            }
+            for (int64_t r2 = 0; r2 < n; ++r2) Hi.outer[r2 + 1] += Hi.outer[r2];
+        }
+        return {std::move(r), std::move(J), std::move(H)};
+    }
+
+    /* (f, g, r, J), f = |r|^2, g = 2 J^T r (VectorFunctionImpl.hh:271-283) */
+    std::tuple<double, std::vector<double>, std::vector<double>, SparseCSR>
+    eval_sum_of_squares_with_derivatives(const std::vector<double>& x) const
+    {
+        double f;
+        std::vector<double> g(this->n_vars()), r(n_outputs());
+        SparseCSR J = jacobian_pattern();
+        check(tad_eval_sum_of_squares_with_derivatives(this->p_, x.data(), &f, g.data(), r.data(), J.values.data()));
+        return {f, std::move(g), std::move(r), std::move(J)};
+    }
+
+    /* gauss_newton_direction(r, J, solver, w) at x (GaussNewtonDirection.hh:24-47) */
+    std::vector<double> gauss_newton_direction(const std::vector<double>& x, double w_identity = 0.0) const
+    {
+        std::vector<double> dvec(this->n_vars());
+        const tad_status s = tad_gauss_newton_direction(this->p_, x.data(), w_identity, dvec.data(), nullptr, nullptr);
+        if (s != TAD_OK && s != TAD_ERR_PCG_NOCONV) check(s);
+        return dvec;
+    }
+
+private:
+    SparseCSR jacobian_pattern() const
+    {
+        int64_t nnz = 0;
+        check(tad_vec_jacobian_nnz(this->p_, &nnz));
+        SparseCSR J;
+        J.rows = n_outputs();
+        J.cols = this->n_vars();
+        J.outer.resize(J.rows + 1);
+        J.inner.resize(nnz);
+        J.values.resize(nnz);
+        check(tad_vec_jacobian_pattern(this->p_, J.outer.data(), J.inner.data()));
+        return J;
+    }
+};
+
+/* vector_function<d>(range) (VectorFunction.hh:198-206) */
+template <int d, typename Range>
+VectorFunction<d> vector_function(const Range& variables, const tad_settings* settings = nullptr)
+{
+    int64_t n = 0;
+    for (auto v : variables) { (void)v; ++n; }
+    return VectorFunction<d>(n, settings);
+}
 
 /* scalar_function<d>(range) (ScalarFunctionImpl.hh:418-442) */
 template <int d, typename Range>

@@ -6,6 +6,8 @@
  *   element variables    tests/ScalarFunctionTest.cc:153-179 (dedup, too many variables)
  *   reduced basis        tests/SwitchSolverTest.cc:16-36 (Newton step (-1, -1))
  *   dynamic valences     tests/DynamicElementsTest.cc:9-33 (grouping, term sizes, f/g/H)
+ *   vector function      tests/VectorFunctionTest.cc:9-72 (r, J, residual Hessians, sum of squares)
+ *   Gauss-Newton         tests/GaussNewtonTest.cc:13-158 (planar mesh, f -> 4)
  *   Laplacian            tests/DynamicElementsTest.cc:35-141 (static triangles and dynamic
  *                        one-ring elements vs the assembled Laplacian, on a closed torus
  *                        with vertex valences 4 and 8)
@@ -298,6 +300,115 @@ static int dynamic_laplacian()
     return 0;
 }
 
+static int vector_function_basic()
+{
+    // R^2 -> R^3: element 1 gives (2 x0, x0^2), element 2 gives (x1^2)
+    auto func = tad::vector_function<1>(tad::range(2));
+    func.add_elements<1, 2>(tad::range(1), [] __device__(auto& element) {
+        using T = TAD_SCALAR_TYPE(element);
+        const T x0 = element.variables(0)[0];
+        tad::Vec<T, 2> r;
+        r[0] = 2.0 * x0;
+        r[1] = tad::sqr(x0);
+        return r;
+    });
+    func.add_elements<1, 1>(tad::range(1), [] __device__(auto& element) {
+        using T = TAD_SCALAR_TYPE(element);
+        const T x1 = element.variables(1)[0];
+        tad::Vec<T, 1> r;
+        r[0] = tad::sqr(x1);
+        return r;
+    });
+    const std::vector<double> x = {3.0, 4.0};
+    const std::vector<double> r = func.eval(x);
+    CHECK(r.size() == 3 && r[0] == 6.0 && r[1] == 9.0 && r[2] == 16.0);
+    CHECK(func.eval_sum_of_squares(x) == 373.0);
+    auto [f, g, rs, Js] = func.eval_sum_of_squares_with_derivatives(x);
+    CHECK(f == 373.0 && rs[2] == 16.0);
+    CHECK(g[0] == 8.0 * x[0] + 4.0 * x[0] * x[0] * x[0] && g[1] == 4.0 * x[1] * x[1] * x[1]);
+    auto [rj, J] = func.eval_with_jacobian(x);
+    CHECK(J.rows == 3 && J.cols == 2);
+    CHECK(J.coeff(0, 0) == 2.0 && J.coeff(1, 0) == 6.0 && J.coeff(2, 1) == 8.0 && J.coeff(0, 1) == 0.0);
+    auto [rh, Jh, H] = func.eval_with_derivatives(x);
+    CHECK(H.size() == 3);
+    CHECK(H[0].coeff(0, 0) == 0.0 && H[1].coeff(0, 0) == 2.0 && H[2].coeff(1, 1) == 2.0);
+    return 0;
+}
+
+static int gauss_newton_planar()
+{
+    // tests/GaussNewtonTest.cc: symmetric Dirichlet residuals (8 per triangle)
+    // and position residuals, 20 Gauss-Newton steps with w = 1e-12
+    const std::vector<double> V_rest = {0, 0, 1, 0, 0, 1, 1, 1, 0, 2, 1, 2};
+    std::vector<double> V = V_rest;
+    for (int v = 0; v < 6; ++v) { V[2 * v] *= 0.5; V[2 * v + 1] *= 0.25; }
+    const std::vector<int> F = {0, 1, 2, 1, 3, 2, 2, 3, 5, 2, 5, 4};
+    const std::vector<int> b = {0, 4};
+    const std::vector<double> bc = {0.0, 0.0, -2.0, 0.0};
+    const double* Vr = to_device(V_rest);
+    const int* Fd = to_device(F);
+    const int* bd = to_device(b);
+    const double* bcd = to_device(bc);
+    const int nF = 4;
+    tad_settings st;
+    tad_settings_default(&st);
+    st.pcg_rel_tol = 1e-12;
+    auto func = tad::vector_function<2>(tad::range(6), &st);
+    func.add_elements<3, 8>(tad::range(nF), [=] __device__(auto& element) {
+        using T = TAD_SCALAR_TYPE(element);
+        using P = TAD_PASSIVE_TYPE(element);
+        const int f = (int)element.handle;
+        tad::Vec<P, 2> ar, br, cr;
+        for (int i = 0; i < 2; ++i)
+        {
+            ar[i] = (P)Vr[2 * Fd[3 * f + 0] + i];
+            br[i] = (P)Vr[2 * Fd[3 * f + 1] + i];
+            cr[i] = (P)Vr[2 * Fd[3 * f + 2] + i];
+        }
+        const tad::Mat<P, 2, 2> Mr = tad::col_mat(br - ar, cr - ar);
+        const tad::Vec<T, 2> a = element.variables(Fd[3 * f + 0]);
+        const tad::Vec<T, 2> bb = element.variables(Fd[3 * f + 1]);
+        const tad::Vec<T, 2> c = element.variables(Fd[3 * f + 2]);
+        const tad::Mat<T, 2, 2> M = tad::col_mat(bb - a, c - a);
+        tad::Vec<T, 8> E;
+        if (tad::determinant(M) <= 0.0)
+        {
+            for (int o = 0; o < 8; ++o) E[o] = T(INFINITY);
+            return E;
+        }
+        const tad::Mat<T, 2, 2> J = M * tad::inverse(Mr);
+        const tad::Mat<T, 2, 2> Ji = Mr * tad::inverse(M);
+        const P s = P(1.0 / sqrt((double)nF));
+        E[0] = J(0, 0) * s; E[1] = J(0, 1) * s; E[2] = J(1, 0) * s; E[3] = J(1, 1) * s;
+        E[4] = Ji(0, 0) * s; E[5] = Ji(0, 1) * s; E[6] = Ji(1, 0) * s; E[7] = Ji(1, 1) * s;
+        return E;
+    });
+    func.add_elements<1, 2>(tad::range(2), [=] __device__(auto& element) {
+        using T = TAD_SCALAR_TYPE(element);
+        using P = TAD_PASSIVE_TYPE(element);
+        const int h = (int)element.handle;
+        const tad::Vec<T, 2> p = element.variables(bd[h]);
+        tad::Vec<T, 2> r;
+        r[0] = P(bcd[2 * h]) - p[0];
+        r[1] = P(bcd[2 * h + 1]) - p[1];
+        return r;
+    });
+    CHECK(func.n_outputs() == 4 * 8 + 2 * 2);
+    std::vector<double> x = func.x_from_data([&](int64_t v) { return std::array<double, 2>{V[2 * v], V[2 * v + 1]}; });
+    for (int i = 0; i < 20; ++i)
+    {
+        auto [f, g, r, J] = func.eval_sum_of_squares_with_derivatives(x);
+        const std::vector<double> d = func.gauss_newton_direction(x, 1e-12);
+        x = func.line_search(x, d, f, g);
+    }
+    auto [f, g, r, J] = func.eval_sum_of_squares_with_derivatives(x);
+    double gmax = 0.0;
+    for (double v : g) gmax = std::fmax(gmax, std::fabs(v));
+    std::printf("gauss-newton planar: f = %.12g, |g|max = %.3g\n", f, gmax);
+    CHECK(std::fabs(f - 4.0) <= 0.1 && gmax <= 0.1);
+    return 0;
+}
+
 int main()
 {
     if (planar_newton()) return 1;
@@ -305,6 +416,8 @@ int main()
     if (element_variables()) return 1;
     if (dynamic_valences()) return 1;
     if (dynamic_laplacian()) return 1;
+    if (vector_function_basic()) return 1;
+    if (gauss_newton_planar()) return 1;
     std::printf("frontend ok\n");
     return 0;
 }

@@ -59,7 +59,10 @@ _lib = None
 
 # every symbol include/tad.h declares (checked by the CPU tests)
 EXPORTS = [
-    "tad_newton_direction_reduced_basis",
+    "tad_newton_direction_reduced_basis", "tad_add_vector_elements", "tad_add_vector_elements_custom", "tad_n_outputs",
+    "tad_vec_eval", "tad_vec_jacobian_nnz", "tad_vec_jacobian_pattern", "tad_vec_eval_with_jacobian",
+    "tad_vec_hessians_nnz", "tad_vec_eval_with_derivatives", "tad_eval_sum_of_squares_with_derivatives",
+    "tad_gauss_newton_direction",
     "tad_settings_default", "tad_last_error_message", "tad_version", "tad_problem_create", "tad_problem_destroy",
     "tad_problem_set_settings", "tad_n_vars", "tad_add_elements", "tad_add_elements_custom", "tad_finalize",
     "tad_hessian_nnz", "tad_hessian_pattern", "tad_eval", "tad_eval_with_gradient", "tad_eval_with_derivatives",
@@ -103,6 +106,18 @@ def load(build_if_missing: bool = True):
     L.tad_eval_with_hessian_proj_d.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, _dp,
                                                ctypes.c_void_p, ctypes.c_void_p]
     L.tad_newton_direction.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_double, ctypes.c_double, _dp, _dp, _dp]
+    L.tad_add_vector_elements.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int64, _ip,
+                                          _dp, ctypes.c_int]
+    L.tad_n_outputs.argtypes = [ctypes.c_void_p]
+    L.tad_n_outputs.restype = ctypes.c_int64
+    L.tad_vec_eval.argtypes = [ctypes.c_void_p, _dp, _dp]
+    L.tad_vec_jacobian_nnz.argtypes = [ctypes.c_void_p, _i64p]
+    L.tad_vec_jacobian_pattern.argtypes = [ctypes.c_void_p, _ip, _ip]
+    L.tad_vec_eval_with_jacobian.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
+    L.tad_vec_hessians_nnz.argtypes = [ctypes.c_void_p, _i64p]
+    L.tad_vec_eval_with_derivatives.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, _i64p, _ip, _ip, _dp]
+    L.tad_eval_sum_of_squares_with_derivatives.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, _dp, _dp]
+    L.tad_gauss_newton_direction.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double, _dp, _dp, _dp]
     L.tad_newton_direction_reduced_basis.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int64, _ip, _ip, _dp, ctypes.c_double,
                                                      ctypes.c_double, _dp, _dp, _dp]
     L.tad_line_search.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double, _dp, ctypes.c_double, _dp, _dp]
@@ -414,6 +429,113 @@ def debug_scalar_op(op: int, a, b=(0.0, 0.0, 0.0), precision: int = PREC_FP64) -
     if rc != TAD_OK:
         raise TinyADError(rc, L.tad_last_error_message().decode())
     return out
+
+
+class VectorFunction(ScalarFunction):
+    """A vector function r: R^n -> R^m defined by per-element residual functors.
+
+    Mirrors TinyAD::VectorFunction<d, double, Eigen::Index>
+    (include/TinyAD/VectorFunction.hh) for the built-in residual functors
+    (tad_vector_energy in include/tad.h); user functors use the C++ front end.
+    The inherited scalar methods act on the sum of squares f = |r|^2
+    (eval = eval_sum_of_squares, eval_with_gradient gives g = 2 J^T r,
+    newton_solve runs Gauss-Newton with the Armijo line search on f).
+    """
+
+    def add_elements(self, energy: int, handles, params, n_outputs: int):
+        """add_elements<N, M>(range, lambda) for a built-in residual functor."""
+        handles = np.ascontiguousarray(handles, dtype=np.int32)
+        if handles.ndim == 1:
+            handles = handles[:, None]
+        params = _f64(params)
+        if params.ndim == 1:
+            params = params[:, None]
+        n, N = handles.shape
+        self._check(self.L.tad_add_vector_elements(self.h, int(energy), N, int(n_outputs), n, handles.ctypes.data_as(_ip),
+                                                   _d(params), params.shape[1] if n > 0 else int(params.shape[-1])))
+        self._jpattern = None
+
+    @property
+    def n_outputs(self) -> int:
+        return int(self.L.tad_n_outputs(self.h))
+
+    def _jacobian_pattern(self):
+        if getattr(self, "_jpattern", None) is None:
+            nnz = np.zeros(1, np.int64)
+            self._check(self.L.tad_vec_jacobian_nnz(self.h, nnz.ctypes.data_as(_i64p)))
+            m = self.n_outputs
+            outer = np.zeros(m + 1, np.int32)
+            inner = np.zeros(int(nnz[0]), np.int32)
+            self._check(self.L.tad_vec_jacobian_pattern(self.h, outer.ctypes.data_as(_ip), inner.ctypes.data_as(_ip)))
+            self._jpattern = (outer, inner)
+        return self._jpattern
+
+    def _jacobian(self, values):
+        import scipy.sparse as sp
+        outer, inner = self._jacobian_pattern()
+        return sp.csr_matrix((values, inner, outer), shape=(self.n_outputs, self.n_vars))
+
+    def eval_vector(self, x) -> np.ndarray:
+        """VectorFunction::eval(x): the residual vector r."""
+        x = self._x(x)
+        r = np.zeros(self.n_outputs)
+        self._check(self.L.tad_vec_eval(self.h, _d(x), _d(r)))
+        return r
+
+    def eval_sum_of_squares(self, x) -> float:
+        return self.eval(x)
+
+    def eval_with_jacobian(self, x):
+        """(r, J), J the n_outputs x n_vars Jacobian (scipy CSR)."""
+        x = self._x(x)
+        outer, inner = self._jacobian_pattern()
+        r = np.zeros(self.n_outputs)
+        vals = np.zeros(inner.size)
+        self._check(self.L.tad_vec_eval_with_jacobian(self.h, _d(x), _d(r), _d(vals)))
+        return r, self._jacobian(vals)
+
+    def eval_with_derivatives(self, x):
+        """(r, J, [H_i]): the residual Hessians as a list of n_vars x n_vars
+        scipy CSR matrices, one per residual."""
+        import scipy.sparse as sp
+        x = self._x(x)
+        outer, inner = self._jacobian_pattern()
+        m = self.n_outputs
+        nnz = np.zeros(1, np.int64)
+        self._check(self.L.tad_vec_hessians_nnz(self.h, nnz.ctypes.data_as(_i64p)))
+        r = np.zeros(m)
+        vals = np.zeros(inner.size)
+        hp = np.zeros(m + 1, np.int64)
+        hr = np.zeros(int(nnz[0]), np.int32)
+        hc = np.zeros(int(nnz[0]), np.int32)
+        hv = np.zeros(int(nnz[0]))
+        self._check(self.L.tad_vec_eval_with_derivatives(self.h, _d(x), _d(r), _d(vals), hp.ctypes.data_as(_i64p),
+                                                         hr.ctypes.data_as(_ip), hc.ctypes.data_as(_ip), _d(hv)))
+        H = [sp.csr_matrix((hv[hp[i]:hp[i + 1]], (hr[hp[i]:hp[i + 1]], hc[hp[i]:hp[i + 1]])),
+                           shape=(self.n_vars, self.n_vars)) for i in range(m)]
+        return r, self._jacobian(vals), H
+
+    def eval_sum_of_squares_with_derivatives(self, x):
+        """(f, g, r, J) with f = |r|^2, g = 2 J^T r."""
+        x = self._x(x)
+        outer, inner = self._jacobian_pattern()
+        f = np.zeros(1)
+        g = np.zeros(self.n_vars)
+        r = np.zeros(self.n_outputs)
+        vals = np.zeros(inner.size)
+        self._check(self.L.tad_eval_sum_of_squares_with_derivatives(self.h, _d(x), _d(f), _d(g), _d(r), _d(vals)))
+        return float(f[0]), g, r, self._jacobian(vals)
+
+    def gauss_newton_direction(self, x, w_identity: float = 0.0):
+        """gauss_newton_direction(r, J, solver, w) at x: d = -(J^T J + w I)^-1 J^T r.
+        Returns (d, f, g)."""
+        x = self._x(x)
+        d = np.zeros(self.n_vars)
+        g = np.zeros(self.n_vars)
+        f = np.zeros(1)
+        self._check(self.L.tad_gauss_newton_direction(self.h, _d(x), float(w_identity), _d(d), _d(f), _d(g)),
+                    allow=(TAD_ERR_PCG_NOCONV,))
+        return d, float(f[0]), g
 
 
 class Batch:

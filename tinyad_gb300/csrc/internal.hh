@@ -64,6 +64,8 @@ struct Term
     tad_term_eval_fn fn = nullptr;
     void* user = nullptr;
     int64_t elem_off = 0, slot_off = 0, pair_off = 0;
+    int M = 0;                       // vector terms: residuals per element (0: scalar term)
+    int64_t out_off = 0, jac_off = 0, hv_off = 0;   // offsets into the residual buffers
 };
 
 /* device-side scalars of one problem */
@@ -87,6 +89,16 @@ struct DevScalars
 
 struct Problem
 {
+    int kind = 0;                    // 0: empty, 1: scalar terms, 2: vector terms (sum of squares)
+    int64_t n_outputs_total = 0;     // vector problems: residuals
+    int64_t jac_size = 0, hv_size = 0;
+    double* vr = nullptr;            // residuals [n_outputs]
+    double* vJ = nullptr;            // residual gradients, per term [n_elem][M][k]
+    double* vHv = nullptr;           // packed residual Hessians, per term [n_elem][M][k(k+1)/2]
+    int vec_outputs = 0;             // which of vr / vJ / vHv the next evaluation fills (0..3)
+    std::vector<int32_t> jptr_h, jcol_h;   // Jacobian CSR pattern (n_outputs x n_vars)
+    int32_t* jmap = nullptr;         // Jacobian CSR value k -> index into vJ
+
     int d = 0;
     int64_t n_handles = 0, n_vars = 0;
     tad_settings settings{};
@@ -149,6 +161,7 @@ tad_status check_device_error(Problem& P);
 
 // ---- builtin_*.cu: launch a built-in energy term for one evaluation mode
 tad_status launch_builtin(Problem& P, Term& T, const tad_term_eval_args& a);
+tad_status launch_builtin_vec(Problem& P, Term& T, const tad_term_eval_args& a);
 tad_status launch_builtin_tri(Problem& P, Term& T, const tad_term_eval_args& a);
 tad_status launch_builtin_tet(Problem& P, Term& T, const tad_term_eval_args& a);
 tad_status launch_builtin_misc(Problem& P, Term& T, const tad_term_eval_args& a);
@@ -170,6 +183,7 @@ void launch_bsr_to_csr(Problem& P, double* out, int precision);
 void launch_zero(double* p, int64_t n, cudaStream_t s);
 
 // ---- solver.cu
+void add_identity(Problem& P, double w, int precision);   // H += w I (assembled H)
 tad_status pcg_solve(Problem& P, const double* b, double* xsol, double w_identity, int precision,
                      double rel_tol, int max_iters, int* iters_out);
 tad_status line_search_device(Problem& P, double* x, const double* d, double f, double s_max,

@@ -53,6 +53,7 @@ static int builtin_dim_ok(int energy, int d, int N, int n_params)
 
 tad_status launch_builtin(Problem& P, Term& T, const tad_term_eval_args& a)
 {
+    if (T.M > 0) return launch_builtin_vec(P, T, a);
     switch (T.energy)
     {
     case TAD_ENERGY_SYMMETRIC_DIRICHLET_TRI:
@@ -225,13 +226,17 @@ tad_status ensure_finalized(Problem& P)
     if (P.finalized) return TAD_OK;
     if (P.terms.empty()) return fail(TAD_ERR_STATE, "problem has no elements");
     // offsets
-    int64_t eo = 0, so = 0, po = 0;
+    int64_t eo = 0, so = 0, po = 0, oo = 0, jo = 0, ho = 0;
     for (Term& T : P.terms)
     {
         T.elem_off = eo; T.slot_off = so; T.pair_off = po;
         eo += T.n_elem; so += T.n_elem * T.N; po += T.n_elem * (T.N * (T.N + 1) / 2);
+        const int64_t k = (int64_t)P.d * T.N;
+        T.out_off = oo; T.jac_off = jo; T.hv_off = ho;
+        oo += T.n_elem * T.M; jo += T.n_elem * T.M * k; ho += T.n_elem * T.M * (k * (k + 1) / 2);
     }
     P.n_elem_total = eo; P.n_slots_total = so; P.n_pairs_total = po;
+    P.n_outputs_total = oo; P.jac_size = jo; P.hv_size = ho;
     dfree(P.ef); dfree(P.eg); dfree(P.eH);
     TAD_CUDA_TRY(dalloc(&P.ef, (size_t)eo * LS_BATCH));
     TAD_CUDA_TRY(dalloc(&P.eg, (size_t)so * P.d));
@@ -245,7 +250,7 @@ tad_status ensure_finalized(Problem& P)
         TAD_CUDA_TRY(dalloc(&T.rec_d, T.n_elem * T.N));
         tad_term_eval_args a{};
         a.mode = TAD_MODE_RECORD;
-        a.n_elem = T.n_elem; a.valence = T.N; a.var_dim = P.d;
+        a.n_elem = T.n_elem; a.valence = T.N; a.var_dim = P.d; a.n_outputs = T.M;
         a.x_d = P.x; a.record_d = T.rec_d; a.error_d = P.err; a.stream = P.stream;
         const int rc = T.fn(T.user, &a);
         if (rc != 0) return fail(TAD_ERR_ARG, "custom term callback failed while recording");
@@ -290,6 +295,13 @@ tad_status eval_elements(Problem& P, int mode, const double* x, double eps, int 
         a.out_H_d = (char*)P.eH + T.pair_off * P.d * P.d * (precision == TAD_PREC_MIXED ? sizeof(float) : sizeof(double));
         a.error_d = P.err;
         a.stream = P.stream;
+        a.n_outputs = T.M;
+        if (T.M > 0)
+        {
+            a.out_r_d = (P.vec_outputs >= 1 && P.vr) ? P.vr + T.out_off : nullptr;
+            a.out_J_d = (P.vec_outputs >= 2 && P.vJ) ? P.vJ + T.jac_off : nullptr;
+            a.out_Hv_d = (P.vec_outputs >= 3 && P.vHv) ? P.vHv + T.hv_off : nullptr;
+        }
         if (mode == TAD_MODE_LINESEARCH) a.f_row_stride = P.n_elem_total;
         tad_status s = T.energy >= 0 ? launch_builtin(P, T, a)
                                      : (T.fn(T.user, &a) == 0 ? TAD_OK : fail(TAD_ERR_ARG, "custom term failed"));
@@ -412,18 +424,13 @@ TAD_API tad_status tad_problem_set_settings(tad_problem* P, const tad_settings* 
 
 TAD_API int64_t tad_n_vars(const tad_problem* P) { return P ? P->n_vars : 0; }
 
-TAD_API tad_status tad_add_elements(tad_problem* P, int energy, int valence, int64_t n_elem,
-                                    const int32_t* handles_h, const double* params_h, int n_params)
+/* a built-in term: element handles (deduplicated per element into the
+   recorded first-access order) and parameters uploaded once */
+static tad_status add_builtin_term(tad_problem* P, int energy, int valence, int n_outputs, int64_t n_elem,
+                                   const int32_t* handles_h, const double* params_h, int n_params)
 {
-    if (!P) return fail(TAD_ERR_ARG, "NULL problem");
-    if (energy < 0 || energy >= TAD_ENERGY_COUNT_) return fail(TAD_ERR_ARG, "unknown energy");
-    if (valence < 1 || valence > 4) return fail(TAD_ERR_ARG, "valence must be 1..4");
-    if (n_elem < 0 || (n_elem > 0 && !handles_h)) return fail(TAD_ERR_ARG, "bad element array");
-    if (!builtin_dim_ok(energy, P->d, valence, n_params))
-        return fail(TAD_ERR_ARG, "energy not available for this (var_dim, valence, n_params)");
-    if (P->finalized) return fail(TAD_ERR_STATE, "elements must be added before the first evaluation");
     Term T;
-    T.energy = energy; T.N = valence; T.n_elem = n_elem; T.n_params = n_params;
+    T.energy = energy; T.N = valence; T.M = n_outputs; T.n_elem = n_elem; T.n_params = n_params;
     T.vtx_h.assign(handles_h, handles_h + n_elem * valence);
     T.rec_h.resize(n_elem * valence);
     for (int64_t e = 0; e < n_elem; ++e)
@@ -451,13 +458,61 @@ TAD_API tad_status tad_add_elements(tad_problem* P, int energy, int valence, int
     return TAD_OK;
 }
 
+TAD_API tad_status tad_add_elements(tad_problem* P, int energy, int valence, int64_t n_elem,
+                                    const int32_t* handles_h, const double* params_h, int n_params)
+{
+    if (!P) return fail(TAD_ERR_ARG, "NULL problem");
+    if (energy < 0 || energy >= TAD_ENERGY_COUNT_) return fail(TAD_ERR_ARG, "unknown energy");
+    if (valence < 1 || valence > 4) return fail(TAD_ERR_ARG, "valence must be 1..4");
+    if (n_elem < 0 || (n_elem > 0 && !handles_h)) return fail(TAD_ERR_ARG, "bad element array");
+    if (!builtin_dim_ok(energy, P->d, valence, n_params))
+        return fail(TAD_ERR_ARG, "energy not available for this (var_dim, valence, n_params)");
+    if (P->finalized) return fail(TAD_ERR_STATE, "elements must be added before the first evaluation");
+    if (P->kind == 2) return fail(TAD_ERR_STATE, "a problem holds either scalar or vector terms");
+    P->kind = 1;
+    return add_builtin_term(P, energy, valence, 0, n_elem, handles_h, params_h, n_params);
+}
+
+TAD_API tad_status tad_add_vector_elements(tad_problem* P, int energy, int valence, int n_outputs, int64_t n_elem,
+                                           const int32_t* handles_h, const double* params_h, int n_params)
+{
+    if (!P) return fail(TAD_ERR_ARG, "NULL problem");
+    if (n_elem < 0 || (n_elem > 0 && !handles_h)) return fail(TAD_ERR_ARG, "bad element array");
+    const bool ok = (energy == TAD_VEC_SYMMETRIC_DIRICHLET_TRI && P->d == 2 && valence == 3 && n_outputs == 8 && n_params == 5) ||
+                    (energy == TAD_VEC_POSITION && P->d >= 1 && P->d <= 3 && valence == 1 && n_outputs == P->d &&
+                     n_params == P->d + 1);
+    if (!ok) return fail(TAD_ERR_ARG, "vector energy not available for this (var_dim, valence, outputs, n_params)");
+    if (P->finalized) return fail(TAD_ERR_STATE, "elements must be added before the first evaluation");
+    if (P->kind == 1) return fail(TAD_ERR_STATE, "a problem holds either scalar or vector terms");
+    P->kind = 2;
+    return add_builtin_term(P, energy, valence, n_outputs, n_elem, handles_h, params_h, n_params);
+}
+
 TAD_API tad_status tad_add_elements_custom(tad_problem* P, int valence, int64_t n_elem, tad_term_eval_fn fn, void* user)
 {
     if (!P || !fn) return fail(TAD_ERR_ARG, "NULL argument");
     if (valence < 1 || valence > 64) return fail(TAD_ERR_ARG, "valence must be 1..64");
     if (P->finalized) return fail(TAD_ERR_STATE, "elements must be added before the first evaluation");
+    if (P->kind == 2) return fail(TAD_ERR_STATE, "a problem holds either scalar or vector terms");
+    P->kind = 1;
     Term T;
     T.energy = -1; T.N = valence; T.n_elem = n_elem; T.fn = fn; T.user = user;
+    P->terms.push_back(std::move(T));
+    return TAD_OK;
+}
+
+TAD_API tad_status tad_add_vector_elements_custom(tad_problem* P, int valence, int n_outputs, int64_t n_elem,
+                                                  tad_term_eval_fn fn, void* user)
+{
+    if (!P || !fn) return fail(TAD_ERR_ARG, "NULL argument");
+    if (valence < 1 || valence > 64) return fail(TAD_ERR_ARG, "valence must be 1..64");
+    if (n_outputs < 1) return fail(TAD_ERR_ARG, "outputs per element must be positive");
+    if (n_elem < 0) return fail(TAD_ERR_ARG, "bad element count");
+    if (P->finalized) return fail(TAD_ERR_STATE, "elements must be added before the first evaluation");
+    if (P->kind == 1) return fail(TAD_ERR_STATE, "a problem holds either scalar or vector terms");
+    P->kind = 2;
+    Term T;
+    T.energy = -1; T.N = valence; T.M = n_outputs; T.n_elem = n_elem; T.fn = fn; T.user = user;
     P->terms.push_back(std::move(T));
     return TAD_OK;
 }

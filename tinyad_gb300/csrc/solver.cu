@@ -551,6 +551,34 @@ static tad_status pcg_dispatch(Problem& P, const double* b, double* xsol, int pr
     return st == TAD_ERR_PCG_NOCONV ? TAD_OK : st;
 }
 
+/* H += w I on the assembled diagonal blocks */
+template <int d, typename T>
+__global__ void k_add_diag(int64_t nh, const int32_t* __restrict__ diag, T* __restrict__ H, double w)
+{
+    GRID_STRIDE(u, nh)
+    {
+        const int32_t b = diag[u];
+        if (b < 0) continue;
+#pragma unroll
+        for (int i = 0; i < d; ++i) H[(int64_t)b * d * d + i * d + i] += (T)w;
+    }
+}
+
+void add_identity(Problem& P, double w, int precision)
+{
+    const bool fp32 = precision == TAD_PREC_MIXED;
+    switch (P.d)
+    {
+    case 1: fp32 ? k_add_diag<1, float><<<RED_BLOCKS, RED_THREADS, 0, P.stream>>>(P.n_handles, P.diag, (float*)P.H, w)
+                 : k_add_diag<1, double><<<RED_BLOCKS, RED_THREADS, 0, P.stream>>>(P.n_handles, P.diag, (double*)P.H, w); break;
+    case 2: fp32 ? k_add_diag<2, float><<<RED_BLOCKS, RED_THREADS, 0, P.stream>>>(P.n_handles, P.diag, (float*)P.H, w)
+                 : k_add_diag<2, double><<<RED_BLOCKS, RED_THREADS, 0, P.stream>>>(P.n_handles, P.diag, (double*)P.H, w); break;
+    default: fp32 ? k_add_diag<3, float><<<RED_BLOCKS, RED_THREADS, 0, P.stream>>>(P.n_handles, P.diag, (float*)P.H, w)
+                  : k_add_diag<3, double><<<RED_BLOCKS, RED_THREADS, 0, P.stream>>>(P.n_handles, P.diag, (double*)P.H, w); break;
+    }
+    P.n_launches += 1;
+}
+
 tad_status pcg_solve(Problem& P, const double* b, double* xsol, double w_identity, int precision, double rel_tol,
                      int max_iters, int* iters_out)
 {
@@ -691,13 +719,14 @@ TAD_API tad_status tad_newton_direction(tad_problem* P, const double* x_h, int p
                                         double* d_h, double* f, double* g_h)
 {
     if (!P || !x_h || !d_h) return fail(TAD_ERR_ARG, "NULL argument");
-    if (w != 0.0) return fail(TAD_ERR_ARG, "w_identity != 0 is not supported");
+    if (!(w >= 0.0) || !std::isfinite(w)) return fail(TAD_ERR_ARG, "w_identity must be finite and non-negative");
     TAD_CUDA_TRY(cudaSetDevice(P->device));
     tad_status s = ensure_finalized(*P);
     if (s != TAD_OK) return s;
     TAD_CUDA_TRY(cudaMemcpyAsync(P->x, x_h, P->n_vars * 8, cudaMemcpyHostToDevice, P->stream));
     s = eval_full(*P, P->x, projected ? TAD_MODE_HESSIAN_PROJ : TAD_MODE_HESSIAN, eps, P->precision);
     if (s != TAD_OK) return s;
+    if (w != 0.0) add_identity(*P, w, P->precision);   // H + w I (NewtonDirection.hh:32)
     k_neg<<<RED_BLOCKS, RED_THREADS, 0, P->stream>>>(P->n_vars, P->g, P->rhs);
     s = check_device_error(*P);
     if (s != TAD_OK) return s;

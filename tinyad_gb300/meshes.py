@@ -35,6 +35,9 @@ TAD_ENERGY_SYMMETRIC_DIRICHLET_TET = 1
 TAD_ENERGY_POSITION_PENALTY = 2
 TAD_ENERGY_QUADRATIC = 3
 TAD_ENERGY_DIRICHLET_TRI = 4
+# residual functors of vector terms (tad_vector_energy)
+TAD_VEC_SYMMETRIC_DIRICHLET_TRI = 0
+TAD_VEC_POSITION = 1
 
 
 @dataclass
@@ -327,4 +330,20 @@ def disk_batch(n_meshes: int = 256, lo: int = 1000, hi: int = 50000, seed: int =
     for i, t in enumerate(targets):
         grid = max(8, int(round(1 + math.sqrt(2.0 * t / math.pi))))
         out.append(disk_param(grid, seed=seed * 100003 + i + 1, name=f"batch{i}"))
+    return out
+
+
+def residual_terms(w: Workload) -> list:
+    """The residual form of a workload made of symmetric Dirichlet triangle
+    and position penalty terms: (vector energy, handles, params, outputs) per
+    term, with the same parameters, so that the sum of squares of the
+    residuals equals the workload's energy (tests/GaussNewtonTest.cc:33-74)."""
+    out = []
+    for t in w.terms:
+        if t.energy == TAD_ENERGY_SYMMETRIC_DIRICHLET_TRI:
+            out.append((TAD_VEC_SYMMETRIC_DIRICHLET_TRI, t.handles, t.params, 8))
+        elif t.energy == TAD_ENERGY_POSITION_PENALTY:
+            out.append((TAD_VEC_POSITION, t.handles, t.params, w.var_dim))
+        else:
+            raise ValueError(f"no residual form for energy {t.energy}")
     return out
