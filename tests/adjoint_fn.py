@@ -13,12 +13,7 @@ from tinyad_gb300 import meshes
 
 
 def solve_min(w, x0, newton_iters=30, full_steps=2, tol=1e-13):
-    fn = tad.ScalarFunction.from_workload(w, pcg_rel_tol=tol, pcg_max_iters=20000)
-    x, _ = fn.newton_solve(x0, newton_iters)
-    for _ in range(full_steps):
-        d, f, g = fn.newton_direction(x, projected=False)
-        x = x + d
-    return x, fn
+    return tad.solve_minimiser(w, x0, newton_iters, full_steps, tol)
 
 
 class RestShapeLoss(torch.autograd.Function):

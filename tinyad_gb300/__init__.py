@@ -431,6 +431,19 @@ def debug_scalar_op(op: int, a, b=(0.0, 0.0, 0.0), precision: int = PREC_FP64) -
     return out
 
 
+def solve_minimiser(w, x0, newton_iters: int = 30, full_steps: int = 2, tol: float = 1e-13, max_iters: int = 20000):
+    """x* = argmin E(x) for workload w from x0 on the device: Projected-Newton
+    iterations, then full Newton steps on the exact Hessian (quadratic
+    convergence to the minimiser the adjoint differentiates).  Returns
+    (x*, the ScalarFunction)."""
+    fn = ScalarFunction.from_workload(w, pcg_rel_tol=tol, pcg_max_iters=max_iters)
+    x, _ = fn.newton_solve(x0, newton_iters)
+    for _ in range(full_steps):
+        d, f, g = fn.newton_direction(x, projected=False)
+        x = x + d
+    return x, fn
+
+
 class VectorFunction(ScalarFunction):
     """A vector function r: R^n -> R^m defined by per-element residual functors.
 
