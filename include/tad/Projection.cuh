@@ -66,6 +66,7 @@ template <> struct JacobiSweeps<float> { static constexpr int value = 8; };
 template <typename T>
 TAD_HD void jacobi_angle(T app, T aqq, T apq, T& t, T& c)
 {
+    if (apq == T(0)) { t = T(0); c = T(1); return; }
     const T theta = (aqq - app) / (T(2) * apq);
     t = (theta >= T(0) ? T(1) : T(-1)) / (tad_abs(theta) + tad_sqrt(theta * theta + T(1)));
     c = T(1) / tad_sqrt(t * t + T(1));
@@ -114,7 +115,8 @@ TAD_HD void jacobi_eigen_packed(T* A, T* V)
             for (int q = p + 1; q < k; ++q)
             {
                 const T apq = A[packed_index(p, q, k)];
-                if (apq == T(0)) continue;
+                // FP32: no branch -- the fast angle maps a_pq = 0 to the identity rotation
+                if (sizeof(T) == 8 && apq == T(0)) continue;
                 const T app = A[packed_index(p, p, k)], aqq = A[packed_index(q, q, k)];
                 T t, c;
                 jacobi_angle(app, aqq, apq, t, c);

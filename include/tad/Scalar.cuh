@@ -106,6 +106,36 @@ TAD_HD DoubleFloat operator*(DoubleFloat a, DoubleFloat b)
     return df_quick_two_sum(p, e);
 }
 TAD_HD DoubleFloat& operator+=(DoubleFloat& a, DoubleFloat b) { a = a + b; return a; }
+
+/* x y + z w with one renormalisation: both Dekker products through FMA,
+   Knuth's two-sum of the high parts, the cross terms and rounding errors
+   gathered in the low part (the product and quotient rules of the gradient) */
+TAD_HD DoubleFloat df_dot2(DoubleFloat x, DoubleFloat y, DoubleFloat z, DoubleFloat w)
+{
+#if defined(__CUDA_ARCH__)
+#define TAD_DF_FMA __fmaf_rn
+#else
+#define TAD_DF_FMA std::fma
+#endif
+    const float p1 = x.hi * y.hi, p2 = z.hi * w.hi;
+    const float e1 = TAD_DF_FMA(x.hi, y.hi, -p1), e2 = TAD_DF_FMA(z.hi, w.hi, -p2);
+    const float s = p1 + p2;
+    const float v = s - p1;
+    float lo = ((p1 - (s - v)) + (p2 - v)) + (e1 + e2);
+    lo = TAD_DF_FMA(x.hi, y.lo, lo);
+    lo = TAD_DF_FMA(x.lo, y.hi, lo);
+    lo = TAD_DF_FMA(z.hi, w.lo, lo);
+    lo = TAD_DF_FMA(z.lo, w.hi, lo);
+#undef TAD_DF_FMA
+    return df_quick_two_sum(s, lo);
+}
+/* x y + z w in the gradient type (fused for the double-float gradient) */
+template <typename G> TAD_HD G grad_dot2(const G& x, const G& y, const G& z, const G& w) { return x * y + z * w; }
+template <> TAD_HD DoubleFloat grad_dot2<DoubleFloat>(const DoubleFloat& x, const DoubleFloat& y, const DoubleFloat& z,
+                                                      const DoubleFloat& w)
+{
+    return df_dot2(x, y, z, w);
+}
 TAD_HD bool isfinite(DoubleFloat a) { using std::isfinite; return isfinite(a.hi) && isfinite(a.lo); }
 
 /* Value channel of the mixed-precision scalar: the unevaluated sum hi + lo of
@@ -559,7 +589,7 @@ TAD_TPL TAD_HD TAD_S operator*(const TAD_S& a, const TAD_S& b)
     r.val = a.val * b.val;
     const G avg = G(a.val), bvg = G(b.val);
 #pragma unroll
-    for (int i = 0; i < K; ++i) r.grad[i] = bvg * a.grad[i] + avg * b.grad[i];
+    for (int i = 0; i < K; ++i) r.grad[i] = grad_dot2(bvg, a.grad[i], avg, b.grad[i]);
     if (H)
     {
         const T av = T(a.val), bv = T(b.val);
@@ -598,8 +628,18 @@ TAD_TPL TAD_HD TAD_S operator/(const TAD_S& a, const TAD_S& b)
     const V ibv = V(1) / b.val;
     r.val = a.val * ibv;
     const G ibg = G(ibv), rvg = G(r.val);
+    if constexpr (std::is_same<G, DoubleFloat>::value)
+    {
+        // (ga - r gb) / b as one fused x y + z w per entry
+        const G nrib = -(rvg * ibg);
 #pragma unroll
-    for (int i = 0; i < K; ++i) r.grad[i] = (a.grad[i] - rvg * b.grad[i]) * ibg;
+        for (int i = 0; i < K; ++i) r.grad[i] = df_dot2(ibg, a.grad[i], nrib, b.grad[i]);
+    }
+    else
+    {
+#pragma unroll
+        for (int i = 0; i < K; ++i) r.grad[i] = (a.grad[i] - rvg * b.grad[i]) * ibg;
+    }
     if (H)
     {
         const T ib = T(ibv), rv = T(r.val);
