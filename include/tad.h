@@ -130,6 +130,12 @@ typedef struct tad_settings {
                                  gradient at the first Newton iteration after
                                  tad_problem_create / tad_problem_set_settings */
     int verbose;
+    int preconditioner;       /* 0 = block Jacobi; 1 (default) = block Jacobi, and an
+                                 FP64 solve whose residual is still more than 4x
+                                 above its target after 9 iterations restarts with
+                                 conjugate gradients preconditioned by an
+                                 aggregation-AMG V-cycle (FP32 solves of mixed
+                                 precision keep block Jacobi) */
 } tad_settings;
 
 typedef struct tad_problem tad_problem;

@@ -46,7 +46,7 @@ class Settings(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("pcg_max_iters", ctypes.c_int), ("pcg_rel_tol", ctypes.c_double),
                 ("refine_max_iters", ctypes.c_int), ("refine_rel_tol", ctypes.c_double),
                 ("ls_max_iters", ctypes.c_int), ("ls_shrink", ctypes.c_double), ("ls_armijo", ctypes.c_double),
-                ("forcing", ctypes.c_int), ("verbose", ctypes.c_int)]
+                ("forcing", ctypes.c_int), ("verbose", ctypes.c_int), ("preconditioner", ctypes.c_int)]
 
 
 class TinyADError(RuntimeError):

@@ -87,8 +87,25 @@ struct DevScalars
     double gg;           // g.g
 };
 
+/* one level of the AMG hierarchy (amg.cu); level 0 borrows the problem's
+   pattern and values */
+struct AmgLevel
+{
+    int64_t n = 0, nb = 0;
+    int32_t *bptr = nullptr, *bcol = nullptr, *diag = nullptr;
+    int32_t *agg = nullptr;                  // rows of the level above -> rows here
+    int32_t *aptr = nullptr, *aidx = nullptr;
+    int32_t *cptr = nullptr, *cidx = nullptr;
+    void *A = nullptr, *dinv = nullptr;      // values / inverted diagonal blocks (PCG precision)
+    void *r = nullptr, *z = nullptr, *w = nullptr, *t = nullptr;
+};
+
 struct Problem
 {
+    std::vector<AmgLevel> amg;       // aggregation-AMG hierarchy, built when first needed
+    int64_t amg_solves = 0;          // solves that used it (statistics)
+    double* amg_omega = nullptr;     // device: per-level smoother damping (+ 2 scratch norms)
+
     int kind = 0;                    // 0: empty, 1: scalar terms, 2: vector terms (sum of squares)
     int64_t n_outputs_total = 0;     // vector problems: residuals
     int64_t jac_size = 0, hv_size = 0;
@@ -142,6 +159,10 @@ struct Problem
 
     // captured PCG iteration graphs (chunk of iterations)
     cudaGraphExec_t pcg_graph = nullptr;
+    cudaGraphExec_t amg_graph = nullptr;     // chunk of AMG-preconditioned CG iterations
+    int amg_graph_prec = -1;
+    const void* amg_graph_x = nullptr;
+    int64_t amg_graph_launches = 0;          // kernels in one replay of amg_graph
     int pcg_graph_chunk = 0;
     int pcg_graph_prec = -1;
     const void* pcg_graph_x = nullptr;
@@ -184,6 +205,10 @@ void launch_zero(double* p, int64_t n, cudaStream_t s);
 
 // ---- solver.cu
 void add_identity(Problem& P, double w, int precision);   // H += w I (assembled H)
+tad_status amg_prepare(Problem& P, int precision);        // hierarchy (lazily) + values for the current H
+void amg_vcycle(Problem& P, int precision, const void* r, void* z);   // z = V-cycle(r) on P.stream
+void amg_free(Problem& P);
+int amg_levels(const Problem& P);
 tad_status pcg_solve(Problem& P, const double* b, double* xsol, double w_identity, int precision,
                      double rel_tol, int max_iters, int* iters_out);
 tad_status line_search_device(Problem& P, double* x, const double* d, double f, double s_max,

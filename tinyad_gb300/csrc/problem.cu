@@ -354,6 +354,7 @@ TAD_API void tad_settings_default(tad_settings* s)
     s->ls_armijo = 1e-4;
     s->forcing = 0;
     s->verbose = 0;
+    s->preconditioner = 1;
 }
 
 TAD_API const char* tad_last_error_message(void) { return g_last_error.c_str(); }
@@ -407,6 +408,8 @@ TAD_API tad_status tad_problem_destroy(tad_problem* P)
     if (P->hs) cudaFreeHost(P->hs);
     if (P->err_h) cudaFreeHost(P->err_h);
     if (P->pcg_graph) cudaGraphExecDestroy(P->pcg_graph);
+    if (P->amg_graph) cudaGraphExecDestroy(P->amg_graph);
+    amg_free(*P);
     for (auto& e : P->ev) if (e) cudaEventDestroy(e);
     if (P->stream) cudaStreamDestroy(P->stream);
     delete P;

@@ -36,66 +36,9 @@
 
 #include "internal.hh"
 #include "grid_reduce.cuh"
+#include "bsr_kernels.cuh"
 
 namespace tadlib {
-
-/* ---- block-Jacobi preconditioner: invert (H_uu + w I) ------------------- */
-template <int d, typename T>
-__global__ void k_diag_inv(int64_t nh, const int32_t* __restrict__ diag, const T* __restrict__ H, double w, T* __restrict__ dinv)
-{
-    GRID_STRIDE(u, nh)
-    {
-        // in the PCG's precision: FP32 blocks are inverted in FP32 (no FP64
-        // instructions in the mixed path)
-        T A[d * d];
-        const int32_t b = diag[u];
-#pragma unroll
-        for (int i = 0; i < d * d; ++i) A[i] = b >= 0 ? H[(int64_t)b * d * d + i] : T(0);
-#pragma unroll
-        for (int i = 0; i < d; ++i) A[i * d + i] += (T)w;
-        T I[d * d];
-        T det;
-        if (d == 1) { det = A[0]; I[0] = T(1) / A[0]; }
-        else if (d == 2)
-        {
-            det = A[0] * A[3] - A[1] * A[2];
-            const T id = T(1) / det;
-            I[0] = A[3] * id; I[1] = -A[1] * id; I[2] = -A[2] * id; I[3] = A[0] * id;
-        }
-        else
-        {
-            const T c00 = A[4] * A[8] - A[5] * A[7], c01 = A[5] * A[6] - A[3] * A[8], c02 = A[3] * A[7] - A[4] * A[6];
-            det = A[0] * c00 + A[1] * c01 + A[2] * c02;
-            const T id = T(1) / det;
-            I[0] = c00 * id; I[3] = c01 * id; I[6] = c02 * id;
-            I[1] = (A[2] * A[7] - A[1] * A[8]) * id; I[4] = (A[0] * A[8] - A[2] * A[6]) * id; I[7] = (A[1] * A[6] - A[0] * A[7]) * id;
-            I[2] = (A[1] * A[5] - A[2] * A[4]) * id; I[5] = (A[2] * A[3] - A[0] * A[5]) * id; I[8] = (A[0] * A[4] - A[1] * A[3]) * id;
-        }
-        const bool ok = det > T(0) && isfinite(det);
-#pragma unroll
-        for (int i = 0; i < d; ++i)
-#pragma unroll
-            for (int j = 0; j < d; ++j)
-            {
-                T v = I[i * d + j];
-                if (!ok) v = (i == j && A[i * d + i] > T(0)) ? T(1) / A[i * d + i] : (i == j ? T(1) : T(0));
-                dinv[u * d * d + i * d + j] = v;
-            }
-    }
-}
-
-template <int d, typename T>
-__device__ __forceinline__ void apply_dinv(const T* __restrict__ dinv, int64_t u, const T (&r)[d], T (&z)[d])
-{
-#pragma unroll
-    for (int i = 0; i < d; ++i)
-    {
-        T acc = T(0);
-#pragma unroll
-        for (int j = 0; j < d; ++j) acc += dinv[u * d * d + i * d + j] * r[j];
-        z[i] = acc;
-    }
-}
 
 /* x = 0, r = b, z = M^-1 r, p = Ap = 0, beta = 0 (the first fused SpMV then
    forms p = z, Ap = A z); rz = r.z, bb = b.b */
@@ -443,12 +386,114 @@ __global__ void k_axpy_ds(int64_t n, double* __restrict__ x, const double* __res
 /* ------------------------------------------------------------------------ */
 static tad_status fail(tad_status s, const std::string& m) { set_error(m); return s; }
 
+/* AMG path, after the V-cycle has produced z: x += alpha p, r -= alpha Ap and
+   r.r; the last block counts the iteration and sets the stop flag */
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_pcg_update_nopc(int64_t n, T* x, T* r, const T* __restrict__ p,
+                                                                 const T* __restrict__ Ap, double* partials, unsigned* counter,
+                                                                 DevScalars* ds)
+{
+    if (*(volatile int32_t*)&ds->done) return;
+    const T alpha = (T)ds->alpha;
+    T part = T(0);
+    GRID_STRIDE(i, n)
+    {
+        x[i] += alpha * p[i];
+        const T ri = r[i] - alpha * Ap[i];
+        r[i] = ri;
+        part += ri * ri;
+    }
+    double v[1] = {(double)part}, tot[1];
+    if (!grid_sum<1>(v, partials, counter, tot)) return;
+    if (threadIdx.x == 0)
+    {
+        ds->rr = tot[0];
+        ds->iters += 1;
+        if (tot[0] <= ds->tol2 || ds->iters >= ds->max_iters || !isfinite(tot[0])) ds->done = 1;
+    }
+}
+
+/* r.z after the V-cycle: beta = r.z / rz_old, rz = r.z (first: beta = 0) */
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_pcg_rz(int64_t n, const T* __restrict__ r, const T* __restrict__ z,
+                                                        double* partials, unsigned* counter, DevScalars* ds, int first)
+{
+    if (*(volatile int32_t*)&ds->done) return;
+    T part = T(0);
+    GRID_STRIDE(i, n) part += r[i] * z[i];
+    double v[1] = {(double)part}, tot[1];
+    if (!grid_sum<1>(v, partials, counter, tot)) return;
+    if (threadIdx.x == 0)
+    {
+        if (!(tot[0] > 0.0) || !isfinite(tot[0])) { ds->breakdown = 1; ds->done = 1; return; }
+        ds->beta = first ? 0.0 : tot[0] / ds->rz;
+        ds->rz = tot[0];
+    }
+}
+
+/* Conjugate gradients preconditioned by one AMG V-cycle, from x = 0. */
+template <int d, typename T>
+static tad_status pcg_core_amg(Problem& P, const double* b, T* xs, double rel_tol, int max_iters, int* iters_out,
+                               T* r, T* z, T* p, T* Ap, int prec)
+{
+    tad_status st = amg_prepare(P, prec);
+    if (st != TAD_OK) return st;
+    ++P.amg_solves;
+    const T* H = (const T*)P.H;
+    const int64_t nh = P.n_handles, n = P.n_vars;
+    cudaStream_t s = P.stream;
+    // x = 0, r = b, p = Ap = 0, tolerance and counters (its z = D^-1 r is replaced)
+    k_pcg_init<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, b, xs, r, z, p, Ap, (const T*)P.amg[0].dinv, P.partials,
+                                                        P.counters, P.ds, rel_tol, max_iters);
+    amg_vcycle(P, prec, r, z);
+    k_pcg_rz<T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, r, z, P.partials, P.counters + 9, P.ds, 1);
+    P.n_launches += 2;
+    TAD_CUDA_TRY(cudaGetLastError());
+    constexpr int CHUNK = 4;
+    auto launch_iteration = [&]() {
+        k_pcg_spmv_fused<d, T, SpmvGroup<d>::value><<<PCG_BLOCKS, RED_THREADS, 0, s>>>(nh, P.bptr, P.bcol, H, z, p, Ap,
+                                                                                  P.partials, P.counters + 1, P.ds);
+        k_pcg_update_nopc<T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, xs, r, p, Ap, P.partials, P.counters + 2, P.ds);
+        amg_vcycle(P, prec, r, z);
+        k_pcg_rz<T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, r, z, P.partials, P.counters + 9, P.ds, 0);
+    };
+    if (P.amg_graph == nullptr || P.amg_graph_prec != prec || P.amg_graph_x != (const void*)xs)
+    {
+        if (P.amg_graph) { cudaGraphExecDestroy(P.amg_graph); P.amg_graph = nullptr; }
+        const int64_t l0 = P.n_launches;
+        cudaGraph_t graph;
+        TAD_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        for (int it = 0; it < CHUNK; ++it) launch_iteration();
+        TAD_CUDA_TRY(cudaStreamEndCapture(s, &graph));
+        TAD_CUDA_TRY(cudaGraphInstantiate(&P.amg_graph, graph, 0));
+        cudaGraphDestroy(graph);
+        P.amg_graph_prec = prec;
+        P.amg_graph_x = (const void*)xs;
+        P.amg_graph_launches = P.n_launches - l0 + 3 * CHUNK;
+        P.n_launches = l0;
+    }
+    int replays = 1;
+    for (;;)
+    {
+        for (int k = 0; k < replays; ++k) TAD_CUDA_TRY(cudaGraphLaunch(P.amg_graph, s));
+        P.n_launches += P.amg_graph_launches * replays;
+        TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
+        TAD_CUDA_TRY(cudaStreamSynchronize(s));
+        if (P.hs->done) break;
+        replays = std::min(4, 2 * replays);
+    }
+    if (iters_out) *iters_out += P.hs->iters;
+    if (P.hs->breakdown) return TAD_ERR_PCG_NOCONV;
+    if (!(P.hs->rr <= P.hs->tol2)) return TAD_ERR_PCG_NOCONV;
+    return TAD_OK;
+}
+
 template <int d, typename T>
 static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double rel_tol, int max_iters, int* iters_out,
                            T* r, T* z, T* p, T* Ap, T* dinv, int prec)
 {
     const T* H = (const T*)P.H;
-    const int64_t nh = P.n_handles, n = P.n_vars;
+    const int64_t nh = P.n_handles;
     cudaStream_t s = P.stream;
     k_diag_inv<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, P.diag, H, w, dinv);
     k_pcg_init<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, b, xs, r, z, p, Ap, dinv, P.partials, P.counters, P.ds, rel_tol, max_iters);
@@ -457,8 +502,15 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
     // The first iteration is launched directly and checked at once (early
     // Newton iterations converge in one); after that, CHUNK iterations
     // captured once per (precision, solution buffer) are replayed, with the
-    // replays between host checks doubling up to 8.
+    // replays between host checks doubling up to 8.  With the AMG policy,
+    // an FP64 solve still far from its tolerance after the first 1 + CHUNK
+    // iterations restarts with the AMG-preconditioned CG (w must be 0 there:
+    // the hierarchy is built from H itself).  FP32 solves (mixed precision)
+    // stay on block Jacobi: FP32 V-cycles on nearly singular systems (the
+    // eps-regularised rigid motions of an unconstrained mesh) did not
+    // converge reliably.
     constexpr int CHUNK = 8;
+    constexpr double AMG_SWITCH_RATIO = 16.0;
     auto launch_iteration = [&]() {
         k_pcg_spmv_fused<d, T, SpmvGroup<d>::value><<<PCG_BLOCKS, RED_THREADS, 0, s>>>(nh, P.bptr, P.bcol, H, z, p, Ap,
                                                                                   P.partials, P.counters + 1, P.ds);
@@ -494,6 +546,17 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
         TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
         TAD_CUDA_TRY(cudaStreamSynchronize(s));
         if (P.hs->done) break;
+        if (sizeof(T) == 8 && replays == 1 && P.settings.preconditioner == 1 && w == 0.0 &&
+            P.hs->rr > AMG_SWITCH_RATIO * P.hs->tol2)
+        {
+            // still more than a factor sqrt(AMG_SWITCH_RATIO) above the target
+            // after 1 + CHUNK iterations: block Jacobi's fast start (the high
+            // frequencies) is over, what is left converges at its slow rate
+            const int it = P.hs->iters;
+            if (iters_out) *iters_out = it;
+            const int left = std::max(1, max_iters - it);
+            return pcg_core_amg<d, T>(P, b, xs, rel_tol, left, iters_out, r, z, p, Ap, prec);
+        }
         replays = replays == 0 ? 1 : std::min(8, 2 * replays);
     }
     if (iters_out) *iters_out = P.hs->iters;
