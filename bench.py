@@ -616,6 +616,43 @@ def main():
         solve = {"f_converged_fp64": h64[-1][1], "f_converged_mixed": hmx[-1][1],
                  "final_energy_rel_err_mixed_vs_fp64": abs(hmx[-1][1] - h64[-1][1]) / abs(h64[-1][1]),
                  "to_1e-8_fp64": reach(h64), "to_1e-8_mixed": reach(hmx)}
+        # error of the mixed path against FP64 at the post-warm-up state: f, g
+        # and H of the evaluation, and the Newton step with both linear solves
+        # taken to 1e-8 (so the difference is the precision, not the PCG tolerance)
+        xw = x_warm.cpu().numpy()
+        tight = dict(settings, pcg_rel_tol=1e-8, pcg_max_iters=50000, refine_max_iters=8, refine_rel_tol=1e-8)
+        e64 = tad.ScalarFunction.from_workload(w, precision=tad.PREC_FP64, **tight)
+        emx = tad.ScalarFunction.from_workload(w, precision=tad.PREC_MIXED, **tight)
+        f64, g64, H64 = e64.eval_with_hessian_proj(xw)
+        fmx, gmx, Hmx = emx.eval_with_hessian_proj(xw)
+        d64, _, _ = e64.newton_direction(xw)
+        dmx, _, _ = emx.newton_direction(xw)
+        # the energy is invariant under rigid motions of the planar layout (2
+        # translations, 1 rotation): the steps are compared with those
+        # (eps-regularised null) components removed, and by the decrease g.d
+        # they predict, which the null components do not change
+        def strip_rigid(v, xx):
+            if w.var_dim != 2:
+                return v
+            uv = xx.reshape(-1, 2)
+            c = uv - uv.mean(axis=0)
+            basis = [np.tile([1.0, 0.0], len(uv)), np.tile([0.0, 1.0], len(uv)), np.column_stack([-c[:, 1], c[:, 0]]).reshape(-1)]
+            q = []
+            for b_ in basis:
+                for qq in q:
+                    b_ = b_ - (qq @ b_) * qq
+                q.append(b_ / np.linalg.norm(b_))
+            for qq in q:
+                v = v - (qq @ v) * qq
+            return v
+        s64, smx = strip_rigid(d64, xw), strip_rigid(dmx, xw)
+        solve["errors_mixed_vs_fp64_at_step_W"] = {
+            "f": abs(fmx - f64) / abs(f64),
+            "g": float(np.linalg.norm(gmx - g64) / np.linalg.norm(g64)),
+            "H_frobenius": float(np.linalg.norm((Hmx - H64).data) / np.linalg.norm(H64.data)),
+            "newton_step_without_rigid_modes": float(np.linalg.norm(smx - s64) / np.linalg.norm(s64)),
+            "predicted_decrease_g_dot_d": float(abs(g64 @ dmx - g64 @ d64) / abs(g64 @ d64))}
+        del e64, emx
 
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:

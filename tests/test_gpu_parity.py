@@ -339,3 +339,43 @@ def test_amg_preconditioned_solve(tad, precision):
     assert rel_err(H @ d_a, -g) <= 1e-8
     assert rel_err(d_a, d_j) <= 1e-6
     assert it_a * 3 < it_j, (it_a, it_j)
+
+
+def test_mixed_newton_step(tad):
+    """The mixed path's Newton step against FP64's at the same state, both
+    linear solves to 1e-10: the difference is the precision of the FP32
+    Hessian (and projection), a few 1e-6 relative here."""
+    w = meshes.disk_param_pinned(32, seed=6)
+    xs, _ = tad.solve_minimiser(w, w.x0)
+    x = xs + np.random.default_rng(8).normal(scale=1e-3, size=xs.size)
+    kw = dict(pcg_rel_tol=1e-10, pcg_max_iters=20000, refine_max_iters=8, refine_rel_tol=1e-10)
+    f64 = tad.ScalarFunction.from_workload(w, precision=tad.PREC_FP64, **kw)
+    fmx = tad.ScalarFunction.from_workload(w, precision=tad.PREC_MIXED, **kw)
+    d64, _, g = f64.newton_direction(x)
+    dmx, _, _ = fmx.newton_direction(x)
+    _, _, H = f64.eval_with_hessian_proj(x)
+    assert rel_err(H @ d64, -g) <= 1e-9
+    assert rel_err(dmx, d64) <= 1e-4
+
+
+def test_mixed_tight_solve_unconstrained(tad, oracle):
+    """A tight mixed-precision solve on an unconstrained disk (the eps-scaled
+    rigid motions make H nearly singular, where FP32 CG stalls): the
+    iterative refinement finishes in FP64 on the FP32 Hessian, so the step
+    solves the FP32-evaluated system to the tolerance and stays within the
+    Hessian's FP32 rounding of the FP64 step."""
+    w = meshes.disk_param(48, seed=13)
+    kw = dict(pcg_rel_tol=1e-8, pcg_max_iters=50000, refine_max_iters=8, refine_rel_tol=1e-8)
+    f64 = tad.ScalarFunction.from_workload(w, precision=tad.PREC_FP64, **kw)
+    fmx = tad.ScalarFunction.from_workload(w, precision=tad.PREC_MIXED, **kw)
+    x, _ = f64.newton_solve(w.x0, 6)
+    d64, _, g = f64.newton_direction(x)
+    dmx, _, gm = fmx.newton_direction(x)
+    _, _, Hm = fmx.eval_with_hessian_proj(x)
+    assert rel_err(Hm @ dmx, -gm) <= 1e-7
+    # the rigid translations are a null space of both systems: compare the steps
+    # after removing their translation components
+    def strip(v):
+        v = v.reshape(-1, 2)
+        return (v - v.mean(axis=0)).reshape(-1)
+    assert rel_err(strip(dmx), strip(d64)) <= 1e-3

@@ -160,6 +160,10 @@ struct Problem
     // captured PCG iteration graphs (chunk of iterations)
     cudaGraphExec_t pcg_graph = nullptr;
     cudaGraphExec_t amg_graph = nullptr;     // chunk of AMG-preconditioned CG iterations
+    const void* pcg_graph_H = nullptr;       // the Hessian buffer each graph reads
+    const void* amg_graph_H = nullptr;
+    void* Hd = nullptr;                      // FP64 copy of an FP32 Hessian (tight mixed solves)
+    double* corr = nullptr;                  // FP64 correction of a tight mixed solve
     int amg_graph_prec = -1;
     const void* amg_graph_x = nullptr;
     int64_t amg_graph_launches = 0;          // kernels in one replay of amg_graph

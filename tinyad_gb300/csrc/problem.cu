@@ -409,6 +409,8 @@ TAD_API tad_status tad_problem_destroy(tad_problem* P)
     if (P->err_h) cudaFreeHost(P->err_h);
     if (P->pcg_graph) cudaGraphExecDestroy(P->pcg_graph);
     if (P->amg_graph) cudaGraphExecDestroy(P->amg_graph);
+    if (P->Hd) cudaFree(P->Hd);
+    if (P->corr) cudaFree(P->corr);
     amg_free(*P);
     for (auto& e : P->ev) if (e) cudaEventDestroy(e);
     if (P->stream) cudaStreamDestroy(P->stream);

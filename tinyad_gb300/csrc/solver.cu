@@ -298,10 +298,17 @@ __global__ void k_neg(int64_t n, const double* __restrict__ a, double* __restric
     GRID_STRIDE(i, n) out[i] = -a[i];
 }
 
+/* y += x */
+__global__ void k_axpy_plain(int64_t n, const double* __restrict__ x, double* __restrict__ y)
+{
+    GRID_STRIDE(i, n) y[i] += x[i];
+}
+
 template <typename T>
 __global__ void k_to_double(int64_t n, const T* __restrict__ a, double* __restrict__ out, int accumulate)
 {
-    GRID_STRIDE(i, n) out[i] = (accumulate ? out[i] : 0.0) + (double)a[i];
+    // accumulate: 0 = set, 1 = add, -1 = subtract
+    GRID_STRIDE(i, n) out[i] = (accumulate ? out[i] : 0.0) + (accumulate < 0 ? -(double)a[i] : (double)a[i]);
 }
 
 /* res = b - (H + wI) y with FP64 accumulation; partial |res|^2 -> ds->rr */
@@ -457,7 +464,7 @@ static tad_status pcg_core_amg(Problem& P, const double* b, T* xs, double rel_to
         amg_vcycle(P, prec, r, z);
         k_pcg_rz<T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, r, z, P.partials, P.counters + 9, P.ds, 0);
     };
-    if (P.amg_graph == nullptr || P.amg_graph_prec != prec || P.amg_graph_x != (const void*)xs)
+    if (P.amg_graph == nullptr || P.amg_graph_prec != prec || P.amg_graph_x != (const void*)xs || P.amg_graph_H != (const void*)H)
     {
         if (P.amg_graph) { cudaGraphExecDestroy(P.amg_graph); P.amg_graph = nullptr; }
         const int64_t l0 = P.n_launches;
@@ -469,6 +476,7 @@ static tad_status pcg_core_amg(Problem& P, const double* b, T* xs, double rel_to
         cudaGraphDestroy(graph);
         P.amg_graph_prec = prec;
         P.amg_graph_x = (const void*)xs;
+        P.amg_graph_H = (const void*)H;
         P.amg_graph_launches = P.n_launches - l0 + 3 * CHUNK;
         P.n_launches = l0;
     }
@@ -527,7 +535,8 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
         }
         else
         {
-            if (P.pcg_graph == nullptr || P.pcg_graph_prec != prec || P.pcg_graph_chunk != CHUNK || P.pcg_graph_x != (const void*)xs)
+            if (P.pcg_graph == nullptr || P.pcg_graph_prec != prec || P.pcg_graph_chunk != CHUNK || P.pcg_graph_x != (const void*)xs ||
+                P.pcg_graph_H != (const void*)H)
             {
                 if (P.pcg_graph) { cudaGraphExecDestroy(P.pcg_graph); P.pcg_graph = nullptr; }
                 cudaGraph_t graph;
@@ -539,6 +548,7 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
                 P.pcg_graph_prec = prec;
                 P.pcg_graph_chunk = CHUNK;
                 P.pcg_graph_x = (const void*)xs;
+                P.pcg_graph_H = (const void*)H;
             }
             for (int k = 0; k < replays; ++k) TAD_CUDA_TRY(cudaGraphLaunch(P.pcg_graph, s));
             P.n_launches += 2 * CHUNK * replays;
@@ -565,6 +575,29 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
     return TAD_OK;
 }
 
+/* FP64 solve of H64 e = res on the FP64 copy of the FP32 Hessian, added to
+   xsol (the robust completion of a tight mixed-precision solve) */
+template <int d>
+static tad_status mixed_fp64_completion(Problem& P, const double* res, double* xsol, double rel_tol, int max_iters, int* iters)
+{
+    cudaStream_t s = P.stream;
+    const int64_t nv = P.nb * d * d;
+    if (!P.Hd) TAD_CUDA_TRY(cudaMalloc(&P.Hd, std::max<int64_t>(nv, 1) * sizeof(double)));
+    k_to_double<float><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nv, (const float*)P.H, (double*)P.Hd, 0);
+    P.n_launches += 1;
+    if (!P.corr) TAD_CUDA_TRY(cudaMalloc(&P.corr, std::max<int64_t>(P.n_vars, 1) * sizeof(double)));
+    void* keep = P.H;
+    P.H = P.Hd;
+    int it = 0;
+    // the correction goes to its own buffer: xsol may be P.dx
+    const tad_status st = pcg_core<d, double>(P, res, P.corr, 0.0, rel_tol, max_iters, &it, P.r, P.z, P.p, P.Ap, P.dinv, 0);
+    P.H = keep;
+    *iters += it;
+    k_axpy_plain<<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_vars, P.corr, xsol);
+    P.n_launches += 1;
+    return st;
+}
+
 template <int d>
 static tad_status pcg_dispatch(Problem& P, const double* b, double* xsol, int precision, double rel_tol, int max_iters, int* iters)
 {
@@ -578,7 +611,12 @@ static tad_status pcg_dispatch(Problem& P, const double* b, double* xsol, int pr
     // tolerance by itself -- its recursively updated residual drifts from the
     // true one by O(eps_fp32 cond(H)) relative, far below 1e-4 -- so that pass
     // is the answer; tighter tolerances compute r = b - H x in FP64 and solve
-    // for corrections until the FP64 residual meets them.
+    // for corrections until the FP64 residual meets them.  A pass that does
+    // not halve the FP64 residual norm -- FP32 CG on a nearly singular H (the
+    // eps-regularised rigid motions of an unconstrained mesh) stalls or
+    // diverges at tight tolerances -- is undone, and the rest is solved in
+    // FP64 on an FP64 copy of the FP32 Hessian (same matrix, so the result is
+    // still exact to the FP32-evaluated Hessian).
     constexpr double LOOSE_TOL = 1e-4;
     const double tol = P.settings.refine_rel_tol;
     const double inner_tol = std::max(rel_tol, 1e-6);
@@ -592,22 +630,50 @@ static tad_status pcg_dispatch(Problem& P, const double* b, double* xsol, int pr
         if (iters) *iters = total;
         return st;
     }
+    const double target = std::min(rel_tol, std::max(tol, 0.0));
+    double rr_prev = bb;
+    bool completion = false;
     const int passes = std::max(1, P.settings.refine_max_iters);
-    for (int pass = 0; pass < passes; ++pass)
+    for (int pass = 0;; ++pass)
     {
         k_residual<d, float><<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_handles, P.bptr, P.bcol, (const float*)P.H, 0.0, xsol, b, P.res,
                                                                 P.partials, P.counters + 3, P.ds);
         P.n_launches += 1;
         TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
         TAD_CUDA_TRY(cudaStreamSynchronize(s));
-        if (P.hs->rr <= tol * tol * bb || total >= max_iters) break;
-        if (rel_tol >= inner_tol && P.hs->rr <= rel_tol * rel_tol * bb) break;
-        if (pass + 1 == passes) break;
+        const double rr = P.hs->rr;
+        if (rr <= target * target * bb || total >= max_iters) break;
+        if (!(rr <= 0.25 * rr_prev))
+        {
+            // the last FP32 pass did not halve the residual: undo it, finish in FP64
+            k_to_double<float><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, P.dx32, xsol, -1);
+            k_residual<d, float><<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_handles, P.bptr, P.bcol, (const float*)P.H, 0.0, xsol, b,
+                                                                    P.res, P.partials, P.counters + 3, P.ds);
+            P.n_launches += 2;
+            completion = true;
+            break;
+        }
+        if (pass + 1 >= passes) break;
+        rr_prev = rr;
         int it = 0;
         st = pcg_core<d, float>(P, P.res, P.dx32, 0.0, inner_tol, max_iters - total, &it, P.r32, P.z32, P.p32, P.Ap32, P.dinv32, 1);
         total += it;
         k_to_double<float><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, P.dx32, xsol, 1);
         P.n_launches += 1;
+    }
+    if (completion)
+    {
+        // res holds b - H x for the current x; relative target against |b|
+        TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
+        TAD_CUDA_TRY(cudaStreamSynchronize(s));
+        const double rres = std::sqrt(std::max(P.hs->rr, 0.0));
+        const double rel = rres > 0.0 ? std::min(0.5, target * std::sqrt(bb) / rres) : 0.5;
+        st = mixed_fp64_completion<d>(P, P.res, xsol, rel, std::max(1, max_iters - total), &total);
+        k_residual<d, float><<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_handles, P.bptr, P.bcol, (const float*)P.H, 0.0, xsol, b, P.res,
+                                                                P.partials, P.counters + 3, P.ds);
+        P.n_launches += 1;
+        TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
+        TAD_CUDA_TRY(cudaStreamSynchronize(s));
     }
     if (iters) *iters = total;
     if (!(P.hs->rr <= rel_tol * rel_tol * bb * 1.0001) && !(P.hs->rr <= tol * tol * bb)) return TAD_ERR_PCG_NOCONV;
