@@ -190,6 +190,10 @@ typedef struct tad_term_eval_args {
     double* out_r_d;          /* [n_elem][M] residuals, or NULL */
     double* out_J_d;          /* [n_elem][M][N*d] residual gradients in local slot order, or NULL */
     double* out_Hv_d;         /* [n_elem][M][k(k+1)/2] packed residual Hessians, k = N*d, or NULL */
+    /* HESSIAN_PROJ: device scratch of n_elem + 1 uint32 (library-owned): the
+       element kernels list there the elements whose Hessian is not
+       translation invariant, which then get the general projection */
+    uint32_t* proj_list_d;
 } tad_term_eval_args;
 
 typedef enum tad_eval_mode {

@@ -26,7 +26,8 @@ enum : int32_t {
     DEVERR_UNRECORDED_ACCESS = 1,   /* handle not in the recorded access list */
     DEVERR_TOO_MANY_VARS = 2,       /* more distinct handles than the valence */
     DEVERR_NONFINITE = 4,           /* non-finite gradient/Hessian entry */
-    DEVERR_TIMEOUT = 8              /* bounded wait gave up */
+    DEVERR_TIMEOUT = 8,             /* bounded wait gave up */
+    DEVERR_NO_PROJ_LIST = 16        /* HESSIAN_PROJ launched without the projection list */
 };
 
 #if defined(__CUDACC__)

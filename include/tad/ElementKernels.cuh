@@ -6,8 +6,9 @@
  *
  * One element per thread.  The functor runs with an element whose
  * variables() seed tad::Scalar<k> values (k = d*N) held in registers; the
- * result (value, gradient, packed Hessian) is optionally PSD-projected in the
- * same thread (project_positive_definite, tad/Projection.cuh) and written as
+ * result (value, gradient, packed Hessian) is optionally PSD-projected
+ * (tad/Projection.cuh: translation-deflated where the element Hessian allows
+ * it, else the general form in a second pass) and written as
  *   f:  double  out_f[e]
  *   g:  Tg      out_g[e][N*d]                         (slot-major)
  *   H:  Th      out_H[e][N(N+1)/2 slot pairs a<=b][d][d]
@@ -18,6 +19,7 @@
  */
 #pragma once
 #include <stdint.h>
+#include <algorithm>
 #include <type_traits>
 #include "Scalar.cuh"
 #include "Element.cuh"
@@ -48,6 +50,7 @@ struct ElemLaunch
     double* out_r;           /* vector terms: residuals [n_elem][M] */
     double* out_J;           /* vector terms: residual gradients [n_elem][M][k] */
     double* out_Hv;          /* vector terms: packed residual Hessians [n_elem][M][k(k+1)/2] */
+    uint32_t* proj_list;     /* HESSIAN_PROJ: [0] count, [1..] elements left for the general projection */
 };
 
 template <int d, int N, typename Energy>
@@ -124,17 +127,79 @@ template <int K> struct GradOf<float, K> { using type = std::conditional_t<(K <=
 /* For k <= 8 the PSD projection runs in its own kernel (k_project_blocks)
    over the element blocks the evaluation kernel wrote: the evaluation needs
    ~250 registers a thread for the live Scalar<k> intermediates, the k = 6
-   projection (packed matrix + eigenvectors) under 100, so apart it runs at
-   about three times the occupancy for the price of re-reading and
-   re-writing the blocks once (measured on the 1.64M-face disk, FP32:
-   1.34 ms fused, 1.17 ms split).  At k = 12 the projection alone (78 + 144
-   entries) exceeds the register file of a thread either way and the second
-   pass only adds traffic (13.6 ms fused, 18.4 ms split on 663,552 tets), so
+   projection under 70, so apart it runs at several times the occupancy for
+   the price of re-reading and re-writing the blocks once.  At k = 12 the
+   evaluation alone spills, and a second pass only adds traffic (13.6 ms
+   fused, 18.4 ms split on 663,552 tets with the full 12 x 12 projection), so
    it stays fused. */
 template <int k> struct FusedProjection { static constexpr bool value = k > 8; };
 
-/* second-order evaluation with the Hessian in T: double (plain Double<k>), or
-   float with FP64 value and double-float gradient (mixed, tad::Mixed<k>). */
+/* Valences whose elements try the translation-deflated projection
+   (project_translation_deflated); elements that are not translation
+   invariant are appended to L.proj_list and projected by
+   k_project_general, which keeps the general k x k eigensolver (and its
+   registers) out of the evaluation and block-projection kernels. */
+template <int N> struct DeflatedProjection { static constexpr bool value = N >= 2 && N <= 9; };
+
+__device__ __forceinline__ void defer_projection(const ElemLaunch& L, int64_t e)
+{
+    if (!L.proj_list) { report_error(L.err, DEVERR_NO_PROJ_LIST); return; }
+    const uint32_t slot = atomicAdd(L.proj_list, 1u);
+    L.proj_list[1 + slot] = (uint32_t)e;
+}
+
+/* PSD projection of an element Hessian in an element kernel: the deflated
+   form where the valence allows it, with non-invariant elements deferred */
+template <int d, int N, typename T>
+__device__ __forceinline__ bool project_or_defer(const ElemLaunch& L, int64_t e, T* hp, T eps)
+{
+    if constexpr (DeflatedProjection<N>::value)
+    {
+        const int r = project_translation_deflated<d, N, T>(hp, eps);
+        if (r < 0) { defer_projection(L, e); return false; }
+        return r > 0;
+    }
+    else return project_positive_definite<d * N, T>(hp, eps);
+}
+
+/* element block layout (NP vertex-pair blocks of d x d, row-major) <->
+   packed upper triangle of the k x k element Hessian */
+template <int d, int N, typename T>
+__device__ __forceinline__ void blocks_to_packed(const T* hb, T* h)
+{
+    constexpr int k = d * N;
+#pragma unroll
+    for (int a = 0; a < N; ++a)
+#pragma unroll
+        for (int b = a; b < N; ++b)
+#pragma unroll
+            for (int p = 0; p < d; ++p)
+#pragma unroll
+                for (int q = 0; q < d; ++q)
+                {
+                    const int i = a * d + p, j = b * d + q;
+                    if (i <= j) h[packed_index(i, j, k)] = hb[packed_index(a, b, N) * d * d + p * d + q];
+                }
+}
+
+template <int d, int N, typename T>
+__device__ __forceinline__ void packed_to_blocks(const T* h, T* hb)
+{
+    constexpr int k = d * N;
+#pragma unroll
+    for (int a = 0; a < N; ++a)
+#pragma unroll
+        for (int b = a; b < N; ++b)
+#pragma unroll
+            for (int p = 0; p < d; ++p)
+#pragma unroll
+                for (int q = 0; q < d; ++q)
+                {
+                    const int i = a * d + p, j = b * d + q;
+                    hb[packed_index(a, b, N) * d * d + p * d + q] = (i <= j) ? h[packed_index(i, j, k)] : h[packed_index(j, i, k)];
+                }
+}
+
 template <int d, int N, typename T, typename Energy>
 __global__ void __launch_bounds__(128) k_elem_hessian(ElemLaunch L, Energy energy)
 {
@@ -150,7 +215,7 @@ __global__ void __launch_bounds__(128) k_elem_hessian(ElemLaunch L, Energy energ
 #pragma unroll
     for (int i = 0; i < N; ++i) el.vh[i] = L.rec[e * N + i];
     S r = energy(el);
-    if (FusedProjection<k>::value && L.project) project_positive_definite<k, T>(r.hess, (T)L.eps);
+    if (FusedProjection<k>::value && L.project) project_or_defer<d, N, T>(L, e, r.hess, (T)L.eps);
     L.out_f[e] = (double)r.val;
     bool fin = true;
     double gv[k];
@@ -182,42 +247,41 @@ __global__ void __launch_bounds__(128) k_elem_hessian(ElemLaunch L, Energy energ
 /* Projection of the element blocks (layout of k_elem_hessian: NP vertex-pair
    blocks of d x d, row-major) in place, one element per thread. */
 template <int d, int N, typename T>
-__global__ void __launch_bounds__(128) k_project_blocks(int64_t n_elem, T* __restrict__ Hblocks, T eps)
+__global__ void __launch_bounds__(128) k_project_blocks(ElemLaunch L, T eps)
 {
     constexpr int k = d * N;
-    constexpr int NP = N * (N + 1) / 2;
-    constexpr int BS = NP * d * d;
+    constexpr int BS = N * (N + 1) / 2 * d * d;
     const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (e >= n_elem) return;
+    if (e >= L.n_elem) return;
+    T* Hblocks = (T*)L.out_H;
     T hb[BS];
     load_row<T, BS>(Hblocks, e, hb);
     T h[k * (k + 1) / 2];
-#pragma unroll
-    for (int a = 0; a < N; ++a)
-#pragma unroll
-        for (int b = a; b < N; ++b)
-#pragma unroll
-            for (int p = 0; p < d; ++p)
-#pragma unroll
-                for (int q = 0; q < d; ++q)
-                {
-                    const int i = a * d + p, j = b * d + q;
-                    if (i <= j) h[packed_index(i, j, k)] = hb[packed_index(a, b, N) * d * d + p * d + q];
-                }
-    if (!project_positive_definite<k, T>(h, eps)) return;
-#pragma unroll
-    for (int a = 0; a < N; ++a)
-#pragma unroll
-        for (int b = a; b < N; ++b)
-#pragma unroll
-            for (int p = 0; p < d; ++p)
-#pragma unroll
-                for (int q = 0; q < d; ++q)
-                {
-                    const int i = a * d + p, j = b * d + q;
-                    hb[packed_index(a, b, N) * d * d + p * d + q] = (i <= j) ? h[packed_index(i, j, k)] : h[packed_index(j, i, k)];
-                }
+    blocks_to_packed<d, N, T>(hb, h);
+    if (!project_or_defer<d, N, T>(L, e, h, eps)) return;
+    packed_to_blocks<d, N, T>(h, hb);
     store_row<T, BS>(Hblocks, e, hb);
+}
+
+/* General projection (project_positive_definite<d*N>) of the elements listed
+   by project_or_defer, grid-stride over the list. */
+template <int d, int N, typename T>
+__global__ void __launch_bounds__(128) k_project_general(const uint32_t* __restrict__ list, T* __restrict__ Hblocks, T eps)
+{
+    constexpr int k = d * N;
+    constexpr int BS = N * (N + 1) / 2 * d * d;
+    const uint32_t n = list[0];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const int64_t e = list[1 + i];
+        T hb[BS];
+        load_row<T, BS>(Hblocks, e, hb);
+        T h[k * (k + 1) / 2];
+        blocks_to_packed<d, N, T>(hb, h);
+        if (!project_positive_definite<k, T>(h, eps)) continue;
+        packed_to_blocks<d, N, T>(h, hb);
+        store_row<T, BS>(Hblocks, e, hb);
+    }
 }
 
 inline unsigned elem_grid(int64_t n) { return (unsigned)((n + 127) / 128); }
@@ -243,6 +307,7 @@ inline ElemLaunch make_launch(const tad_term_eval_args& a)
     L.out_r = a.out_r_d;
     L.out_J = a.out_J_d;
     L.out_Hv = a.out_Hv_d;
+    L.proj_list = a.proj_list_d;
     return L;
 }
 
@@ -252,10 +317,14 @@ template <int d, int N, typename T, typename Energy>
 inline void launch_elements_hessian(const ElemLaunch& L, const Energy& energy, cudaStream_t s)
 {
     if (L.n_elem <= 0) return;
+    constexpr bool deflated = DeflatedProjection<N>::value;
+    if (deflated && L.project && L.proj_list) cudaMemsetAsync(L.proj_list, 0, sizeof(uint32_t), s);
     k_elem_hessian<d, N, T, Energy><<<elem_grid(L.n_elem), 128, 0, s>>>(L, energy);
     if constexpr (!FusedProjection<d * N>::value)
-        if (L.project)
-        k_project_blocks<d, N, T><<<elem_grid(L.n_elem), 128, 0, s>>>(L.n_elem, (T*)L.out_H, (T)L.eps);
+        if (L.project) k_project_blocks<d, N, T><<<elem_grid(L.n_elem), 128, 0, s>>>(L, (T)L.eps);
+    if constexpr (deflated)
+        if (L.project && L.proj_list)
+            k_project_general<d, N, T><<<std::min(elem_grid(L.n_elem), 1216u), 128, 0, s>>>(L.proj_list, (T*)L.out_H, (T)L.eps);
 }
 
 /* Value, gradient, line-search and record kernels (modes 0, 1, 4, 5).  The

@@ -199,4 +199,158 @@ TAD_HD bool project_positive_definite(T* hp, T eps)
     return true;
 }
 
+/* ------------------------------------------------------------------------ */
+/* Translation-deflated projection of an element Hessian                     */
+/* ------------------------------------------------------------------------ */
+
+/* 1 / sqrt((m+1)(m+2)), m = 0..7, as literals so that unrolled loops fold
+   them to constants */
+TAD_HD constexpr double helmert_scale(int m)
+{
+    return m == 0 ? 0.7071067811865475 : m == 1 ? 0.4082482904638631 : m == 2 ? 0.2886751345948129
+         : m == 3 ? 0.22360679774997896 : m == 4 ? 0.18257418583505536 : m == 5 ? 0.1543033499620919
+         : m == 6 ? 0.1336306209562122 : 0.11785113019775793;
+}
+
+/* Helmert basis of the complement of (1, ..., 1) in R^N (N <= 9): column m
+   (0 <= m < N-1) is (1, ..., 1, -(m+1), 0, ...) / sqrt((m+1)(m+2)) with m+1
+   leading ones.  Orthonormal, and orthogonal to the constant vector. */
+TAD_HD constexpr double helmert(int a, int m)
+{
+    return a <= m ? helmert_scale(m) : (a == m + 1 ? -(m + 1.0) * helmert_scale(m) : 0.0);
+}
+
+/* Row-sum tolerance (relative to max |H_ij|) below which an element Hessian
+   counts as translation invariant: a few hundred rounding units of the
+   evaluation precision. */
+template <typename T> struct TranslationTol { static constexpr double value = 256.0 * 2.220446049250313e-16; };
+template <> struct TranslationTol<float> { static constexpr double value = 256.0 * 1.1920928955078125e-07; };
+
+/* Projection of the packed Hessian hp of an element with N vertices of d
+   coordinates (variable a*d+p = coordinate p of vertex a), with the result of
+   project_positive_definite<d*N>, for element energies that are invariant
+   under translations of all N vertices (every energy of edge vectors or
+   vertex differences: distortion, elasticity, Laplacian).
+   For those the d translations t_p (t_p[a*d+p] = 1/sqrt(N)) are exact null
+   vectors of H, hence eigenvectors with eigenvalue 0 (clamped to eps), and
+   the other eigenpairs are those of the (d(N-1))^2 matrix A = Q^T H Q, Q =
+   (Helmert basis of the complement of 1) x I_d.  The eigenproblem shrinks
+   from k = dN to d(N-1) (k = 6 -> 4, 12 -> 9; the Jacobi cost goes with the
+   cube).  The result is written in correction form,
+       H + sum_{l: lambda_l(A) < eps} (eps - lambda_l) (Q v_l)(Q v_l)^T + eps sum_p t_p t_p^T,
+   (for eps < 0, negative lambda_l flip: (|lambda_l| - lambda_l); the
+   translations are left as they are), equal to V max(Lambda, eps) V^T in exact
+   arithmetic.
+   The diagonal-dominance early out of the general rule comes first (for
+   eps < 0 its margin is negative and it can hold for invariant matrices).
+   Returns 0 (hp unchanged) when it holds; -1 without touching hp when H is
+   not translation invariant (some row sum H t_p above TranslationTol times
+   max |H_ij|, or a non-finite entry): the caller then runs
+   project_positive_definite<d*N>.  Otherwise returns 1 (hp projected). */
+template <int d, int N, typename T>
+TAD_HD int project_translation_deflated(T* hp, T eps)
+{
+    constexpr int k = d * N, R = d * (N - 1), NR = R * (R + 1) / 2;
+    if (positive_diagonally_dominant<k, T>(hp, eps)) return 0;
+    auto H = [&](int i, int j) -> T { return i <= j ? hp[packed_index(i, j, k)] : hp[packed_index(j, i, k)]; };
+    T hmax = T(0);
+#pragma unroll
+    for (int q = 0; q < k * (k + 1) / 2; ++q) hmax = tad_abs(hp[q]) > hmax ? tad_abs(hp[q]) : hmax;
+    T rmax = T(0);
+#pragma unroll
+    for (int i = 0; i < k; ++i)
+#pragma unroll
+        for (int q = 0; q < d; ++q)
+        {
+            T s = T(0);
+#pragma unroll
+            for (int b = 0; b < N; ++b) s += H(i, b * d + q);
+            rmax = tad_abs(s) > rmax ? tad_abs(s) : rmax;
+        }
+    if (!(rmax <= T(TranslationTol<T>::value) * hmax) || !(hmax < T(INFINITY))) return -1;
+    // A = Q^T (H Q) (packed R x R, reduced index m*d + p), streamed over the
+    // rows i = a*d + p of H: w = (H Q)[i][J] is formed and at once added to
+    // the rows (m, p) of A with Q[a][m] != 0 (m >= a-1), so no k x R
+    // intermediate is held
+    T A[NR];
+#pragma unroll
+    for (int q = 0; q < NR; ++q) A[q] = T(0);
+#pragma unroll
+    for (int i = 0; i < k; ++i)
+    {
+        const int a = i / d, p = i % d;
+#pragma unroll
+        for (int J = 0; J < R; ++J)
+        {
+            const int m2 = J / d, q = J % d;
+            if ((a > 0 ? a - 1 : 0) * d + p > J) continue;   // no (m, p) <= J receives this entry
+            T w = T(0);
+#pragma unroll
+            for (int b = 0; b <= m2 + 1; ++b) w += H(i, b * d + q) * T(helmert(b, m2));
+#pragma unroll
+            for (int m = (a > 0 ? a - 1 : 0); m < N - 1; ++m)
+                if (m * d + p <= J) A[packed_index(m * d + p, J, R)] += T(helmert(a, m)) * w;
+        }
+    }
+    T V[R * R];
+    T lam0[R];
+    jacobi_eigen_packed<R, T>(A, V);
+#pragma unroll
+    for (int l = 0; l < R; ++l)
+    {
+        const T lv = A[packed_index(l, l, R)];
+        T c = T(0);
+        if (eps < T(0)) { if (lv < T(0)) c = -lv - lv; }
+        else if (lv < eps) c = eps - lv;
+        lam0[l] = c;
+    }
+    // clamped modes, lifted back: w = Q v_l
+#pragma unroll
+    for (int l = 0; l < R; ++l)
+    {
+        if (lam0[l] == T(0)) continue;
+        T w[k];
+#pragma unroll
+        for (int a = 0; a < N; ++a)
+#pragma unroll
+            for (int p = 0; p < d; ++p)
+            {
+                T s = T(0);
+#pragma unroll
+                for (int m = (a > 0 ? a - 1 : 0); m < N - 1; ++m) s += T(helmert(a, m)) * V[(m * d + p) * R + l];
+                w[a * d + p] = s;
+            }
+#pragma unroll
+        for (int i = 0; i < k; ++i)
+#pragma unroll
+            for (int j = i; j < k; ++j) hp[packed_index(i, j, k)] += lam0[l] * w[i] * w[j];
+    }
+    if (eps > T(0))
+    {
+        const T c = eps / T(N);
+#pragma unroll
+        for (int a = 0; a < N; ++a)
+#pragma unroll
+            for (int b = 0; b < N; ++b)
+#pragma unroll
+                for (int p = 0; p < d; ++p)
+                    if (a * d + p <= b * d + p) hp[packed_index(a * d + p, b * d + p, k)] += c;
+    }
+    return 1;
+}
+
+/* Element projection: the translation-deflated form where it applies (N >= 2
+   and H translation invariant), else the general one.  Returns true if hp was
+   changed. */
+template <int d, int N, typename T>
+TAD_HD bool project_element_hessian(T* hp, T eps)
+{
+    if constexpr (N >= 2 && N <= 9)
+    {
+        const int r = project_translation_deflated<d, N, T>(hp, eps);
+        if (r >= 0) return r > 0;
+    }
+    return project_positive_definite<d * N, T>(hp, eps);
+}
+
 } // namespace tad

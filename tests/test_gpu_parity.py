@@ -149,6 +149,47 @@ def test_inverted_elements(tad, oracle):
     assert fn.eval(x) == np.inf
 
 
+@pytest.mark.parametrize("d", [1, 2])
+def test_projection_paths(tad, oracle, d):
+    """Both device projection paths in one term, against the oracle's general
+    projection: dense quadratic elements (N = 2) whose Hessian is translation
+    invariant (A = P S P, P removing the d translations; deflated
+    eigenproblem) and general ones (A = S; listed and projected by the
+    general kernel).  FP64 within 1e-10, mixed precision at FP32 accuracy."""
+    rng = np.random.default_rng(23 + d)
+    n_handles, n_elem, k = 300, 2000, 2 * d
+    handles = np.stack([rng.integers(0, n_handles, n_elem), rng.integers(0, n_handles, n_elem)], 1)
+    handles[handles[:, 0] == handles[:, 1], 1] = (handles[handles[:, 0] == handles[:, 1], 0] + 1) % n_handles
+    Pm = np.eye(k) - np.array([[1.0 / 2 if (i % d) == (j % d) else 0.0 for j in range(k)] for i in range(k)])
+    params = []
+    n_general = 0
+    for e in range(n_elem):
+        M = rng.normal(size=(k, k))
+        S = M @ np.diag(rng.choice([-1.0, 1.0], k) * 10.0 ** rng.uniform(-2, 1, k)) @ M.T
+        if e % 4 == 0:
+            A = S
+            n_general += 1
+        else:
+            A = Pm @ S @ Pm
+        params.append(np.concatenate([0.5 * (A + A.T).ravel(), rng.normal(size=k), [0.0]]))
+    params = np.array(params)
+    x = rng.normal(size=d * n_handles)
+    p = oracle.Problem(d, n_handles)
+    p.add_elements(meshes.TAD_ENERGY_QUADRATIC, handles, params)
+    fo, go, Ho = p.eval_with_hessian_proj(x)
+    assert n_general > 0
+    for prec, tol in ((tad.PREC_FP64, TOL), (tad.PREC_MIXED, 2e-5)):
+        fn = tad.ScalarFunction(d, n_handles, precision=prec)
+        fn.add_elements(meshes.TAD_ENERGY_QUADRATIC, handles, params)
+        f, g, H = fn.eval_with_hessian_proj(x)
+        assert rel_err(f, fo) <= TOL and rel_err(g, go) <= TOL
+        assert sparse_rel_err(H, Ho) <= tol, (prec, sparse_rel_err(H, Ho))
+        # flip mode (eps < 0)
+        fo2, go2, Ho2 = p.eval_with_hessian_proj(x, eps=-1.0)
+        f2, g2, H2 = fn.eval_with_hessian_proj(x, projection_eps=-1.0)
+        assert sparse_rel_err(H2, Ho2) <= tol, (prec, sparse_rel_err(H2, Ho2))
+
+
 def test_disk_newton_parity(tad, oracle):
     """Config 0: 20 Projected-Newton iterations on the device reach the
     oracle's (LDL^T-based) final energy within 1e-8 relative."""

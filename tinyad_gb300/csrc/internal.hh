@@ -130,6 +130,7 @@ struct Problem
     double* eg = nullptr;
     void* eH = nullptr;
     size_t eH_bytes = 0;
+    uint32_t* proj_list = nullptr;   // largest term's n_elem + 1: elements left for the general projection
 
     // pattern
     int64_t nb = 0, ncontrib = 0, ninc = 0;
@@ -150,6 +151,9 @@ struct Problem
     float *r32 = nullptr, *z32 = nullptr, *p32 = nullptr, *Ap32 = nullptr, *dx32 = nullptr, *dinv32 = nullptr;
     double *rhs = nullptr, *res = nullptr;
     double* steps = nullptr;   // LS_BATCH trial step sizes (device)
+    double* steps_seq = nullptr;   // the line search's whole step sequence (device), for steps_key
+    int steps_seq_cap = 0;
+    double steps_key[3] = {0.0, 0.0, 0.0};   // s_max, shrink, length of the sequence in steps_seq
     double* partials = nullptr;
     unsigned* counters = nullptr;
     DevScalars* ds = nullptr;
@@ -215,8 +219,9 @@ void amg_free(Problem& P);
 int amg_levels(const Problem& P);
 tad_status pcg_solve(Problem& P, const double* b, double* xsol, double w_identity, int precision,
                      double rel_tol, int max_iters, int* iters_out);
+/* f_on_device: the energy at x is already in ds->f (f is then ignored) */
 tad_status line_search_device(Problem& P, double* x, const double* d, double f, double s_max,
-                              bool* found, double* f_out, int* trials);
+                              bool* found, double* f_out, int* trials, bool f_on_device = false);
 tad_status newton_solve(Problem& P, double* x_d, int n_iters, double eps, double stop_decrement,
                         double* f_hist, int* iters_done);
 

@@ -90,6 +90,7 @@ tad_status check_device_error(Problem& P)
     if (e & 1) return fail(TAD_ERR_ARG, "element accessed a variable handle outside its recorded access list");
     if (e & 4) return fail(TAD_ERR_NONFINITE, "Assertion failed: Not finite (element gradient or Hessian)");
     if (e & 8) return fail(TAD_ERR_TIMEOUT, "a bounded device-side wait gave up");
+    if (e & 16) return fail(TAD_ERR_ARG, "HESSIAN_PROJ element kernel launched without tad_term_eval_args.proj_list_d");
     return fail(TAD_ERR_CUDA, "device error word " + std::to_string(e));
 }
 
@@ -242,6 +243,14 @@ tad_status ensure_finalized(Problem& P)
     TAD_CUDA_TRY(dalloc(&P.eg, (size_t)so * P.d));
     P.eH_bytes = (size_t)po * P.d * P.d * sizeof(double);
     TAD_CUDA_TRY(cudaMalloc(&P.eH, std::max<size_t>(P.eH_bytes, 8)));
+    {
+        int64_t mx = 0;
+        for (const Term& T : P.terms) mx = std::max(mx, T.n_elem);
+        if (mx >= (int64_t)UINT32_MAX) return fail(TAD_ERR_ARG, "a term has 2^32 - 1 or more elements");
+        dfree(P.proj_list);
+        TAD_CUDA_TRY(cudaMalloc(&P.proj_list, (size_t)(mx + 1) * sizeof(uint32_t)));
+        TAD_CUDA_TRY(cudaMemsetAsync(P.proj_list, 0, sizeof(uint32_t), P.stream));
+    }
     // record access order of custom terms (x = 0)
     for (Term& T : P.terms)
     {
@@ -295,6 +304,7 @@ tad_status eval_elements(Problem& P, int mode, const double* x, double eps, int 
         a.out_H_d = (char*)P.eH + T.pair_off * P.d * P.d * (precision == TAD_PREC_MIXED ? sizeof(float) : sizeof(double));
         a.error_d = P.err;
         a.stream = P.stream;
+        a.proj_list_d = P.proj_list;
         a.n_outputs = T.M;
         if (T.M > 0)
         {
@@ -403,7 +413,7 @@ TAD_API tad_status tad_problem_destroy(tad_problem* P)
     void* bufs[] = {P->ef, P->eg, P->eH, P->bptr, P->bcol, P->diag, P->cptr, P->cidx, P->gptr, P->gidx,
                     P->x, P->g, P->H, P->H64, P->csr_tmp, P->r, P->z, P->p, P->Ap, P->dx, P->dinv,
                     P->r32, P->z32, P->p32, P->Ap32, P->dx32, P->dinv32, P->rhs, P->res, P->steps,
-                    P->partials, P->counters, P->ds, P->err};
+                    P->partials, P->counters, P->ds, P->err, P->proj_list, P->steps_seq};
     for (void* b : bufs) dfree(b);
     if (P->hs) cudaFreeHost(P->hs);
     if (P->err_h) cudaFreeHost(P->err_h);

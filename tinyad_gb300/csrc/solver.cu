@@ -41,11 +41,14 @@
 namespace tadlib {
 
 /* x = 0, r = b, z = M^-1 r, p = Ap = 0, beta = 0 (the first fused SpMV then
-   forms p = z, Ap = A z); rz = r.z, bb = b.b */
+   forms p = z, Ap = A z); rz = r.z, bb = b.b.  With H given (block Jacobi),
+   the inverted diagonal blocks of H + w I are formed here and stored in dinv;
+   with H = NULL dinv is read (the AMG finest level's). */
 template <int d, typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_pcg_init(int64_t nh, const double* __restrict__ b, T* x, T* r, T* z, T* p,
-                                                          T* Ap, const T* __restrict__ dinv, double* partials, unsigned* counter,
-                                                          DevScalars* ds, double rel_tol, int max_iters)
+                                                          T* Ap, T* __restrict__ dinv, const int32_t* __restrict__ diag,
+                                                          const T* __restrict__ H, double w, double* partials,
+                                                          unsigned* counter, DevScalars* ds, double rel_tol, int max_iters)
 {
     // per-thread partials in the PCG's precision (a few rows each), combined in FP64
     T acc_rz = T(0), acc_bb = T(0);
@@ -54,7 +57,20 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_init(int64_t nh, const doub
         T rv[d], zv[d];
 #pragma unroll
         for (int i = 0; i < d; ++i) { rv[i] = (T)b[u * d + i]; x[u * d + i] = T(0); r[u * d + i] = rv[i]; }
-        apply_dinv<d, T>(dinv, u, rv, zv);
+        if (H)
+        {
+            T I[d * d];
+            diag_block_inverse<d, T>(diag, H, w, u, I);
+#pragma unroll
+            for (int i = 0; i < d; ++i)
+            {
+                T acc = T(0);
+#pragma unroll
+                for (int j = 0; j < d; ++j) { acc += I[i * d + j] * rv[j]; dinv[u * d * d + i * d + j] = I[i * d + j]; }
+                zv[i] = acc;
+            }
+        }
+        else apply_dinv<d, T>(dinv, u, rv, zv);
 #pragma unroll
         for (int i = 0; i < d; ++i)
         {
@@ -353,11 +369,17 @@ __global__ void __launch_bounds__(RED_THREADS) k_dot_dg(int64_t n, const double*
     if (threadIdx.x == 0) { ds->dg = tot[0]; ds->decrement = -0.5 * tot[0]; }
 }
 
-__global__ void __launch_bounds__(RED_THREADS) k_dot_gg(int64_t n, const double* __restrict__ a,
+/* rhs = -g and g.g in one pass (the Newton right-hand side and |g|^2) */
+__global__ void __launch_bounds__(RED_THREADS) k_neg_gg(int64_t n, const double* __restrict__ g, double* __restrict__ rhs,
                                                         double* partials, unsigned* counter, DevScalars* ds)
 {
     double part[1] = {0.0};
-    GRID_STRIDE(i, n) part[0] += a[i] * a[i];
+    GRID_STRIDE(i, n)
+    {
+        const double v = g[i];
+        rhs[i] = -v;
+        part[0] += v * v;
+    }
     double tot[1];
     if (!grid_sum<1>(part, partials, counter, tot)) return;
     if (threadIdx.x == 0) ds->gg = tot[0];
@@ -450,8 +472,8 @@ static tad_status pcg_core_amg(Problem& P, const double* b, T* xs, double rel_to
     const int64_t nh = P.n_handles, n = P.n_vars;
     cudaStream_t s = P.stream;
     // x = 0, r = b, p = Ap = 0, tolerance and counters (its z = D^-1 r is replaced)
-    k_pcg_init<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, b, xs, r, z, p, Ap, (const T*)P.amg[0].dinv, P.partials,
-                                                        P.counters, P.ds, rel_tol, max_iters);
+    k_pcg_init<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, b, xs, r, z, p, Ap, (T*)P.amg[0].dinv, nullptr, nullptr, 0.0,
+                                                        P.partials, P.counters, P.ds, rel_tol, max_iters);
     amg_vcycle(P, prec, r, z);
     k_pcg_rz<T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, r, z, P.partials, P.counters + 9, P.ds, 1);
     P.n_launches += 2;
@@ -503,9 +525,9 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
     const T* H = (const T*)P.H;
     const int64_t nh = P.n_handles;
     cudaStream_t s = P.stream;
-    k_diag_inv<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, P.diag, H, w, dinv);
-    k_pcg_init<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, b, xs, r, z, p, Ap, dinv, P.partials, P.counters, P.ds, rel_tol, max_iters);
-    P.n_launches += 2;
+    k_pcg_init<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, b, xs, r, z, p, Ap, dinv, P.diag, H, w, P.partials, P.counters, P.ds,
+                                                        rel_tol, max_iters);
+    P.n_launches += 1;
     TAD_CUDA_TRY(cudaGetLastError());
     // The first iteration is launched directly and checked at once (early
     // Newton iterations converge in one); after that, CHUNK iterations
@@ -734,31 +756,57 @@ static void step_sequence(double s_max, double shrink, int n, std::vector<double
     }
 }
 
+/* The step sequence for (s_max, shrink, n) in P.steps_seq, uploaded only
+   when the key changes. */
+static tad_status ensure_step_sequence(Problem& P, double s_max, int n)
+{
+    const double shrink = P.settings.ls_shrink;
+    if (P.steps_seq && P.steps_key[0] == s_max && P.steps_key[1] == shrink && P.steps_key[2] == (double)n) return TAD_OK;
+    if (n > P.steps_seq_cap)
+    {
+        if (P.steps_seq) TAD_CUDA_TRY(cudaFree(P.steps_seq));
+        P.steps_seq = nullptr;
+        TAD_CUDA_TRY(cudaMalloc(&P.steps_seq, (size_t)n * sizeof(double)));
+        P.steps_seq_cap = n;
+    }
+    std::vector<double> seq;
+    step_sequence(s_max, shrink, n, seq);
+    TAD_CUDA_TRY(cudaMemcpyAsync(P.steps_seq, seq.data(), (size_t)n * sizeof(double), cudaMemcpyHostToDevice, P.stream));
+    TAD_CUDA_TRY(cudaStreamSynchronize(P.stream));   // seq is a host temporary
+    P.steps_key[0] = s_max; P.steps_key[1] = shrink; P.steps_key[2] = (double)n;
+    return TAD_OK;
+}
+
 tad_status line_search_device(Problem& P, double* x, const double* d, double f, double s_max, bool* found,
-                              double* f_out, int* trials)
+                              double* f_out, int* trials, bool f_on_device)
 {
     cudaStream_t s = P.stream;
     const int max_iters = P.settings.ls_max_iters > 0 ? P.settings.ls_max_iters : 64;
-    std::vector<double> seq;
-    step_sequence(s_max, P.settings.ls_shrink, max_iters, seq);
+    tad_status st = ensure_step_sequence(P, s_max, max_iters);
+    if (st != TAD_OK) return st;
     k_dot_dg<<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_vars, d, P.g, P.partials, P.counters + 4, P.ds);
     P.n_launches += 1;
-    // current energy: caller provides it in ds->f
-    TAD_CUDA_TRY(cudaMemcpyAsync(&P.ds->f, &f, sizeof(double), cudaMemcpyHostToDevice, s));
+    // current energy: ds->f, from the caller unless it is already there
+    if (!f_on_device) TAD_CUDA_TRY(cudaMemcpyAsync(&P.ds->f, &f, sizeof(double), cudaMemcpyHostToDevice, s));
     *found = false;
     int t0 = 0;
     int batch = 1;
     while (t0 < max_iters)
     {
         const int nb = std::min(batch, max_iters - t0);
-        TAD_CUDA_TRY(cudaMemcpyAsync(P.steps, seq.data() + t0, nb * sizeof(double), cudaMemcpyHostToDevice, s));
-        tad_status st = eval_elements(P, TAD_MODE_LINESEARCH, x, 0.0, P.precision, d, nb);
+        double* keep = P.steps;
+        P.steps = P.steps_seq + t0;
+        st = eval_elements(P, TAD_MODE_LINESEARCH, x, 0.0, P.precision, d, nb);
+        P.steps = keep;
         if (st != TAD_OK) return st;
         launch_reduce_f(P, nb, P.ds->f_trial);
-        k_ls_select<<<1, 32, 0, s>>>(nb, P.steps, P.settings.ls_armijo, P.ds);
+        k_ls_select<<<1, 32, 0, s>>>(nb, P.steps_seq + t0, P.settings.ls_armijo, P.ds);
         P.n_launches += 2;
         TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
+        TAD_CUDA_TRY(cudaMemcpyAsync(P.err_h, P.err, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
         TAD_CUDA_TRY(cudaStreamSynchronize(s));
+        // an element error of this step (or of the evaluation before it) first
+        if (*P.err_h != 0) return check_device_error(P);
         if (P.hs->ls_choice == -2) return fail(TAD_ERR_NONFINITE, "Assertion failed: f_new == f_new (NaN energy in line search)");
         if (P.hs->ls_choice >= 0)
         {
@@ -772,7 +820,7 @@ tad_status line_search_device(Problem& P, double* x, const double* d, double f, 
         t0 += nb;
         batch = LS_BATCH;
     }
-    if (f_out) *f_out = f;
+    if (f_out) *f_out = f_on_device ? P.hs->f : f;
     if (trials) *trials = max_iters;
     return TAD_OK;
 }
@@ -786,6 +834,12 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
     for (int i = 0; i < 4; ++i) P.ms_stage[i] = 0.0;
     P.pcg_iters_total = 0;
     P.ls_trials_total = 0;
+    // Without the forcing sequence nothing on the host needs f or |g| before
+    // the line search, so the iteration runs without a host round trip until
+    // the PCG's first check: f stays in ds->f, and the element error word is
+    // read with the line search's scalars (an element error there stops the
+    // iteration before x is updated).
+    const bool forcing = P.settings.forcing == 1;
     double f = 0.0;
     int it = 0;
     for (; it < n_iters; ++it)
@@ -796,31 +850,32 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
         cudaEventRecord(P.ev[1], st);
         s = assemble(P, true, true, prec);
         if (s != TAD_OK) return s;
-        k_neg<<<RED_BLOCKS, RED_THREADS, 0, st>>>(P.n_vars, P.g, P.rhs);
-        k_dot_gg<<<RED_BLOCKS, RED_THREADS, 0, st>>>(P.n_vars, P.g, P.partials, P.counters + 5, P.ds);
-        P.n_launches += 2;
+        k_neg_gg<<<RED_BLOCKS, RED_THREADS, 0, st>>>(P.n_vars, P.g, P.rhs, P.partials, P.counters + 5, P.ds);
+        P.n_launches += 1;
         cudaEventRecord(P.ev[2], st);
-        s = check_device_error(P);
-        if (s != TAD_OK) return s;
-        TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, st));
-        TAD_CUDA_TRY(cudaStreamSynchronize(st));
-        f = P.hs->f;
-        if (f_hist) f_hist[it] = f;
-        const double gnorm = std::sqrt(P.hs->gg);
-        if (P.g0_norm == 0.0) P.g0_norm = gnorm;   // first iteration since create / set_settings
         double tol = P.settings.pcg_rel_tol;
-        if (P.settings.forcing == 1 && P.g0_norm > 0.0)
-            tol = std::max(tol, std::min(0.5, std::sqrt(gnorm / P.g0_norm)));
+        if (forcing)
+        {
+            s = check_device_error(P);
+            if (s != TAD_OK) return s;
+            TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, st));
+            TAD_CUDA_TRY(cudaStreamSynchronize(st));
+            const double gnorm = std::sqrt(P.hs->gg);
+            if (P.g0_norm == 0.0) P.g0_norm = gnorm;   // first iteration since create / set_settings
+            if (P.g0_norm > 0.0) tol = std::max(tol, std::min(0.5, std::sqrt(gnorm / P.g0_norm)));
+        }
         int pit = 0;
         s = pcg_solve(P, P.rhs, P.dx, 0.0, prec, tol, P.settings.pcg_max_iters, &pit);
         P.pcg_iters_total += pit;
         if (s != TAD_OK && s != TAD_ERR_PCG_NOCONV) return s;
         cudaEventRecord(P.ev[3], st);
         bool found = false;
-        double fn = f;
+        double fn = 0.0;
         int trials = 0;
-        s = line_search_device(P, x, P.dx, f, 1.0, &found, &fn, &trials);
+        s = line_search_device(P, x, P.dx, 0.0, 1.0, &found, &fn, &trials, true);
         if (s != TAD_OK) return s;
+        f = P.hs->f;   // the energy at the start of this iteration (ds->f, read with the line search's scalars)
+        if (f_hist) f_hist[it] = f;
         cudaEventRecord(P.ev[4], st);
         TAD_CUDA_TRY(cudaEventSynchronize(P.ev[4]));
         float ms;
@@ -931,9 +986,9 @@ TAD_API tad_status tad_profile_kernels(tad_problem* P, const double* x_d, int re
 #define TAD_PROF(D)                                                                                                  \
     if (prec == TAD_PREC_MIXED)                                                                                     \
     {                                                                                                               \
-        k_diag_inv<D, float><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.diag, (const float*)Q.H, 0.0, Q.dinv32);     \
         k_pcg_init<D, float><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.rhs, Q.dx32, Q.r32, Q.z32, Q.p32, Q.Ap32,    \
-                                                                 Q.dinv32, Q.partials, Q.counters, Q.ds, 1e-30, 1 << 30); \
+                                                                 Q.dinv32, Q.diag, (const float*)Q.H, 0.0,         \
+                                                                 Q.partials, Q.counters, Q.ds, 1e-30, 1 << 30);    \
         ms5[2] = timed([&] { k_pcg_spmv_fused<D, float, SpmvGroup<D>::value><<<PCG_BLOCKS, RED_THREADS, 0, st>>>(   \
                                nh, Q.bptr, Q.bcol, (const float*)Q.H, Q.z32, Q.p32, Q.Ap32, Q.partials,              \
                                Q.counters + 1, Q.ds); });                                                             \
@@ -942,8 +997,8 @@ TAD_API tad_status tad_profile_kernels(tad_problem* P, const double* x_d, int re
     }                                                                                                               \
     else                                                                                                            \
     {                                                                                                               \
-        k_diag_inv<D, double><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.diag, (const double*)Q.H, 0.0, Q.dinv);     \
         k_pcg_init<D, double><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.rhs, Q.dx, Q.r, Q.z, Q.p, Q.Ap, Q.dinv,     \
+                                                                  Q.diag, (const double*)Q.H, 0.0,                  \
                                                                   Q.partials, Q.counters, Q.ds, 1e-30, 1 << 30);    \
         ms5[2] = timed([&] { k_pcg_spmv_fused<D, double, SpmvGroup<D>::value><<<PCG_BLOCKS, RED_THREADS, 0, st>>>(  \
                                nh, Q.bptr, Q.bcol, (const double*)Q.H, Q.z, Q.p, Q.Ap, Q.partials,                   \
