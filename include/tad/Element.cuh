@@ -17,6 +17,7 @@
  */
 #pragma once
 #include <stdint.h>
+#include <type_traits>
 #include "Mat.cuh"
 
 namespace tad {
@@ -37,7 +38,11 @@ __device__ __forceinline__ void report_error(int32_t* err, int32_t bit)
 }
 #endif
 
-template <int d, int N, typename S>
+/* FirstPassive: the first recorded vertex (slot 0) enters as a constant and
+   slot s >= 1 seeds derivative indices (s-1)*d + i, so S has d(N-1)
+   derivatives -- for translation-invariant energies, whose slot-0
+   derivatives follow from the others (lift_translation_invariant). */
+template <int d, int N, typename S, bool FirstPassive = false>
 struct ActiveElement
 {
     using scalar_type = S;
@@ -64,7 +69,7 @@ struct ActiveElement
         if (slot < 0) { report_error(err, DEVERR_UNRECORDED_ACCESS); slot = 0; }
         Vec<S, d> r;
 #pragma unroll
-        for (int i = 0; i < d; ++i) r[i] = S((passive_type)x[(int64_t)d * v + i], slot * d + i);
+        for (int i = 0; i < d; ++i) r[i] = S((passive_type)x[(int64_t)d * v + i], (FirstPassive ? slot - 1 : slot) * d + i);
         return r;
     }
     __device__ S variable(int v) const
@@ -149,6 +154,17 @@ struct RecordElement
 };
 
 /* TINYAD_SCALAR_TYPE(element) of the reference (Element.hh:300-331) */
+/* Energies invariant under a common translation of all their vertices
+   declare `static constexpr bool translation_invariant = true;` (a function
+   of edge vectors / vertex differences only).  The second-order kernels then
+   differentiate with respect to N-1 vertices and recover the first one's
+   derivatives from the invariance, and the PSD projection works on the
+   d(N-1)-dimensional complement of the translations. */
+template <typename E, typename = void> struct IsTranslationInvariant : std::false_type {};
+template <typename E>
+struct IsTranslationInvariant<E, std::void_t<decltype(E::translation_invariant)>>
+    : std::integral_constant<bool, E::translation_invariant> {};
+
 #define TAD_SCALAR_TYPE(element) typename std::decay_t<decltype(element)>::scalar_type
 #define TAD_PASSIVE_TYPE(element) typename std::decay_t<decltype(element)>::passive_type
 #define TAD_ACTIVE_MODE(element) (std::decay_t<decltype(element)>::active_mode)

@@ -200,46 +200,111 @@ __device__ __forceinline__ void packed_to_blocks(const T* h, T* hb)
                 }
 }
 
+/* Translation-invariant energies (IsTranslationInvariant) with N >= 2 are
+   differentiated with respect to slots 1..N-1 only (d(N-1) derivatives,
+   slot 0 passive); the full derivatives follow from E(x + t) = E(x):
+     g_0 = -sum_{s>=1} g_s,  H_0t = -sum_{s>=1} H_st,  H_00 = sum_{s,t>=1} H_st.
+   For a triangle in 2D that is 4 instead of 6 gradient and 10 instead of 21
+   Hessian entries per live intermediate (tetrahedron: 9 / 45 instead of
+   12 / 78), which is most of the evaluation's work and registers. */
+template <typename Energy, int N> struct ReducedDerivatives
+{
+    static constexpr bool value = IsTranslationInvariant<Energy>::value && N >= 2;
+};
+
+template <int d, int N, typename S, typename G, typename T>
+__device__ __forceinline__ void lift_translation_invariant(const S& r, G (&g)[d * N], T (&h)[d * N * (d * N + 1) / 2])
+{
+    constexpr int k = d * N, kr = d * (N - 1);
+#pragma unroll
+    for (int i = 0; i < d; ++i)
+    {
+        G acc = G(0);
+#pragma unroll
+        for (int sl = 1; sl < N; ++sl)
+        {
+            g[sl * d + i] = r.grad[(sl - 1) * d + i];
+            acc = acc + r.grad[(sl - 1) * d + i];
+        }
+        g[i] = -acc;
+    }
+    // C[p][J] = sum_{s>=1} H'((s-1)d + p, J): the slot-0 rows, negated
+    T C[d][kr];
+#pragma unroll
+    for (int p = 0; p < d; ++p)
+#pragma unroll
+        for (int J = 0; J < kr; ++J)
+        {
+            T acc = T(0);
+#pragma unroll
+            for (int sl = 1; sl < N; ++sl) acc += r.H((sl - 1) * d + p, J);
+            C[p][J] = acc;
+        }
+#pragma unroll
+    for (int I = 0; I < k; ++I)
+#pragma unroll
+        for (int J = I; J < k; ++J)
+        {
+            const int a = I / d, p = I % d, b = J / d, q = J % d;
+            T v;
+            if (a >= 1) v = r.H(I - d, J - d);
+            else if (b >= 1) v = -C[p][J - d];
+            else
+            {
+                v = T(0);
+#pragma unroll
+                for (int t = 1; t < N; ++t) v += C[p][(t - 1) * d + q];
+            }
+            h[packed_index(I, J, k)] = v;
+        }
+}
+
+/* Minimum resident 128-thread blocks per SM for k_elem_hessian: 4 (<= 128
+   registers) for the FP32-Hessian kernels up to k = 8 -- the reduced k = 6
+   mixed kernel needs 168 registers unbounded, spills 72 B at 128, and
+   measured 4.7 % faster at the higher occupancy (1.64M-face disk); no bound
+   otherwise. */
+template <int k, typename T> struct ElemHessianMinBlocks { static constexpr int value = (k <= 8 && sizeof(T) == 4) ? 4 : 1; };
+
 template <int d, int N, typename T, typename Energy>
-__global__ void __launch_bounds__(128) k_elem_hessian(ElemLaunch L, Energy energy)
+__global__ void __launch_bounds__(128, ElemHessianMinBlocks<d * N, T>::value) k_elem_hessian(ElemLaunch L, Energy energy)
 {
     constexpr int k = d * N;
     constexpr int NP = N * (N + 1) / 2;
-    using S = Scalar<k, T, true, typename ValOf<T, k>::type, typename GradOf<T, k>::type>;
+    constexpr bool reduced = ReducedDerivatives<Energy, N>::value;
+    constexpr int kd = reduced ? d * (N - 1) : k;
+    using G = typename GradOf<T, kd>::type;
+    using S = Scalar<kd, T, true, typename ValOf<T, k>::type, G>;
     const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (e >= L.n_elem) return;
-    ActiveElement<d, N, S> el;
+    ActiveElement<d, N, S, reduced> el;
     el.handle = e;
     el.x = L.x;
     el.err = L.err;
 #pragma unroll
     for (int i = 0; i < N; ++i) el.vh[i] = L.rec[e * N + i];
-    S r = energy(el);
-    if (FusedProjection<k>::value && L.project) project_or_defer<d, N, T>(L, e, r.hess, (T)L.eps);
+    const S r = energy(el);
+    G gf[k];
+    T hf[k * (k + 1) / 2];
+    if constexpr (reduced) lift_translation_invariant<d, N>(r, gf, hf);
+    else
+    {
+#pragma unroll
+        for (int i = 0; i < k; ++i) gf[i] = r.grad[i];
+#pragma unroll
+        for (int i = 0; i < k * (k + 1) / 2; ++i) hf[i] = r.hess[i];
+    }
+    if (FusedProjection<k>::value && L.project) project_or_defer<d, N, T>(L, e, hf, (T)L.eps);
     L.out_f[e] = (double)r.val;
     bool fin = true;
     double gv[k];
 #pragma unroll
-    for (int i = 0; i < k; ++i) { gv[i] = (double)r.grad[i]; fin = fin && finite_val(gv[i]); }
+    for (int i = 0; i < k; ++i) { gv[i] = (double)gf[i]; fin = fin && finite_val(gv[i]); }
     store_row<double, k>((double*)L.out_g, e, gv);
     T hb[NP * d * d];
+    packed_to_blocks<d, N, T>(hf, hb);
 #pragma unroll
-    for (int a = 0; a < N; ++a)
-#pragma unroll
-        for (int b = a; b < N; ++b)
-        {
-            const int pr = packed_index(a, b, N);
-#pragma unroll
-            for (int p = 0; p < d; ++p)
-#pragma unroll
-                for (int q = 0; q < d; ++q)
-                {
-                    const int i = a * d + p, j = b * d + q;
-                    const T v = (i <= j) ? r.hess[packed_index(i, j, k)] : r.hess[packed_index(j, i, k)];
-                    fin = fin && finite_val(v);
-                    hb[pr * d * d + p * d + q] = v;
-                }
-        }
+    for (int i = 0; i < NP * d * d; ++i) fin = fin && finite_val(hb[i]);
     store_row<T, NP * d * d>((T*)L.out_H, e, hb);
     if (!fin) report_error(L.err, DEVERR_NONFINITE);
 }

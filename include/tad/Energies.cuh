@@ -27,6 +27,7 @@ namespace tad {
 struct SymmetricDirichletTri
 {
     static constexpr int d = 2, N = 3, n_params = 5;
+    static constexpr bool translation_invariant = true;   // a function of edge vectors
     const int32_t* vtx;
     const double* prm;
 
@@ -51,6 +52,7 @@ struct SymmetricDirichletTri
 struct SymmetricDirichletTet
 {
     static constexpr int d = 3, N = 4, n_params = 10;
+    static constexpr bool translation_invariant = true;   // a function of edge vectors
     const int32_t* vtx;
     const double* prm;
 
@@ -136,6 +138,7 @@ template <int D>
 struct DirichletTri
 {
     static constexpr int d = D, N = 3, n_params = 1;
+    static constexpr bool translation_invariant = true;   // a function of edge vectors
     const int32_t* vtx;
     const double* prm;
 

@@ -222,9 +222,11 @@ TAD_HD constexpr double helmert(int a, int m)
 
 /* Row-sum tolerance (relative to max |H_ij|) below which an element Hessian
    counts as translation invariant: a few hundred rounding units of the
-   evaluation precision. */
-template <typename T> struct TranslationTol { static constexpr double value = 256.0 * 2.220446049250313e-16; };
-template <> struct TranslationTol<float> { static constexpr double value = 256.0 * 1.1920928955078125e-07; };
+   evaluation precision (4-byte types: FP32, else FP64). */
+template <typename T> struct TranslationTol
+{
+    static constexpr double value = 256.0 * (sizeof(T) == 4 ? 1.1920928955078125e-07 : 2.220446049250313e-16);
+};
 
 /* Projection of the packed Hessian hp of an element with N vertices of d
    coordinates (variable a*d+p = coordinate p of vertex a), with the result of

@@ -3,5 +3,5 @@
 set -e
 HERE="$(cd "$(dirname "$0")" && pwd)"
 mkdir -p "$HERE/_build"
-g++ -std=c++17 -O1 -o "$HERE/_build/flop_count" "$HERE/flop_count.cpp"
+g++ -std=c++17 -O1 -I "$HERE/../include" -o "$HERE/_build/flop_count" "$HERE/flop_count.cpp"
 "$HERE/_build/flop_count"

@@ -95,12 +95,29 @@ __global__ void k_assemble_grad(int64_t nh, const int32_t* __restrict__ gptr, co
     double acc[d];
 #pragma unroll
     for (int p = 0; p < d; ++p) acc[p] = 0.0;
-    const int32_t q1 = gptr[u + 1];
-    for (int32_t q = gptr[u]; q < q1; ++q)
+    // slots in batches of GATHER (ids, then values, loaded together), summed in order
+    constexpr int GATHER = 4;
+    const int32_t q0 = gptr[u], q1 = gptr[u + 1];
+    for (int32_t q = q0; q < q1; q += GATHER)
     {
-        const int64_t s = gidx[q];
+        int64_t sl[GATHER];
 #pragma unroll
-        for (int p = 0; p < d; ++p) acc[p] += eg[s * d + p];
+        for (int j = 0; j < GATHER; ++j) sl[j] = (q + j < q1) ? gidx[q + j] : 0;
+        double v[GATHER][d];
+#pragma unroll
+        for (int j = 0; j < GATHER; ++j)
+            if (q + j < q1)
+            {
+#pragma unroll
+                for (int p = 0; p < d; ++p) v[j][p] = eg[sl[j] * d + p];
+            }
+#pragma unroll
+        for (int j = 0; j < GATHER; ++j)
+        {
+            if (q + j >= q1) break;
+#pragma unroll
+            for (int p = 0; p < d; ++p) acc[p] += v[j][p];
+        }
     }
 #pragma unroll
     for (int p = 0; p < d; ++p) g[u * d + p] = acc[p];
@@ -126,23 +143,35 @@ __global__ void k_assemble_hess(int64_t nb, const int32_t* __restrict__ cptr, co
     T acc[d * d];
 #pragma unroll
     for (int i = 0; i < d * d; ++i) acc[i] = T(0);
-    const int32_t q1 = cptr[b + 1];
-    for (int32_t q = cptr[b]; q < q1; ++q)
+    // contributions in batches of GATHER: the ids, then the blocks, are loaded
+    // together (independent loads in flight), then summed in order
+    constexpr int GATHER = 4;
+    const int32_t q0 = cptr[b], q1 = cptr[b + 1];
+    for (int32_t q = q0; q < q1; q += GATHER)
     {
-        const int32_t c = cidx[q];
-        T v[d * d];
-        tad::load_row<T, d * d>(eH, (int64_t)(c & 0x7fffffff), v);   // one 16-byte load per 2x2 FP32 block
-        if (c < 0)
+        int32_t c[GATHER];
+#pragma unroll
+        for (int j = 0; j < GATHER; ++j) c[j] = (q + j < q1) ? cidx[q + j] : 0;
+        T v[GATHER][d * d];
+#pragma unroll
+        for (int j = 0; j < GATHER; ++j)
+            if (q + j < q1) tad::load_row<T, d * d>(eH, (int64_t)(c[j] & 0x7fffffff), v[j]);   // one 16-byte load per 2x2 FP32 block
+#pragma unroll
+        for (int j = 0; j < GATHER; ++j)
         {
+            if (q + j >= q1) break;
+            if (c[j] < 0)
+            {
 #pragma unroll
-            for (int p = 0; p < d; ++p)
+                for (int p = 0; p < d; ++p)
 #pragma unroll
-                for (int r = 0; r < d; ++r) acc[p * d + r] += v[r * d + p];
-        }
-        else
-        {
+                    for (int r = 0; r < d; ++r) acc[p * d + r] += v[j][r * d + p];
+            }
+            else
+            {
 #pragma unroll
-            for (int i = 0; i < d * d; ++i) acc[i] += v[i];
+                for (int i = 0; i < d * d; ++i) acc[i] += v[j][i];
+            }
         }
     }
     tad::store_row<T, d * d>(H, b, acc);

@@ -633,13 +633,15 @@ static tad_status pcg_dispatch(Problem& P, const double* b, double* xsol, int pr
     // tolerance by itself -- its recursively updated residual drifts from the
     // true one by O(eps_fp32 cond(H)) relative, far below 1e-4 -- so that pass
     // is the answer; tighter tolerances compute r = b - H x in FP64 and solve
-    // for corrections until the FP64 residual meets them.  A pass that does
-    // not halve the FP64 residual norm -- FP32 CG on a nearly singular H (the
-    // eps-regularised rigid motions of an unconstrained mesh) stalls or
-    // diverges at tight tolerances -- is undone, and the rest is solved in
-    // FP64 on an FP64 copy of the FP32 Hessian (same matrix, so the result is
-    // still exact to the FP32-evaluated Hessian).
+    // for corrections until the FP64 residual meets them.  FP32 CG on a nearly
+    // singular H (the eps-regularised rigid motions of an unconstrained mesh)
+    // stalls or diverges at tight tolerances: a pass that increases the FP64
+    // residual is undone, and once a pass reduces its norm by less than
+    // MIN_PASS_GAIN (or the passes run out) the rest is solved in FP64 on an
+    // FP64 copy of the FP32 Hessian (same matrix, so the result is still exact
+    // to the FP32-evaluated Hessian).
     constexpr double LOOSE_TOL = 1e-4;
+    constexpr double MIN_PASS_GAIN = 100.0;
     const double tol = P.settings.refine_rel_tol;
     const double inner_tol = std::max(rel_tol, 1e-6);
     int total = 0;
@@ -665,9 +667,9 @@ static tad_status pcg_dispatch(Problem& P, const double* b, double* xsol, int pr
         TAD_CUDA_TRY(cudaStreamSynchronize(s));
         const double rr = P.hs->rr;
         if (rr <= target * target * bb || total >= max_iters) break;
-        if (!(rr <= 0.25 * rr_prev))
+        if (!(rr < rr_prev))
         {
-            // the last FP32 pass did not halve the residual: undo it, finish in FP64
+            // the last FP32 pass made the residual worse: undo it, finish in FP64
             k_to_double<float><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, P.dx32, xsol, -1);
             k_residual<d, float><<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_handles, P.bptr, P.bcol, (const float*)P.H, 0.0, xsol, b,
                                                                     P.res, P.partials, P.counters + 3, P.ds);
@@ -675,7 +677,13 @@ static tad_status pcg_dispatch(Problem& P, const double* b, double* xsol, int pr
             completion = true;
             break;
         }
-        if (pass + 1 >= passes) break;
+        if (!(rr <= rr_prev / (MIN_PASS_GAIN * MIN_PASS_GAIN)) || pass + 1 >= passes)
+        {
+            // FP32 passes are not effective here (or none are left): keep this
+            // one, finish in FP64 from the residual just computed
+            completion = true;
+            break;
+        }
         rr_prev = rr;
         int it = 0;
         st = pcg_core<d, float>(P, P.res, P.dx32, 0.0, inner_tol, max_iters - total, &it, P.r32, P.z32, P.p32, P.Ap32, P.dinv32, 1);
