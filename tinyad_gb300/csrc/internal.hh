@@ -72,6 +72,7 @@ struct Term
 struct DevScalars
 {
     double f;            // energy at x
+    double f_prev;       // energy before an adopted line-search step (k_ls_select)
     double f_trial[LS_BATCH];
     double dg;           // d . g
     double alpha, beta, rz, rz_new, rr, bb, pAp;
@@ -150,6 +151,7 @@ struct Problem
     double *r = nullptr, *z = nullptr, *p = nullptr, *Ap = nullptr, *dx = nullptr, *dinv = nullptr;
     float *r32 = nullptr, *z32 = nullptr, *p32 = nullptr, *Ap32 = nullptr, *dx32 = nullptr, *dinv32 = nullptr;
     double *rhs = nullptr, *res = nullptr;
+    double* x_trial = nullptr;   // Newton: the speculative full-step state x + d (n_vars, allocated on first use)
     double* steps = nullptr;   // LS_BATCH trial step sizes (device)
     double* steps_seq = nullptr;   // the line search's whole step sequence (device), for steps_key
     int steps_seq_cap = 0;
@@ -200,13 +202,15 @@ tad_status launch_builtin_misc(Problem& P, Term& T, const tad_term_eval_args& a)
 tad_status eval_elements(Problem& P, int mode, const double* x, double eps, int precision,
                          const double* dir = nullptr, int n_steps = 0);
 /* assemble element buffers -> f (device scalar ds->f), g, H */
-tad_status assemble(Problem& P, bool gradient, bool hessian, int precision);
+/* f (into f_dst, default ds->f), gradient and Hessian from the element buffers */
+tad_status assemble(Problem& P, bool gradient, bool hessian, int precision, double* f_dst = nullptr);
 /* full f/g/H evaluation at device x */
 tad_status eval_full(Problem& P, const double* x, int mode, double eps, int precision);
 
 // ---- kernels (kernels.cu)
 void launch_reduce_f(Problem& P, int n_rows, double* out);      // sums ef rows into out[row]
-void launch_assemble_grad(Problem& P);
+/* g from the element gradient slots, in element order; mixed precision sums in double-float */
+void launch_assemble_grad(Problem& P, int precision = TAD_PREC_FP64);
 void launch_assemble_hess(Problem& P, int precision);
 void launch_bsr_to_csr(Problem& P, double* out, int precision);
 void launch_zero(double* p, int64_t n, cudaStream_t s);
@@ -219,9 +223,10 @@ void amg_free(Problem& P);
 int amg_levels(const Problem& P);
 tad_status pcg_solve(Problem& P, const double* b, double* xsol, double w_identity, int precision,
                      double rel_tol, int max_iters, int* iters_out);
-/* f_on_device: the energy at x is already in ds->f (f is then ignored) */
+/* f_on_device: the energy at x is already in ds->f (f is then ignored);
+   t_start > 0 resumes the trial sequence there with ds->dg already set */
 tad_status line_search_device(Problem& P, double* x, const double* d, double f, double s_max,
-                              bool* found, double* f_out, int* trials, bool f_on_device = false);
+                              bool* found, double* f_out, int* trials, bool f_on_device = false, int t_start = 0);
 tad_status newton_solve(Problem& P, double* x_d, int n_iters, double eps, double stop_decrement,
                         double* f_hist, int* iters_done);
 

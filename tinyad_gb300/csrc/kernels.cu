@@ -18,6 +18,7 @@
  */
 #include "internal.hh"
 #include "../../include/tad/RowIO.cuh"
+#include "../../include/tad/Scalar.cuh"
 
 namespace tadlib {
 
@@ -86,15 +87,19 @@ void launch_reduce_f(Problem& P, int n_rows, double* out)
     k_reduce_rows<<<grid, RED_THREADS, 0, P.stream>>>(P.ef, n, n, P.partials, P.counters, out);
 }
 
-template <int d>
+/* Acc = double (FP64 path) or tad::DoubleFloatValue (mixed: the double slot
+   values are split bit-wise and summed on the FP32 pipe, ~48-bit, the
+   precision of the mixed element gradients; FP64 adds bound this gather
+   otherwise) */
+template <int d, typename Acc>
 __global__ void k_assemble_grad(int64_t nh, const int32_t* __restrict__ gptr, const int32_t* __restrict__ gidx,
                                 const double* __restrict__ eg, double* __restrict__ g)
 {
     const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (u >= nh) return;
-    double acc[d];
+    Acc acc[d];
 #pragma unroll
-    for (int p = 0; p < d; ++p) acc[p] = 0.0;
+    for (int p = 0; p < d; ++p) acc[p] = Acc(0.0);
     // slots in batches of GATHER (ids, then values, loaded together), summed in order
     constexpr int GATHER = 4;
     const int32_t q0 = gptr[u], q1 = gptr[u + 1];
@@ -116,22 +121,29 @@ __global__ void k_assemble_grad(int64_t nh, const int32_t* __restrict__ gptr, co
         {
             if (q + j >= q1) break;
 #pragma unroll
-            for (int p = 0; p < d; ++p) acc[p] += v[j][p];
+            for (int p = 0; p < d; ++p) acc[p] = acc[p] + Acc(v[j][p]);
         }
     }
 #pragma unroll
-    for (int p = 0; p < d; ++p) g[u * d + p] = acc[p];
+    for (int p = 0; p < d; ++p) g[u * d + p] = (double)acc[p];
 }
 
-void launch_assemble_grad(Problem& P)
+template <typename Acc>
+static void assemble_grad_as(Problem& P)
 {
     const unsigned grid = (unsigned)((P.n_handles + 255) / 256);
     switch (P.d)
     {
-    case 1: k_assemble_grad<1><<<grid, 256, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g); break;
-    case 2: k_assemble_grad<2><<<grid, 256, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g); break;
-    default: k_assemble_grad<3><<<grid, 256, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g); break;
+    case 1: k_assemble_grad<1, Acc><<<grid, 256, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g); break;
+    case 2: k_assemble_grad<2, Acc><<<grid, 256, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g); break;
+    default: k_assemble_grad<3, Acc><<<grid, 256, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g); break;
     }
+}
+
+void launch_assemble_grad(Problem& P, int precision)
+{
+    if (precision == TAD_PREC_MIXED) assemble_grad_as<tad::DoubleFloatValue>(P);
+    else assemble_grad_as<double>(P);
 }
 
 template <int d, typename T>

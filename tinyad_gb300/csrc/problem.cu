@@ -322,10 +322,10 @@ tad_status eval_elements(Problem& P, int mode, const double* x, double eps, int 
     return TAD_OK;
 }
 
-tad_status assemble(Problem& P, bool gradient, bool hessian, int precision)
+tad_status assemble(Problem& P, bool gradient, bool hessian, int precision, double* f_dst)
 {
-    launch_reduce_f(P, 1, &P.ds->f);
-    if (gradient) launch_assemble_grad(P);
+    launch_reduce_f(P, 1, f_dst ? f_dst : &P.ds->f);
+    if (gradient) launch_assemble_grad(P, precision);
     if (hessian) launch_assemble_hess(P, precision);
     P.n_launches += 1 + (gradient ? 1 : 0) + (hessian ? 1 : 0);
     TAD_CUDA_TRY(cudaGetLastError());
@@ -413,7 +413,7 @@ TAD_API tad_status tad_problem_destroy(tad_problem* P)
     void* bufs[] = {P->ef, P->eg, P->eH, P->bptr, P->bcol, P->diag, P->cptr, P->cidx, P->gptr, P->gidx,
                     P->x, P->g, P->H, P->H64, P->csr_tmp, P->r, P->z, P->p, P->Ap, P->dx, P->dinv,
                     P->r32, P->z32, P->p32, P->Ap32, P->dx32, P->dinv32, P->rhs, P->res, P->steps,
-                    P->partials, P->counters, P->ds, P->err, P->proj_list, P->steps_seq};
+                    P->partials, P->counters, P->ds, P->err, P->proj_list, P->steps_seq, P->x_trial};
     for (void* b : bufs) dfree(b);
     if (P->hs) cudaFreeHost(P->hs);
     if (P->err_h) cudaFreeHost(P->err_h);

@@ -386,7 +386,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_neg_gg(int64_t n, const double*
 }
 
 /* first trial j (of n) with f_trial[j] <= f + c s_j dg (LineSearch.hh:14-24, :53) */
-__global__ void k_ls_select(int n, const double* __restrict__ steps, double c, DevScalars* ds)
+__global__ void k_ls_select(int n, const double* __restrict__ steps, double c, DevScalars* ds, int adopt = 0)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     ds->ls_choice = -1;
@@ -399,9 +399,16 @@ __global__ void k_ls_select(int n, const double* __restrict__ steps, double c, D
             ds->ls_choice = j;
             ds->ls_f = fn;
             ds->ls_s = steps[j];
+            if (adopt) { ds->f_prev = ds->f; ds->f = fn; }   // the accepted point becomes the current one
             return;
         }
     }
+}
+
+/* out = a + b */
+__global__ void k_add(int64_t n, const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ out)
+{
+    GRID_STRIDE(i, n) out[i] = a[i] + b[i];
 }
 
 __global__ void k_axpy_ds(int64_t n, double* __restrict__ x, const double* __restrict__ dx, const DevScalars* ds)
@@ -786,19 +793,22 @@ static tad_status ensure_step_sequence(Problem& P, double s_max, int n)
 }
 
 tad_status line_search_device(Problem& P, double* x, const double* d, double f, double s_max, bool* found,
-                              double* f_out, int* trials, bool f_on_device)
+                              double* f_out, int* trials, bool f_on_device, int t_start)
 {
     cudaStream_t s = P.stream;
     const int max_iters = P.settings.ls_max_iters > 0 ? P.settings.ls_max_iters : 64;
     tad_status st = ensure_step_sequence(P, s_max, max_iters);
     if (st != TAD_OK) return st;
-    k_dot_dg<<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_vars, d, P.g, P.partials, P.counters + 4, P.ds);
-    P.n_launches += 1;
+    if (t_start == 0)
+    {
+        k_dot_dg<<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_vars, d, P.g, P.partials, P.counters + 4, P.ds);
+        P.n_launches += 1;
+    }
     // current energy: ds->f, from the caller unless it is already there
     if (!f_on_device) TAD_CUDA_TRY(cudaMemcpyAsync(&P.ds->f, &f, sizeof(double), cudaMemcpyHostToDevice, s));
     *found = false;
-    int t0 = 0;
-    int batch = 1;
+    int t0 = t_start;
+    int batch = t_start == 0 ? 1 : LS_BATCH;
     while (t0 < max_iters)
     {
         const int nb = std::min(batch, max_iters - t0);
@@ -833,6 +843,30 @@ tad_status line_search_device(Problem& P, double* x, const double* d, double f, 
     return TAD_OK;
 }
 
+/* The first line-search trial (s = 1) evaluated as the next iteration's
+   derivatives: x_t = x + d, the full element kernels and assembly at x_t,
+   the trial energy into f_trial[0] and the Armijo test (which makes it the
+   current energy if it passes).  Returns the selection in P.hs after one
+   host round trip; the caller adopts x_t (its derivatives are then already
+   assembled) or continues the line search at trial 2. */
+static tad_status speculative_first_trial(Problem& P, const double* x, const double* d, double* xt, double eps)
+{
+    cudaStream_t s = P.stream;
+    k_dot_dg<<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_vars, d, P.g, P.partials, P.counters + 4, P.ds);
+    k_add<<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_vars, x, d, xt);
+    P.n_launches += 2;
+    tad_status st = eval_elements(P, TAD_MODE_HESSIAN_PROJ, xt, eps, P.precision);
+    if (st != TAD_OK) return st;
+    st = assemble(P, true, true, P.precision, P.ds->f_trial);
+    if (st != TAD_OK) return st;
+    k_ls_select<<<1, 32, 0, s>>>(1, P.steps_seq, P.settings.ls_armijo, P.ds, 1);
+    P.n_launches += 1;
+    TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
+    TAD_CUDA_TRY(cudaMemcpyAsync(P.err_h, P.err, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    TAD_CUDA_TRY(cudaStreamSynchronize(s));
+    return TAD_OK;
+}
+
 tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double stop_decrement, double* f_hist, int* iters_done)
 {
     tad_status s = ensure_finalized(P);
@@ -847,17 +881,46 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
     // the PCG's first check: f stays in ds->f, and the element error word is
     // read with the line search's scalars (an element error there stops the
     // iteration before x is updated).
+    //
+    // The full step s = 1 is tried first and is accepted in almost every
+    // iteration of a Newton solve; its energy is then evaluated by the full
+    // element kernels at x + d, which are the next iteration's derivatives
+    // (speculative_first_trial).  A rejection falls back to the energy-only
+    // line search from trial 2, with the same trial sequence and Armijo test,
+    // and turns the speculation off until a full step is accepted again.  The
+    // last iteration of a call does not speculate (its derivatives would be
+    // discarded).  The accepted state alternates between x and P.x_trial; x
+    // holds it on return.
     const bool forcing = P.settings.forcing == 1;
+    const int ls_max = P.settings.ls_max_iters > 0 ? P.settings.ls_max_iters : 64;
+    if (!P.x_trial) TAD_CUDA_TRY(cudaMalloc(&P.x_trial, std::max<int64_t>(P.n_vars, 1) * sizeof(double)));
+    s = ensure_step_sequence(P, 1.0, ls_max);
+    if (s != TAD_OK) return s;
+    double* cur = x;
+    double* spare = P.x_trial;
+    auto finish = [&](tad_status rs) {
+        if (cur != x) cudaMemcpyAsync(x, cur, P.n_vars * sizeof(double), cudaMemcpyDeviceToDevice, st);
+        cudaStreamSynchronize(st);
+        return rs;
+    };
+    bool have_derivs = false;   // derivatives at cur already assembled (accepted speculative step)
+    bool speculate = true;
     double f = 0.0;
     int it = 0;
     for (; it < n_iters; ++it)
     {
         cudaEventRecord(P.ev[0], st);
-        s = eval_elements(P, TAD_MODE_HESSIAN_PROJ, x, eps, prec);
-        if (s != TAD_OK) return s;
+        if (!have_derivs)
+        {
+            s = eval_elements(P, TAD_MODE_HESSIAN_PROJ, cur, eps, prec);
+            if (s != TAD_OK) return finish(s);
+        }
         cudaEventRecord(P.ev[1], st);
-        s = assemble(P, true, true, prec);
-        if (s != TAD_OK) return s;
+        if (!have_derivs)
+        {
+            s = assemble(P, true, true, prec);
+            if (s != TAD_OK) return finish(s);
+        }
         k_neg_gg<<<RED_BLOCKS, RED_THREADS, 0, st>>>(P.n_vars, P.g, P.rhs, P.partials, P.counters + 5, P.ds);
         P.n_launches += 1;
         cudaEventRecord(P.ev[2], st);
@@ -865,7 +928,7 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
         if (forcing)
         {
             s = check_device_error(P);
-            if (s != TAD_OK) return s;
+            if (s != TAD_OK) return finish(s);
             TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, st));
             TAD_CUDA_TRY(cudaStreamSynchronize(st));
             const double gnorm = std::sqrt(P.hs->gg);
@@ -875,14 +938,47 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
         int pit = 0;
         s = pcg_solve(P, P.rhs, P.dx, 0.0, prec, tol, P.settings.pcg_max_iters, &pit);
         P.pcg_iters_total += pit;
-        if (s != TAD_OK && s != TAD_ERR_PCG_NOCONV) return s;
+        if (s != TAD_OK && s != TAD_ERR_PCG_NOCONV) return finish(s);
         cudaEventRecord(P.ev[3], st);
         bool found = false;
         double fn = 0.0;
         int trials = 0;
-        s = line_search_device(P, x, P.dx, 0.0, 1.0, &found, &fn, &trials, true);
-        if (s != TAD_OK) return s;
-        f = P.hs->f;   // the energy at the start of this iteration (ds->f, read with the line search's scalars)
+        have_derivs = false;
+        if (speculate && it + 1 < n_iters)   // the last iteration has no next one to evaluate for
+        {
+            s = speculative_first_trial(P, cur, P.dx, spare, eps);
+            if (s != TAD_OK) return finish(s);
+            const int choice = P.hs->ls_choice;
+            if (choice == -2)
+                return finish(fail(TAD_ERR_NONFINITE, "Assertion failed: f_new == f_new (NaN energy in line search)"));
+            if (choice == 0)
+            {
+                // accepted: x + d is the new state, its derivatives are assembled
+                std::swap(cur, spare);
+                have_derivs = true;
+                found = true;
+                fn = P.hs->ls_f;
+                trials = 1;
+                if (*P.err_h != 0) return finish(check_device_error(P));   // as the next evaluation would report
+            }
+            else
+            {
+                // rejected: derivatives at x + d are not needed (clear what they reported)
+                if (*P.err_h != 0) TAD_CUDA_TRY(cudaMemsetAsync(P.err, 0, sizeof(int32_t), st));
+                s = line_search_device(P, cur, P.dx, 0.0, 1.0, &found, &fn, &trials, true, 1);
+                if (s != TAD_OK) return finish(s);
+                speculate = false;
+            }
+        }
+        else
+        {
+            s = line_search_device(P, cur, P.dx, 0.0, 1.0, &found, &fn, &trials, true);
+            if (s != TAD_OK) return finish(s);
+            speculate = found && trials == 1;
+        }
+        // the energy at the start of this iteration (ds->f, or what an accepted
+        // speculative step replaced there)
+        f = have_derivs ? P.hs->f_prev : P.hs->f;
         if (f_hist) f_hist[it] = f;
         cudaEventRecord(P.ev[4], st);
         TAD_CUDA_TRY(cudaEventSynchronize(P.ev[4]));
@@ -898,7 +994,7 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
     }
     if (f_hist) f_hist[it] = f;
     if (iters_done) *iters_done = it;
-    return TAD_OK;
+    return finish(TAD_OK);
 }
 
 } // namespace tadlib
@@ -989,7 +1085,7 @@ TAD_API tad_status tad_profile_kernels(tad_problem* P, const double* x_d, int re
         return (double)ms / reps;
     };
     ms5[0] = timed([&] { eval_elements(Q, TAD_MODE_HESSIAN_PROJ, x_d, 1e-9, prec); });
-    ms5[1] = timed([&] { launch_assemble_grad(Q); launch_assemble_hess(Q, prec); });
+    ms5[1] = timed([&] { launch_assemble_grad(Q, prec); launch_assemble_hess(Q, prec); });
     const int64_t nh = Q.n_handles, n = Q.n_vars;
 #define TAD_PROF(D)                                                                                                  \
     if (prec == TAD_PREC_MIXED)                                                                                     \
