@@ -152,6 +152,8 @@ struct Problem
     float *r32 = nullptr, *z32 = nullptr, *p32 = nullptr, *Ap32 = nullptr, *dx32 = nullptr, *dinv32 = nullptr;
     double *rhs = nullptr, *res = nullptr;
     double* x_trial = nullptr;   // Newton: the speculative full-step state x + d (n_vars, allocated on first use)
+    bool defer_fp32 = false;     // Newton asks a loose mixed solve to leave its solution in dx32 ...
+    bool solution_in_dx32 = false;   // ... and the solve says it did (P.dx not written)
     double* steps = nullptr;   // LS_BATCH trial step sizes (device)
     double* steps_seq = nullptr;   // the line search's whole step sequence (device), for steps_key
     int steps_seq_cap = 0;
@@ -202,8 +204,9 @@ tad_status launch_builtin_misc(Problem& P, Term& T, const tad_term_eval_args& a)
 tad_status eval_elements(Problem& P, int mode, const double* x, double eps, int precision,
                          const double* dir = nullptr, int n_steps = 0);
 /* assemble element buffers -> f (device scalar ds->f), g, H */
-/* f (into f_dst, default ds->f), gradient and Hessian from the element buffers */
-tad_status assemble(Problem& P, bool gradient, bool hessian, int precision, double* f_dst = nullptr);
+/* f (into f_dst, default ds->f), gradient and Hessian from the element
+   buffers; newton_rhs: the gradient assembly also writes rhs = -g and ds->gg */
+tad_status assemble(Problem& P, bool gradient, bool hessian, int precision, double* f_dst = nullptr, bool newton_rhs = false);
 /* full f/g/H evaluation at device x */
 tad_status eval_full(Problem& P, const double* x, int mode, double eps, int precision);
 
@@ -211,6 +214,8 @@ tad_status eval_full(Problem& P, const double* x, int mode, double eps, int prec
 void launch_reduce_f(Problem& P, int n_rows, double* out);      // sums ef rows into out[row]
 /* g from the element gradient slots, in element order; mixed precision sums in double-float */
 void launch_assemble_grad(Problem& P, int precision = TAD_PREC_FP64);
+/* the same, also rhs = -g and ds->gg = g.g (Newton right-hand side) */
+void launch_assemble_grad_newton(Problem& P, int precision);
 void launch_assemble_hess(Problem& P, int precision);
 void launch_bsr_to_csr(Problem& P, double* out, int precision);
 void launch_zero(double* p, int64_t n, cudaStream_t s);

@@ -17,6 +17,7 @@
  *                     from the BSR blocks, for the host-facing Hessian.
  */
 #include "internal.hh"
+#include "grid_reduce.cuh"
 #include "../../include/tad/RowIO.cuh"
 #include "../../include/tad/Scalar.cuh"
 
@@ -87,20 +88,19 @@ void launch_reduce_f(Problem& P, int n_rows, double* out)
     k_reduce_rows<<<grid, RED_THREADS, 0, P.stream>>>(P.ef, n, n, P.partials, P.counters, out);
 }
 
-/* Acc = double (FP64 path) or tad::DoubleFloatValue (mixed: the double slot
-   values are split bit-wise and summed on the FP32 pipe, ~48-bit, the
-   precision of the mixed element gradients; FP64 adds bound this gather
-   otherwise) */
+/* g[u] = sum of handle u's element gradient slots, in element order.  Acc =
+   double (FP64 path) or tad::DoubleFloatValue (mixed: the double slot values
+   are split bit-wise and summed on the FP32 pipe, ~48-bit, the precision of
+   the mixed element gradients; FP64 adds bound this gather otherwise).
+   Slots are gathered in batches of GATHER (ids, then values, loaded
+   together) and summed in order. */
 template <int d, typename Acc>
-__global__ void k_assemble_grad(int64_t nh, const int32_t* __restrict__ gptr, const int32_t* __restrict__ gidx,
-                                const double* __restrict__ eg, double* __restrict__ g)
+__device__ __forceinline__ void gather_gradient(int64_t u, const int32_t* __restrict__ gptr, const int32_t* __restrict__ gidx,
+                                                const double* __restrict__ eg, double (&out)[d])
 {
-    const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (u >= nh) return;
     Acc acc[d];
 #pragma unroll
     for (int p = 0; p < d; ++p) acc[p] = Acc(0.0);
-    // slots in batches of GATHER (ids, then values, loaded together), summed in order
     constexpr int GATHER = 4;
     const int32_t q0 = gptr[u], q1 = gptr[u + 1];
     for (int32_t q = q0; q < q1; q += GATHER)
@@ -125,7 +125,46 @@ __global__ void k_assemble_grad(int64_t nh, const int32_t* __restrict__ gptr, co
         }
     }
 #pragma unroll
-    for (int p = 0; p < d; ++p) g[u * d + p] = (double)acc[p];
+    for (int p = 0; p < d; ++p) out[p] = (double)acc[p];
+}
+
+template <int d, typename Acc>
+__global__ void k_assemble_grad(int64_t nh, const int32_t* __restrict__ gptr, const int32_t* __restrict__ gidx,
+                                const double* __restrict__ eg, double* __restrict__ g)
+{
+    const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (u >= nh) return;
+    double gv[d];
+    gather_gradient<d, Acc>(u, gptr, gidx, eg, gv);
+#pragma unroll
+    for (int p = 0; p < d; ++p) g[u * d + p] = gv[p];
+}
+
+/* The Newton variant: also rhs = -g and g.g (the PCG right-hand side and
+   |g|^2), grid-stride over a capped grid for the fixed-order grid sum */
+template <int d, typename Acc>
+__global__ void __launch_bounds__(RED_THREADS) k_assemble_grad_newton(int64_t nh, const int32_t* __restrict__ gptr,
+                                                                       const int32_t* __restrict__ gidx,
+                                                                       const double* __restrict__ eg, double* __restrict__ g,
+                                                                       double* __restrict__ rhs, double* partials,
+                                                                       unsigned* counter, DevScalars* ds)
+{
+    double part[1] = {0.0};
+    GRID_STRIDE(u, nh)
+    {
+        double gv[d];
+        gather_gradient<d, Acc>(u, gptr, gidx, eg, gv);
+#pragma unroll
+        for (int p = 0; p < d; ++p)
+        {
+            g[u * d + p] = gv[p];
+            rhs[u * d + p] = -gv[p];
+            part[0] += gv[p] * gv[p];
+        }
+    }
+    double tot[1];
+    if (!grid_sum<1>(part, partials, counter, tot)) return;
+    if (threadIdx.x == 0) ds->gg = tot[0];
 }
 
 template <typename Acc>
@@ -144,6 +183,27 @@ void launch_assemble_grad(Problem& P, int precision)
 {
     if (precision == TAD_PREC_MIXED) assemble_grad_as<tad::DoubleFloatValue>(P);
     else assemble_grad_as<double>(P);
+}
+
+template <typename Acc>
+static void assemble_grad_newton_as(Problem& P)
+{
+    const unsigned grid = (unsigned)std::min<int64_t>(4 * RED_BLOCKS, std::max<int64_t>(1, (P.n_handles + RED_THREADS - 1) / RED_THREADS));
+    switch (P.d)
+    {
+    case 1: k_assemble_grad_newton<1, Acc><<<grid, RED_THREADS, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g, P.rhs,
+                                                                               P.partials, P.counters + 5, P.ds); break;
+    case 2: k_assemble_grad_newton<2, Acc><<<grid, RED_THREADS, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g, P.rhs,
+                                                                               P.partials, P.counters + 5, P.ds); break;
+    default: k_assemble_grad_newton<3, Acc><<<grid, RED_THREADS, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g, P.rhs,
+                                                                                P.partials, P.counters + 5, P.ds); break;
+    }
+}
+
+void launch_assemble_grad_newton(Problem& P, int precision)
+{
+    if (precision == TAD_PREC_MIXED) assemble_grad_newton_as<tad::DoubleFloatValue>(P);
+    else assemble_grad_newton_as<double>(P);
 }
 
 template <int d, typename T>

@@ -411,6 +411,26 @@ __global__ void k_add(int64_t n, const double* __restrict__ a, const double* __r
     GRID_STRIDE(i, n) out[i] = a[i] + b[i];
 }
 
+/* A mixed solution left in FP32 (d32) to FP64 d, the trial point
+   xt = x + d and d.g (with the Newton decrement), in one pass */
+__global__ void __launch_bounds__(RED_THREADS) k_step_prepare(int64_t n, const float* __restrict__ d32, const double* __restrict__ x,
+                                                              const double* __restrict__ g, double* __restrict__ d,
+                                                              double* __restrict__ xt, double* partials, unsigned* counter,
+                                                              DevScalars* ds)
+{
+    double part[1] = {0.0};
+    GRID_STRIDE(i, n)
+    {
+        const double v = (double)d32[i];
+        d[i] = v;
+        xt[i] = x[i] + v;
+        part[0] += v * g[i];
+    }
+    double tot[1];
+    if (!grid_sum<1>(part, partials, counter, tot)) return;
+    if (threadIdx.x == 0) { ds->dg = tot[0]; ds->decrement = -0.5 * tot[0]; }
+}
+
 __global__ void k_axpy_ds(int64_t n, double* __restrict__ x, const double* __restrict__ dx, const DevScalars* ds)
 {
     const double s = ds->ls_s;
@@ -510,6 +530,8 @@ static tad_status pcg_core_amg(Problem& P, const double* b, T* xs, double rel_to
         P.n_launches = l0;
     }
     int replays = 1;
+    double rr_last = 0.0;
+    int slow = 0;
     for (;;)
     {
         for (int k = 0; k < replays; ++k) TAD_CUDA_TRY(cudaGraphLaunch(P.amg_graph, s));
@@ -517,6 +539,19 @@ static tad_status pcg_core_amg(Problem& P, const double* b, T* xs, double rel_to
         TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
         TAD_CUDA_TRY(cudaStreamSynchronize(s));
         if (P.hs->done) break;
+        if (sizeof(T) == 4)
+        {
+            // FP32 V-cycles on a system that is nearly singular at FP32
+            // rounding level can stop reducing the residual: give up after
+            // two host checks without a 10 % reduction (the caller falls back)
+            if (rr_last > 0.0 && !(P.hs->rr < 0.9 * rr_last)) ++slow;
+            rr_last = P.hs->rr;
+            if (slow >= 2)
+            {
+                if (iters_out) *iters_out += P.hs->iters;
+                return TAD_ERR_PCG_NOCONV;
+            }
+        }
         replays = std::min(4, 2 * replays);
     }
     if (iters_out) *iters_out += P.hs->iters;
@@ -527,7 +562,7 @@ static tad_status pcg_core_amg(Problem& P, const double* b, T* xs, double rel_to
 
 template <int d, typename T>
 static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double rel_tol, int max_iters, int* iters_out,
-                           T* r, T* z, T* p, T* Ap, T* dinv, int prec)
+                           T* r, T* z, T* p, T* Ap, T* dinv, int prec, bool allow_amg = true)
 {
     const T* H = (const T*)P.H;
     const int64_t nh = P.n_handles;
@@ -540,12 +575,13 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
     // Newton iterations converge in one); after that, CHUNK iterations
     // captured once per (precision, solution buffer) are replayed, with the
     // replays between host checks doubling up to 8.  With the AMG policy,
-    // an FP64 solve still far from its tolerance after the first 1 + CHUNK
+    // a solve still far from its tolerance after the first 1 + CHUNK
     // iterations restarts with the AMG-preconditioned CG (w must be 0 there:
-    // the hierarchy is built from H itself).  FP32 solves (mixed precision)
-    // stay on block Jacobi: FP32 V-cycles on nearly singular systems (the
-    // eps-regularised rigid motions of an unconstrained mesh) did not
-    // converge reliably.
+    // the hierarchy is built from H itself).  An FP32 solve (mixed precision)
+    // whose V-cycles break down or stall -- FP32 V-cycles on systems nearly
+    // singular at FP32 rounding level (the eps-regularised rigid motions of
+    // an unconstrained mesh) do not converge reliably -- falls back to block
+    // Jacobi alone, from zero.
     constexpr int CHUNK = 8;
     constexpr double AMG_SWITCH_RATIO = 16.0;
     auto launch_iteration = [&]() {
@@ -585,7 +621,7 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
         TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
         TAD_CUDA_TRY(cudaStreamSynchronize(s));
         if (P.hs->done) break;
-        if (sizeof(T) == 8 && replays == 1 && P.settings.preconditioner == 1 && w == 0.0 &&
+        if (allow_amg && replays == 1 && P.settings.preconditioner == 1 && w == 0.0 &&
             P.hs->rr > AMG_SWITCH_RATIO * P.hs->tol2)
         {
             // still more than a factor sqrt(AMG_SWITCH_RATIO) above the target
@@ -594,7 +630,17 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
             const int it = P.hs->iters;
             if (iters_out) *iters_out = it;
             const int left = std::max(1, max_iters - it);
-            return pcg_core_amg<d, T>(P, b, xs, rel_tol, left, iters_out, r, z, p, Ap, prec);
+            const tad_status sa = pcg_core_amg<d, T>(P, b, xs, rel_tol, left, iters_out, r, z, p, Ap, prec);
+            if (sizeof(T) == 8 || sa == TAD_OK) return sa;
+            // FP32: the V-cycle broke down or stalled (a system nearly singular
+            // at FP32 rounding level, e.g. the rigid motions of an
+            // unconstrained mesh): block Jacobi alone, from zero
+            const int used = iters_out ? *iters_out : 0;
+            int more = 0;
+            const tad_status sj = pcg_core<d, T>(P, b, xs, w, rel_tol, std::max(1, max_iters - used), &more, r, z, p, Ap, dinv,
+                                                 prec, false);
+            if (iters_out) *iters_out = used + more;
+            return sj;
         }
         replays = replays == 0 ? 1 : std::min(8, 2 * replays);
     }
@@ -653,14 +699,20 @@ static tad_status pcg_dispatch(Problem& P, const double* b, double* xsol, int pr
     const double inner_tol = std::max(rel_tol, 1e-6);
     int total = 0;
     tad_status st = pcg_core<d, float>(P, b, P.dx32, 0.0, inner_tol, max_iters, &total, P.r32, P.z32, P.p32, P.Ap32, P.dinv32, 1);
-    k_to_double<float><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, P.dx32, xsol, 0);
-    P.n_launches += 1;
     const double bb = P.hs->bb;
     if (rel_tol >= LOOSE_TOL || bb == 0.0)
     {
+        if (P.defer_fp32 && xsol == P.dx) P.solution_in_dx32 = true;   // the caller converts it (k_step_prepare)
+        else
+        {
+            k_to_double<float><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, P.dx32, xsol, 0);
+            P.n_launches += 1;
+        }
         if (iters) *iters = total;
         return st;
     }
+    k_to_double<float><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, P.dx32, xsol, 0);
+    P.n_launches += 1;
     const double target = std::min(rel_tol, std::max(tol, 0.0));
     double rr_prev = bb;
     bool completion = false;
@@ -849,15 +901,23 @@ tad_status line_search_device(Problem& P, double* x, const double* d, double f, 
    current energy if it passes).  Returns the selection in P.hs after one
    host round trip; the caller adopts x_t (its derivatives are then already
    assembled) or continues the line search at trial 2. */
-static tad_status speculative_first_trial(Problem& P, const double* x, const double* d, double* xt, double eps)
+static tad_status speculative_first_trial(Problem& P, const double* x, double* d, double* xt, double eps, bool d_in_fp32)
 {
     cudaStream_t s = P.stream;
-    k_dot_dg<<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_vars, d, P.g, P.partials, P.counters + 4, P.ds);
-    k_add<<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_vars, x, d, xt);
-    P.n_launches += 2;
+    if (d_in_fp32)
+    {
+        k_step_prepare<<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_vars, P.dx32, x, P.g, d, xt, P.partials, P.counters + 4, P.ds);
+        P.n_launches += 1;
+    }
+    else
+    {
+        k_dot_dg<<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_vars, d, P.g, P.partials, P.counters + 4, P.ds);
+        k_add<<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_vars, x, d, xt);
+        P.n_launches += 2;
+    }
     tad_status st = eval_elements(P, TAD_MODE_HESSIAN_PROJ, xt, eps, P.precision);
     if (st != TAD_OK) return st;
-    st = assemble(P, true, true, P.precision, P.ds->f_trial);
+    st = assemble(P, true, true, P.precision, P.ds->f_trial, true);
     if (st != TAD_OK) return st;
     k_ls_select<<<1, 32, 0, s>>>(1, P.steps_seq, P.settings.ls_armijo, P.ds, 1);
     P.n_launches += 1;
@@ -918,11 +978,10 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
         cudaEventRecord(P.ev[1], st);
         if (!have_derivs)
         {
-            s = assemble(P, true, true, prec);
+            // f, g, H, and rhs = -g with |g|^2 (an accepted speculative step assembled them already)
+            s = assemble(P, true, true, prec, nullptr, true);
             if (s != TAD_OK) return finish(s);
         }
-        k_neg_gg<<<RED_BLOCKS, RED_THREADS, 0, st>>>(P.n_vars, P.g, P.rhs, P.partials, P.counters + 5, P.ds);
-        P.n_launches += 1;
         cudaEventRecord(P.ev[2], st);
         double tol = P.settings.pcg_rel_tol;
         if (forcing)
@@ -935,8 +994,14 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
             if (P.g0_norm == 0.0) P.g0_norm = gnorm;   // first iteration since create / set_settings
             if (P.g0_norm > 0.0) tol = std::max(tol, std::min(0.5, std::sqrt(gnorm / P.g0_norm)));
         }
+        const bool spec_now = speculate && it + 1 < n_iters;   // the last iteration has no next one to evaluate for
         int pit = 0;
+        P.defer_fp32 = spec_now;
+        P.solution_in_dx32 = false;
         s = pcg_solve(P, P.rhs, P.dx, 0.0, prec, tol, P.settings.pcg_max_iters, &pit);
+        const bool d_in_fp32 = P.solution_in_dx32;
+        P.defer_fp32 = false;
+        P.solution_in_dx32 = false;
         P.pcg_iters_total += pit;
         if (s != TAD_OK && s != TAD_ERR_PCG_NOCONV) return finish(s);
         cudaEventRecord(P.ev[3], st);
@@ -944,9 +1009,9 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
         double fn = 0.0;
         int trials = 0;
         have_derivs = false;
-        if (speculate && it + 1 < n_iters)   // the last iteration has no next one to evaluate for
+        if (spec_now)
         {
-            s = speculative_first_trial(P, cur, P.dx, spare, eps);
+            s = speculative_first_trial(P, cur, P.dx, spare, eps, d_in_fp32);
             if (s != TAD_OK) return finish(s);
             const int choice = P.hs->ls_choice;
             if (choice == -2)
