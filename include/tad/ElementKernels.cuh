@@ -150,12 +150,12 @@ __device__ __forceinline__ void defer_projection(const ElemLaunch& L, int64_t e)
 
 /* PSD projection of an element Hessian in an element kernel: the deflated
    form where the valence allows it, with non-invariant elements deferred */
-template <int d, int N, typename T>
+template <int d, int N, typename T, bool KnownInvariant = false>
 __device__ __forceinline__ bool project_or_defer(const ElemLaunch& L, int64_t e, T* hp, T eps)
 {
     if constexpr (DeflatedProjection<N>::value)
     {
-        const int r = project_translation_deflated<d, N, T>(hp, eps);
+        const int r = project_translation_deflated<d, N, T, KnownInvariant>(hp, eps);
         if (r < 0) { defer_projection(L, e); return false; }
         return r > 0;
     }
@@ -294,7 +294,7 @@ __global__ void __launch_bounds__(128, ElemHessianMinBlocks<d * N, T>::value) k_
 #pragma unroll
         for (int i = 0; i < k * (k + 1) / 2; ++i) hf[i] = r.hess[i];
     }
-    if (FusedProjection<k>::value && L.project) project_or_defer<d, N, T>(L, e, hf, (T)L.eps);
+    if (FusedProjection<k>::value && L.project) project_or_defer<d, N, T, reduced>(L, e, hf, (T)L.eps);
     L.out_f[e] = (double)r.val;
     bool fin = true;
     double gv[k];
@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(128, ElemHessianMinBlocks<d * N, T>::value) k_
 
 /* Projection of the element blocks (layout of k_elem_hessian: NP vertex-pair
    blocks of d x d, row-major) in place, one element per thread. */
-template <int d, int N, typename T>
+template <int d, int N, typename T, bool KnownInvariant = false>
 __global__ void __launch_bounds__(128) k_project_blocks(ElemLaunch L, T eps)
 {
     constexpr int k = d * N;
@@ -323,7 +323,7 @@ __global__ void __launch_bounds__(128) k_project_blocks(ElemLaunch L, T eps)
     load_row<T, BS>(Hblocks, e, hb);
     T h[k * (k + 1) / 2];
     blocks_to_packed<d, N, T>(hb, h);
-    if (!project_or_defer<d, N, T>(L, e, h, eps)) return;
+    if (!project_or_defer<d, N, T, KnownInvariant>(L, e, h, eps)) return;
     packed_to_blocks<d, N, T>(h, hb);
     store_row<T, BS>(Hblocks, e, hb);
 }
@@ -386,7 +386,8 @@ inline void launch_elements_hessian(const ElemLaunch& L, const Energy& energy, c
     if (deflated && L.project && L.proj_list) cudaMemsetAsync(L.proj_list, 0, sizeof(uint32_t), s);
     k_elem_hessian<d, N, T, Energy><<<elem_grid(L.n_elem), 128, 0, s>>>(L, energy);
     if constexpr (!FusedProjection<d * N>::value)
-        if (L.project) k_project_blocks<d, N, T><<<elem_grid(L.n_elem), 128, 0, s>>>(L, (T)L.eps);
+        if (L.project)
+            k_project_blocks<d, N, T, ReducedDerivatives<Energy, N>::value><<<elem_grid(L.n_elem), 128, 0, s>>>(L, (T)L.eps);
     if constexpr (deflated)
         if (L.project && L.proj_list)
             k_project_general<d, N, T><<<std::min(elem_grid(L.n_elem), 1216u), 128, 0, s>>>(L.proj_list, (T*)L.out_H, (T)L.eps);

@@ -249,27 +249,35 @@ template <typename T> struct TranslationTol
    not translation invariant (some row sum H t_p above TranslationTol times
    max |H_ij|, or a non-finite entry): the caller then runs
    project_positive_definite<d*N>.  Otherwise returns 1 (hp projected). */
-template <int d, int N, typename T>
+template <int d, int N, typename T, bool KnownInvariant = false>
 TAD_HD int project_translation_deflated(T* hp, T eps)
 {
     constexpr int k = d * N, R = d * (N - 1), NR = R * (R + 1) / 2;
-    if (positive_diagonally_dominant<k, T>(hp, eps)) return 0;
     auto H = [&](int i, int j) -> T { return i <= j ? hp[packed_index(i, j, k)] : hp[packed_index(j, i, k)]; };
-    T hmax = T(0);
+    // KnownInvariant: hp was built invariant (lift_translation_invariant of
+    // an energy that declares it), so the row-sum test is skipped; its
+    // diagonal then equals minus the off-diagonal sum of its coordinate, and
+    // the dominance early out can only hold for eps <= 0
+    if (!KnownInvariant || !(eps > T(0)))
+        if (positive_diagonally_dominant<k, T>(hp, eps)) return 0;
+    if constexpr (!KnownInvariant)
+    {
+        T hmax = T(0);
 #pragma unroll
-    for (int q = 0; q < k * (k + 1) / 2; ++q) hmax = tad_abs(hp[q]) > hmax ? tad_abs(hp[q]) : hmax;
-    T rmax = T(0);
+        for (int q = 0; q < k * (k + 1) / 2; ++q) hmax = tad_abs(hp[q]) > hmax ? tad_abs(hp[q]) : hmax;
+        T rmax = T(0);
 #pragma unroll
-    for (int i = 0; i < k; ++i)
+        for (int i = 0; i < k; ++i)
 #pragma unroll
-        for (int q = 0; q < d; ++q)
-        {
-            T s = T(0);
+            for (int q = 0; q < d; ++q)
+            {
+                T s = T(0);
 #pragma unroll
-            for (int b = 0; b < N; ++b) s += H(i, b * d + q);
-            rmax = tad_abs(s) > rmax ? tad_abs(s) : rmax;
-        }
-    if (!(rmax <= T(TranslationTol<T>::value) * hmax) || !(hmax < T(INFINITY))) return -1;
+                for (int b = 0; b < N; ++b) s += H(i, b * d + q);
+                rmax = tad_abs(s) > rmax ? tad_abs(s) : rmax;
+            }
+        if (!(rmax <= T(TranslationTol<T>::value) * hmax) || !(hmax < T(INFINITY))) return -1;
+    }
     // A = Q^T (H Q) (packed R x R, reduced index m*d + p), streamed over the
     // rows i = a*d + p of H: w = (H Q)[i][J] is formed and at once added to
     // the rows (m, p) of A with Q[a][m] != 0 (m >= a-1), so no k x R

@@ -7,6 +7,8 @@
 //     form must be taken and agree with the general projection, in FP64 to
 //     rounding and in FP32 at FP32 accuracy, for eps > 0 and eps < 0 (flip);
 //   * one vertex unused (zero rows and columns): still invariant, same result;
+//   * the variant for matrices known to be invariant (no row-sum test) gives
+//     the same result;
 //   * general matrices (S itself): the deflated form must decline (-1) and
 //     leave the matrix untouched.
 // Prints one line "name max_error" per check; exits non-zero on failure.
@@ -92,6 +94,11 @@ static void check(std::mt19937_64& rng, int trials)
             if (r < 0) { ++wrongly_declined; continue; }
             double err = 0;
             for (int q = 0; q < NP; ++q) err = std::fmax(err, std::fabs(a[q] - ref[q]));
+            // the variant for matrices known invariant by construction (no row-sum test)
+            double kn[NP];
+            for (int q = 0; q < NP; ++q) kn[q] = hp[q];
+            if (project_translation_deflated<d, N, double, true>(kn, eps) < 0) ++wrongly_declined;
+            for (int q = 0; q < NP; ++q) err = std::fmax(err, std::fabs(kn[q] - ref[q]));
             if (eps > 0) { if (unused) eunused = std::fmax(eunused, err / hmax); else e64 = std::fmax(e64, err / hmax); }
             else eflip = std::fmax(eflip, err / hmax);
             if (eps > 0)
