@@ -38,23 +38,6 @@ constexpr int RED_BLOCKS = 608;    // 4 x 152 SMs: fixed grid of the reductions
 constexpr int PCG_BLOCKS = 1216;
 constexpr int RED_THREADS = 256;
 
-/* Gather lists regrouped by length, for the assembly kernels.  An output row
-   (BSR block, or handle) with at most W items sits in bucket W (W = 1, 2, 4,
-   ..., 64), padded to a multiple of 32 rows; a bucket stores its rows' output
-   indices and, column-major, their item ids (-1 = none, always after a
-   row's items), so a warp's id loads are coalesced and do not wait on a row
-   pointer.  Rows with more items keep the CSR gather (long_rows). */
-constexpr int GATHER_BUCKETS = 7;
-struct GatherBuckets
-{
-    int32_t row_begin[GATHER_BUCKETS + 1] = {};   // padded rows of bucket b: [row_begin[b], row_begin[b+1])
-    int64_t id_begin[GATHER_BUCKETS] = {};
-    int32_t* rows = nullptr;        // output row of each padded row, -1 = padding
-    int32_t* ids = nullptr;         // item ids, bucket-major, then column-major within a bucket
-    int32_t* long_rows = nullptr;   // rows with more than 64 items
-    int64_t n_long = 0;
-};
-
 void set_error(const std::string& msg);
 
 #define TAD_CUDA_TRY(expr)                                                          \
@@ -156,7 +139,6 @@ struct Problem
     int32_t *bptr = nullptr, *bcol = nullptr, *diag = nullptr;
     int32_t *cptr = nullptr, *cidx = nullptr;
     int32_t *gptr = nullptr, *gidx = nullptr;
-    GatherBuckets hess_buckets, grad_buckets;   // the same lists regrouped by length
 
     // assembled quantities
     double* x = nullptr;

@@ -88,158 +88,78 @@ void launch_reduce_f(Problem& P, int n_rows, double* out)
     k_reduce_rows<<<grid, RED_THREADS, 0, P.stream>>>(P.ef, n, n, P.partials, P.counters, out);
 }
 
-/* ---- gradient assembly -------------------------------------------------
-   g[u] = sum of handle u's element gradient slots, in element order.  Acc =
+/* g[u] = sum of handle u's element gradient slots, in element order.  Acc =
    double (FP64 path) or tad::DoubleFloatValue (mixed: the double slot values
    are split bit-wise and summed on the FP32 pipe, ~48-bit, the precision of
    the mixed element gradients; FP64 adds bound this gather otherwise).
-   Rows come from the length buckets (GatherBuckets): a thread loads its
-   row's slot ids (coalesced across the warp, column-major), then the slot
-   values, CH at a time, and sums them in order; rows longer than 64 slots
-   use the CSR lists. */
-template <int d, typename Acc, int W>
-__device__ __forceinline__ void bucket_gather_grad(const int32_t* __restrict__ ids, int64_t stride, int64_t i,
-                                                   const double* __restrict__ eg, Acc (&acc)[d])
-{
-    constexpr int CH = W < 4 ? W : 4;
-#pragma unroll(W <= 8 ? W / CH : 1)
-    for (int j0 = 0; j0 < W; j0 += CH)
-    {
-        int32_t c[CH];
-#pragma unroll
-        for (int jj = 0; jj < CH; ++jj) c[jj] = ids[(int64_t)(j0 + jj) * stride + i];
-        if (c[0] < 0) break;   // padding follows a row's slots
-        double v[CH][d];
-#pragma unroll
-        for (int jj = 0; jj < CH; ++jj)
-            if (c[jj] >= 0)
-            {
-#pragma unroll
-                for (int p = 0; p < d; ++p) v[jj][p] = eg[(int64_t)c[jj] * d + p];
-            }
-#pragma unroll
-        for (int jj = 0; jj < CH; ++jj)
-        {
-            if (c[jj] < 0) break;
-#pragma unroll
-            for (int p = 0; p < d; ++p) acc[p] = acc[p] + Acc(v[jj][p]);
-        }
-    }
-}
-
+   Slots are gathered in batches of GATHER (ids, then values, loaded
+   together) and summed in order. */
 template <int d, typename Acc>
-__device__ __forceinline__ void csr_gather_grad(int64_t u, const int32_t* __restrict__ gptr, const int32_t* __restrict__ gidx,
-                                                const double* __restrict__ eg, Acc (&acc)[d])
-{
-    for (int32_t q = gptr[u]; q < gptr[u + 1]; ++q)
-    {
-        const int64_t sl = gidx[q];
-#pragma unroll
-        for (int p = 0; p < d; ++p) acc[p] = acc[p] + Acc(eg[sl * d + p]);
-    }
-}
-
-/* bucket b of padded row t, its index i within the bucket, the bucket's row
-   count (the id stride) and id base, selected with unrolled compares so the
-   kernel parameter stays in constant memory */
-__device__ __forceinline__ void bucket_of_row(const GatherBuckets& B, int64_t t, int& b, int64_t& i, int64_t& stride,
-                                              const int32_t*& ids)
-{
-    b = 0;
-    int64_t lo = B.row_begin[0], hi = B.row_begin[1], ib = B.id_begin[0];
-#pragma unroll
-    for (int q = 1; q < GATHER_BUCKETS; ++q)
-        if (t >= B.row_begin[q])
-        {
-            b = q;
-            lo = B.row_begin[q];
-            hi = B.row_begin[q + 1];
-            ib = B.id_begin[q];
-        }
-    i = t - lo;
-    stride = hi - lo;
-    ids = B.ids + ib;
-}
-
-/* row t of the bucket list (t < padded rows) or long row t - padded; returns
-   the output row (-1 for padding) and the sum */
-template <int d, typename Acc>
-__device__ __forceinline__ int64_t gather_grad_row(int64_t t, const GatherBuckets& B, const int32_t* __restrict__ gptr,
-                                                   const int32_t* __restrict__ gidx, const double* __restrict__ eg,
-                                                   double (&out)[d])
+__device__ __forceinline__ void gather_gradient(int64_t u, const int32_t* __restrict__ gptr, const int32_t* __restrict__ gidx,
+                                                const double* __restrict__ eg, double (&out)[d])
 {
     Acc acc[d];
 #pragma unroll
     for (int p = 0; p < d; ++p) acc[p] = Acc(0.0);
-    const int64_t padded = B.row_begin[GATHER_BUCKETS];
-    int64_t r;
-    if (t < padded)
+    constexpr int GATHER = 4;
+    const int32_t q0 = gptr[u], q1 = gptr[u + 1];
+    for (int32_t q = q0; q < q1; q += GATHER)
     {
-        int b;
-        int64_t i, stride;
-        const int32_t* ids;
-        bucket_of_row(B, t, b, i, stride, ids);
-        switch (b)
+        int64_t sl[GATHER];
+#pragma unroll
+        for (int j = 0; j < GATHER; ++j) sl[j] = (q + j < q1) ? gidx[q + j] : 0;
+        double v[GATHER][d];
+#pragma unroll
+        for (int j = 0; j < GATHER; ++j)
+            if (q + j < q1)
+            {
+#pragma unroll
+                for (int p = 0; p < d; ++p) v[j][p] = eg[sl[j] * d + p];
+            }
+#pragma unroll
+        for (int j = 0; j < GATHER; ++j)
         {
-        case 0: bucket_gather_grad<d, Acc, 1>(ids, stride, i, eg, acc); break;
-        case 1: bucket_gather_grad<d, Acc, 2>(ids, stride, i, eg, acc); break;
-        case 2: bucket_gather_grad<d, Acc, 4>(ids, stride, i, eg, acc); break;
-        case 3: bucket_gather_grad<d, Acc, 8>(ids, stride, i, eg, acc); break;
-        case 4: bucket_gather_grad<d, Acc, 16>(ids, stride, i, eg, acc); break;
-        case 5: bucket_gather_grad<d, Acc, 32>(ids, stride, i, eg, acc); break;
-        default: bucket_gather_grad<d, Acc, 64>(ids, stride, i, eg, acc); break;
+            if (q + j >= q1) break;
+#pragma unroll
+            for (int p = 0; p < d; ++p) acc[p] = acc[p] + Acc(v[j][p]);
         }
-        r = B.rows[t];
-    }
-    else
-    {
-        r = B.long_rows[t - padded];
-        csr_gather_grad<d, Acc>(r, gptr, gidx, eg, acc);
     }
 #pragma unroll
     for (int p = 0; p < d; ++p) out[p] = (double)acc[p];
-    return r;
 }
 
 template <int d, typename Acc>
-__global__ void __launch_bounds__(256) k_assemble_grad(GatherBuckets B, const int32_t* __restrict__ gptr,
-                                                       const int32_t* __restrict__ gidx, const double* __restrict__ eg,
-                                                       double* __restrict__ g)
+__global__ void k_assemble_grad(int64_t nh, const int32_t* __restrict__ gptr, const int32_t* __restrict__ gidx,
+                                const double* __restrict__ eg, double* __restrict__ g)
 {
-    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (t >= B.row_begin[GATHER_BUCKETS] + B.n_long) return;
+    const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (u >= nh) return;
     double gv[d];
-    const int64_t r = gather_grad_row<d, Acc>(t, B, gptr, gidx, eg, gv);
-    if (r < 0) return;
+    gather_gradient<d, Acc>(u, gptr, gidx, eg, gv);
 #pragma unroll
-    for (int p = 0; p < d; ++p) g[r * d + p] = gv[p];
+    for (int p = 0; p < d; ++p) g[u * d + p] = gv[p];
 }
 
 /* The Newton variant: also rhs = -g and g.g (the PCG right-hand side and
-   |g|^2), one thread per row, block partials summed in block order by the
-   last block (the partials buffer holds one per block) */
+   |g|^2), grid-stride over a capped grid for the fixed-order grid sum */
 template <int d, typename Acc>
-__global__ void __launch_bounds__(RED_THREADS) k_assemble_grad_newton(GatherBuckets B, const int32_t* __restrict__ gptr,
-                                                                    const int32_t* __restrict__ gidx,
-                                                                    const double* __restrict__ eg, double* __restrict__ g,
-                                                                    double* __restrict__ rhs, double* partials,
-                                                                    unsigned* counter, DevScalars* ds)
+__global__ void __launch_bounds__(RED_THREADS) k_assemble_grad_newton(int64_t nh, const int32_t* __restrict__ gptr,
+                                                                       const int32_t* __restrict__ gidx,
+                                                                       const double* __restrict__ eg, double* __restrict__ g,
+                                                                       double* __restrict__ rhs, double* partials,
+                                                                       unsigned* counter, DevScalars* ds)
 {
     double part[1] = {0.0};
-    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (t < B.row_begin[GATHER_BUCKETS] + B.n_long)
+    GRID_STRIDE(u, nh)
     {
         double gv[d];
-        const int64_t r = gather_grad_row<d, Acc>(t, B, gptr, gidx, eg, gv);
-        if (r >= 0)
-        {
+        gather_gradient<d, Acc>(u, gptr, gidx, eg, gv);
 #pragma unroll
-            for (int p = 0; p < d; ++p)
-            {
-                g[r * d + p] = gv[p];
-                rhs[r * d + p] = -gv[p];
-                part[0] += gv[p] * gv[p];
-            }
+        for (int p = 0; p < d; ++p)
+        {
+            g[u * d + p] = gv[p];
+            rhs[u * d + p] = -gv[p];
+            part[0] += gv[p] * gv[p];
         }
     }
     double tot[1];
@@ -250,14 +170,12 @@ __global__ void __launch_bounds__(RED_THREADS) k_assemble_grad_newton(GatherBuck
 template <typename Acc>
 static void assemble_grad_as(Problem& P)
 {
-    const int64_t rows = P.grad_buckets.row_begin[GATHER_BUCKETS] + P.grad_buckets.n_long;
-    if (rows == 0) return;
-    const unsigned grid = (unsigned)((rows + 255) / 256);
+    const unsigned grid = (unsigned)((P.n_handles + 255) / 256);
     switch (P.d)
     {
-    case 1: k_assemble_grad<1, Acc><<<grid, 256, 0, P.stream>>>(P.grad_buckets, P.gptr, P.gidx, P.eg, P.g); break;
-    case 2: k_assemble_grad<2, Acc><<<grid, 256, 0, P.stream>>>(P.grad_buckets, P.gptr, P.gidx, P.eg, P.g); break;
-    default: k_assemble_grad<3, Acc><<<grid, 256, 0, P.stream>>>(P.grad_buckets, P.gptr, P.gidx, P.eg, P.g); break;
+    case 1: k_assemble_grad<1, Acc><<<grid, 256, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g); break;
+    case 2: k_assemble_grad<2, Acc><<<grid, 256, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g); break;
+    default: k_assemble_grad<3, Acc><<<grid, 256, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g); break;
     }
 }
 
@@ -270,15 +188,14 @@ void launch_assemble_grad(Problem& P, int precision)
 template <typename Acc>
 static void assemble_grad_newton_as(Problem& P)
 {
-    const int64_t rows = P.grad_buckets.row_begin[GATHER_BUCKETS] + P.grad_buckets.n_long;
-    const unsigned grid = (unsigned)std::max<int64_t>(1, (rows + RED_THREADS - 1) / RED_THREADS);   // <= partials_cap
+    const unsigned grid = (unsigned)std::min<int64_t>(4 * RED_BLOCKS, std::max<int64_t>(1, (P.n_handles + RED_THREADS - 1) / RED_THREADS));
     switch (P.d)
     {
-    case 1: k_assemble_grad_newton<1, Acc><<<grid, RED_THREADS, 0, P.stream>>>(P.grad_buckets, P.gptr, P.gidx, P.eg, P.g, P.rhs,
+    case 1: k_assemble_grad_newton<1, Acc><<<grid, RED_THREADS, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g, P.rhs,
                                                                                P.partials, P.counters + 5, P.ds); break;
-    case 2: k_assemble_grad_newton<2, Acc><<<grid, RED_THREADS, 0, P.stream>>>(P.grad_buckets, P.gptr, P.gidx, P.eg, P.g, P.rhs,
+    case 2: k_assemble_grad_newton<2, Acc><<<grid, RED_THREADS, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g, P.rhs,
                                                                                P.partials, P.counters + 5, P.ds); break;
-    default: k_assemble_grad_newton<3, Acc><<<grid, RED_THREADS, 0, P.stream>>>(P.grad_buckets, P.gptr, P.gidx, P.eg, P.g, P.rhs,
+    default: k_assemble_grad_newton<3, Acc><<<grid, RED_THREADS, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g, P.rhs,
                                                                                 P.partials, P.counters + 5, P.ds); break;
     }
 }
@@ -289,108 +206,58 @@ void launch_assemble_grad_newton(Problem& P, int precision)
     else assemble_grad_newton_as<double>(P);
 }
 
-/* ---- Hessian assembly ---------------------------------------------------
-   H block (u, w) = sum of its element pair blocks in element order (bit 31 of
-   an id: the element block is stored transposed).  Same bucket scheme. */
 template <int d, typename T>
-__device__ __forceinline__ void add_block(T (&acc)[d * d], const T (&v)[d * d], bool transposed)
+__global__ void k_assemble_hess(int64_t nb, const int32_t* __restrict__ cptr, const int32_t* __restrict__ cidx,
+                                const T* __restrict__ eH, T* __restrict__ H)
 {
-    if (transposed)
-    {
-#pragma unroll
-        for (int p = 0; p < d; ++p)
-#pragma unroll
-            for (int r = 0; r < d; ++r) acc[p * d + r] += v[r * d + p];
-    }
-    else
-    {
-#pragma unroll
-        for (int i = 0; i < d * d; ++i) acc[i] += v[i];
-    }
-}
-
-template <int d, typename T, int W>
-__device__ __forceinline__ void bucket_gather_hess(const int32_t* __restrict__ ids, int64_t stride, int64_t i,
-                                                   const T* __restrict__ eH, T (&acc)[d * d])
-{
-    constexpr int CH = W < 4 ? W : 4;
-#pragma unroll(W <= 8 ? W / CH : 1)
-    for (int j0 = 0; j0 < W; j0 += CH)
-    {
-        int32_t c[CH];
-#pragma unroll
-        for (int jj = 0; jj < CH; ++jj) c[jj] = ids[(int64_t)(j0 + jj) * stride + i];
-        if (c[0] == -1) break;   // padding follows a row's contributions
-        T v[CH][d * d];
-#pragma unroll
-        for (int jj = 0; jj < CH; ++jj)
-            if (c[jj] != -1) tad::load_row<T, d * d>(eH, (int64_t)(c[jj] & 0x7fffffff), v[jj]);   // 16-byte load per 2x2 FP32 block
-#pragma unroll
-        for (int jj = 0; jj < CH; ++jj)
-        {
-            if (c[jj] == -1) break;
-            add_block<d, T>(acc, v[jj], c[jj] < 0);
-        }
-    }
-}
-
-template <int d, typename T>
-__global__ void __launch_bounds__(256) k_assemble_hess(GatherBuckets B, const int32_t* __restrict__ cptr,
-                                                       const int32_t* __restrict__ cidx, const T* __restrict__ eH,
-                                                       T* __restrict__ H)
-{
-    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const int64_t padded = B.row_begin[GATHER_BUCKETS];
-    if (t >= padded + B.n_long) return;
+    const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (b >= nb) return;
     T acc[d * d];
 #pragma unroll
     for (int i = 0; i < d * d; ++i) acc[i] = T(0);
-    int64_t r;
-    if (t < padded)
+    // contributions in batches of GATHER: the ids, then the blocks, are loaded
+    // together (independent loads in flight), then summed in order
+    constexpr int GATHER = 4;
+    const int32_t q0 = cptr[b], q1 = cptr[b + 1];
+    for (int32_t q = q0; q < q1; q += GATHER)
     {
-        int b;
-        int64_t i, stride;
-        const int32_t* ids;
-        bucket_of_row(B, t, b, i, stride, ids);
-        switch (b)
+        int32_t c[GATHER];
+#pragma unroll
+        for (int j = 0; j < GATHER; ++j) c[j] = (q + j < q1) ? cidx[q + j] : 0;
+        T v[GATHER][d * d];
+#pragma unroll
+        for (int j = 0; j < GATHER; ++j)
+            if (q + j < q1) tad::load_row<T, d * d>(eH, (int64_t)(c[j] & 0x7fffffff), v[j]);   // one 16-byte load per 2x2 FP32 block
+#pragma unroll
+        for (int j = 0; j < GATHER; ++j)
         {
-        case 0: bucket_gather_hess<d, T, 1>(ids, stride, i, eH, acc); break;
-        case 1: bucket_gather_hess<d, T, 2>(ids, stride, i, eH, acc); break;
-        case 2: bucket_gather_hess<d, T, 4>(ids, stride, i, eH, acc); break;
-        case 3: bucket_gather_hess<d, T, 8>(ids, stride, i, eH, acc); break;
-        case 4: bucket_gather_hess<d, T, 16>(ids, stride, i, eH, acc); break;
-        case 5: bucket_gather_hess<d, T, 32>(ids, stride, i, eH, acc); break;
-        default: bucket_gather_hess<d, T, 64>(ids, stride, i, eH, acc); break;
-        }
-        r = B.rows[t];
-        if (r < 0) return;
-    }
-    else
-    {
-        r = B.long_rows[t - padded];
-        for (int32_t q = cptr[r]; q < cptr[r + 1]; ++q)
-        {
-            const int32_t c = cidx[q];
-            T v[d * d];
-            tad::load_row<T, d * d>(eH, (int64_t)(c & 0x7fffffff), v);
-            add_block<d, T>(acc, v, c < 0);
+            if (q + j >= q1) break;
+            if (c[j] < 0)
+            {
+#pragma unroll
+                for (int p = 0; p < d; ++p)
+#pragma unroll
+                    for (int r = 0; r < d; ++r) acc[p * d + r] += v[j][r * d + p];
+            }
+            else
+            {
+#pragma unroll
+                for (int i = 0; i < d * d; ++i) acc[i] += v[j][i];
+            }
         }
     }
-    tad::store_row<T, d * d>(H, r, acc);
+    tad::store_row<T, d * d>(H, b, acc);
 }
 
 void launch_assemble_hess(Problem& P, int precision)
 {
-    const int64_t rows = P.hess_buckets.row_begin[GATHER_BUCKETS] + P.hess_buckets.n_long;
-    if (P.nb == 0 || rows == 0) return;
-    const unsigned grid = (unsigned)((rows + 255) / 256);
-#define TAD_ASM(D)                                                                                                   \
-    if (precision == TAD_PREC_MIXED)                                                                                 \
-        k_assemble_hess<D, float><<<grid, 256, 0, P.stream>>>(P.hess_buckets, P.cptr, P.cidx, (const float*)P.eH,    \
-                                                              (float*)P.H);                                          \
-    else                                                                                                             \
-        k_assemble_hess<D, double><<<grid, 256, 0, P.stream>>>(P.hess_buckets, P.cptr, P.cidx, (const double*)P.eH,  \
-                                                               (double*)P.H);
+    const unsigned grid = (unsigned)((P.nb + 255) / 256);
+    if (P.nb == 0) return;
+#define TAD_ASM(D)                                                                                         \
+    if (precision == TAD_PREC_MIXED)                                                                       \
+        k_assemble_hess<D, float><<<grid, 256, 0, P.stream>>>(P.nb, P.cptr, P.cidx, (const float*)P.eH, (float*)P.H); \
+    else                                                                                                   \
+        k_assemble_hess<D, double><<<grid, 256, 0, P.stream>>>(P.nb, P.cptr, P.cidx, (const double*)P.eH, (double*)P.H);
     switch (P.d)
     {
     case 1: TAD_ASM(1); break;

@@ -97,62 +97,6 @@ tad_status check_device_error(Problem& P)
 /* ------------------------------------------------------------------------ */
 /* pattern construction                                                      */
 /* ------------------------------------------------------------------------ */
-/* GatherBuckets from a CSR gather list (ptr[n+1], idx) */
-static tad_status build_buckets(const std::vector<int32_t>& ptr, const int32_t* idx, GatherBuckets& B)
-{
-    const int64_t n = (int64_t)ptr.size() - 1;
-    auto bucket_of = [](int32_t c) {
-        int b = 0;
-        while (b < GATHER_BUCKETS && c > (1 << b)) ++b;
-        return b;   // GATHER_BUCKETS: a long row
-    };
-    std::vector<int64_t> cnt(GATHER_BUCKETS, 0);
-    std::vector<int32_t> long_rows;
-    for (int64_t r = 0; r < n; ++r)
-    {
-        const int b = bucket_of(ptr[r + 1] - ptr[r]);
-        if (b < GATHER_BUCKETS) ++cnt[b];
-        else long_rows.push_back((int32_t)r);
-    }
-    int64_t rows_total = 0, ids_total = 0;
-    for (int b = 0; b < GATHER_BUCKETS; ++b)
-    {
-        const int64_t padded = (cnt[b] + 31) / 32 * 32;
-        if (rows_total + padded >= (int64_t(1) << 31)) return fail(TAD_ERR_ARG, "gather buckets exceed 2^31 rows");
-        B.row_begin[b] = (int32_t)rows_total;
-        B.id_begin[b] = ids_total;
-        rows_total += padded;
-        ids_total += padded << b;
-    }
-    B.row_begin[GATHER_BUCKETS] = (int32_t)rows_total;
-    std::vector<int32_t> rows(std::max<int64_t>(rows_total, 1), -1), ids(std::max<int64_t>(ids_total, 1), -1);
-    std::vector<int64_t> fill(GATHER_BUCKETS, 0);
-    for (int64_t r = 0; r < n; ++r)
-    {
-        const int32_t c = ptr[r + 1] - ptr[r];
-        const int b = bucket_of(c);
-        if (b >= GATHER_BUCKETS) continue;
-        const int64_t i = fill[b]++;
-        const int64_t stride = B.row_begin[b + 1] - B.row_begin[b];
-        rows[B.row_begin[b] + i] = (int32_t)r;
-        for (int32_t j = 0; j < c; ++j) ids[B.id_begin[b] + j * stride + i] = idx[ptr[r] + j];
-    }
-    B.n_long = (int64_t)long_rows.size();
-    TAD_CUDA_TRY(dalloc(&B.rows, (int64_t)rows.size()));
-    TAD_CUDA_TRY(dalloc(&B.ids, (int64_t)ids.size()));
-    TAD_CUDA_TRY(dalloc(&B.long_rows, std::max<int64_t>(B.n_long, 1)));
-    TAD_CUDA_TRY(cudaMemcpy(B.rows, rows.data(), rows.size() * 4, cudaMemcpyHostToDevice));
-    TAD_CUDA_TRY(cudaMemcpy(B.ids, ids.data(), ids.size() * 4, cudaMemcpyHostToDevice));
-    if (B.n_long) TAD_CUDA_TRY(cudaMemcpy(B.long_rows, long_rows.data(), B.n_long * 4, cudaMemcpyHostToDevice));
-    return TAD_OK;
-}
-
-static void free_buckets(GatherBuckets& B)
-{
-    dfree(B.rows); dfree(B.ids); dfree(B.long_rows);
-    B = GatherBuckets{};
-}
-
 static tad_status build_pattern(Problem& P)
 {
     const int64_t nh = P.n_handles;
@@ -275,11 +219,7 @@ static tad_status build_pattern(Problem& P)
     TAD_CUDA_TRY(cudaMemcpy(P.cidx, cidx.data(), ncontrib * 4, cudaMemcpyHostToDevice));
     TAD_CUDA_TRY(cudaMemcpy(P.gptr, gptr.data(), (nh + 1) * 4, cudaMemcpyHostToDevice));
     TAD_CUDA_TRY(cudaMemcpy(P.gidx, gidx.data(), ninc * 4, cudaMemcpyHostToDevice));
-    free_buckets(P.hess_buckets);
-    free_buckets(P.grad_buckets);
-    tad_status s = build_buckets(ccnt, cidx.data(), P.hess_buckets);
-    if (s != TAD_OK) return s;
-    return build_buckets(gptr, gidx.data(), P.grad_buckets);
+    return TAD_OK;
 }
 
 tad_status ensure_finalized(Problem& P)
@@ -456,10 +396,7 @@ TAD_API tad_status tad_problem_create(int var_dim, int64_t n_handles, const tad_
     TAD_CUDA_TRY(cudaMalloc(&P->counters, 64 * sizeof(unsigned)));
     TAD_CUDA_TRY(cudaMemset(P->counters, 0, 64 * sizeof(unsigned)));
     static_assert(PCG_BLOCKS * 3 <= RED_BLOCKS * LS_BATCH * 4, "PCG grid sums must fit the partials buffer");
-    // also one partial per 256-thread block of the per-row gradient assembly
-    // (gather buckets pad each of 7 buckets to 32 rows, long rows are extra)
-    const int64_t grad_blocks = (n_handles + GATHER_BUCKETS * 32 + 255) / 256 + 1;
-    TAD_CUDA_TRY(cudaMalloc(&P->partials, (size_t)std::max<int64_t>(RED_BLOCKS * LS_BATCH * 4, grad_blocks) * sizeof(double)));
+    TAD_CUDA_TRY(cudaMalloc(&P->partials, (size_t)RED_BLOCKS * LS_BATCH * 4 * sizeof(double)));
     TAD_CUDA_TRY(cudaMalloc(&P->steps, 64 * sizeof(double)));
     TAD_CUDA_TRY(cudaMalloc(&P->x, P->n_vars * sizeof(double)));
     TAD_CUDA_TRY(cudaMemset(P->x, 0, P->n_vars * sizeof(double)));
@@ -479,8 +416,6 @@ TAD_API tad_status tad_problem_destroy(tad_problem* P)
                     P->r32, P->z32, P->p32, P->Ap32, P->dx32, P->dinv32, P->rhs, P->res, P->steps,
                     P->partials, P->counters, P->ds, P->err, P->proj_list, P->steps_seq, P->x_trial};
     for (void* b : bufs) dfree(b);
-    free_buckets(P->hess_buckets);
-    free_buckets(P->grad_buckets);
     if (P->hs) cudaFreeHost(P->hs);
     if (P->err_h) cudaFreeHost(P->err_h);
     if (P->pcg_graph) cudaGraphExecDestroy(P->pcg_graph);
