@@ -10,7 +10,10 @@
  * (tad/Projection.cuh: translation-deflated where the element Hessian allows
  * it, else the general form in a second pass) and written as
  *   f:  double  out_f[e]
- *   g:  Tg      out_g[e][N*d]                         (slot-major)
+ *   g:  out_g[e][N*d] (slot-major): double, or -- in the mixed second-order
+ *       modes (T = float, HESSIAN / HESSIAN_PROJ) -- a double-float pair
+ *       (hi, lo floats, the same 8 bytes) that the mixed assembly sums
+ *       without FP64 instructions
  *   H:  Th      out_H[e][N(N+1)/2 slot pairs a<=b][d][d]
  * which the assembly kernels gather per global block in element order.  This
  * replaces the per-element std::vector results and the serial triplet
@@ -207,6 +210,10 @@ __device__ __forceinline__ void packed_to_blocks(const T* h, T* hb)
    For a triangle in 2D that is 4 instead of 6 gradient and 10 instead of 21
    Hessian entries per live intermediate (tetrahedron: 9 / 45 instead of
    12 / 78), which is most of the evaluation's work and registers. */
+/* a gradient entry as a double-float pair */
+__device__ __forceinline__ DoubleFloatValue gf_pair(const DoubleFloat& g) { return DoubleFloatValue(g.hi, g.lo); }
+__device__ __forceinline__ DoubleFloatValue gf_pair(double g) { return DoubleFloatValue(g); }
+
 template <typename Energy, int N> struct ReducedDerivatives
 {
     static constexpr bool value = IsTranslationInvariant<Energy>::value && N >= 2;
@@ -297,10 +304,27 @@ __global__ void __launch_bounds__(128, ElemHessianMinBlocks<d * N, T>::value) k_
     if (FusedProjection<k>::value && L.project) project_or_defer<d, N, T, reduced>(L, e, hf, (T)L.eps);
     L.out_f[e] = (double)r.val;
     bool fin = true;
-    double gv[k];
+    if constexpr (std::is_same<T, float>::value)
+    {
+        // double-float pairs (the gradient type's own, or split from double)
+        float gp[2 * k];
 #pragma unroll
-    for (int i = 0; i < k; ++i) { gv[i] = (double)gf[i]; fin = fin && finite_val(gv[i]); }
-    store_row<double, k>((double*)L.out_g, e, gv);
+        for (int i = 0; i < k; ++i)
+        {
+            const DoubleFloatValue v = gf_pair(gf[i]);
+            gp[2 * i] = v.hi;
+            gp[2 * i + 1] = v.lo;
+            fin = fin && finite_val(v.hi);
+        }
+        store_row<float, 2 * k>((float*)L.out_g, e, gp);
+    }
+    else
+    {
+        double gv[k];
+#pragma unroll
+        for (int i = 0; i < k; ++i) { gv[i] = (double)gf[i]; fin = fin && finite_val(gv[i]); }
+        store_row<double, k>((double*)L.out_g, e, gv);
+    }
     T hb[NP * d * d];
     packed_to_blocks<d, N, T>(hf, hb);
 #pragma unroll
@@ -508,7 +532,20 @@ __global__ void __launch_bounds__(128) k_vec_first_order(ElemLaunch L, Energy en
         }
     }
     L.out_f[e] = f;
-    store_row<double, k>((double*)L.out_g, e, g);
+    if (gn && std::is_same<T, float>::value)
+    {
+        // mixed second-order mode: double-float pairs, as k_elem_hessian writes them
+        float gp[2 * k];
+#pragma unroll
+        for (int i = 0; i < k; ++i)
+        {
+            const DoubleFloatValue v(g[i]);
+            gp[2 * i] = v.hi;
+            gp[2 * i + 1] = v.lo;
+        }
+        store_row<float, 2 * k>((float*)L.out_g, e, gp);
+    }
+    else store_row<double, k>((double*)L.out_g, e, g);
     if (gn)
     {
         T hb[NP * d * d];

@@ -463,7 +463,7 @@ static tad_status record_iteration(Batch& B, int prec, double eps)
     tad_status st = eval_elements(P, TAD_MODE_HESSIAN_PROJ, B.x, eps, prec);
     if (st != TAD_OK) return st;
     k_b_reduce_rows<<<dim3(G, 1), TH, 0, s>>>(B.ech, B.n_ech, B.emcb, B.emce, P.ef, P.n_elem_total, B.partials, B.counters, B.S.f, 1);
-    launch_assemble_grad(P, prec);
+    launch_assemble_grad(P, prec, prec == TAD_PREC_MIXED);
     launch_assemble_hess(P, prec);
     k_b_neg<<<G, TH, 0, s>>>(n, P.g, P.rhs);
     // 2. PCG, per-mesh tolerance

@@ -212,10 +212,12 @@ tad_status eval_full(Problem& P, const double* x, int mode, double eps, int prec
 
 // ---- kernels (kernels.cu)
 void launch_reduce_f(Problem& P, int n_rows, double* out);      // sums ef rows into out[row]
-/* g from the element gradient slots, in element order; mixed precision sums in double-float */
-void launch_assemble_grad(Problem& P, int precision = TAD_PREC_FP64);
+/* g from the element gradient slots, in element order; mixed precision sums
+   in double-float.  pairs: the slots hold double-float pairs (what the
+   mixed second-order element kernels write) */
+void launch_assemble_grad(Problem& P, int precision = TAD_PREC_FP64, bool pairs = false);
 /* the same, also rhs = -g and ds->gg = g.g (Newton right-hand side) */
-void launch_assemble_grad_newton(Problem& P, int precision);
+void launch_assemble_grad_newton(Problem& P, int precision, bool pairs);
 void launch_assemble_hess(Problem& P, int precision);
 void launch_bsr_to_csr(Problem& P, double* out, int precision);
 void launch_zero(double* p, int64_t n, cudaStream_t s);

@@ -94,10 +94,12 @@ void launch_reduce_f(Problem& P, int n_rows, double* out)
    the mixed element gradients; FP64 adds bound this gather otherwise).
    Slots are gathered in batches of GATHER (ids, then values, loaded
    together) and summed in order. */
-template <int d, typename Acc>
+template <int d, typename Acc, bool Pairs>
 __device__ __forceinline__ void gather_gradient(int64_t u, const int32_t* __restrict__ gptr, const int32_t* __restrict__ gidx,
                                                 const double* __restrict__ eg, double (&out)[d])
 {
+    // Pairs: the slots hold double-float pairs (mixed second-order modes)
+    const float2* __restrict__ eg2 = reinterpret_cast<const float2*>(eg);
     Acc acc[d];
 #pragma unroll
     for (int p = 0; p < d; ++p) acc[p] = Acc(0.0);
@@ -108,41 +110,62 @@ __device__ __forceinline__ void gather_gradient(int64_t u, const int32_t* __rest
         int64_t sl[GATHER];
 #pragma unroll
         for (int j = 0; j < GATHER; ++j) sl[j] = (q + j < q1) ? gidx[q + j] : 0;
-        double v[GATHER][d];
-#pragma unroll
-        for (int j = 0; j < GATHER; ++j)
-            if (q + j < q1)
-            {
-#pragma unroll
-                for (int p = 0; p < d; ++p) v[j][p] = eg[sl[j] * d + p];
-            }
-#pragma unroll
-        for (int j = 0; j < GATHER; ++j)
+        if constexpr (Pairs)
         {
-            if (q + j >= q1) break;
+            float2 v[GATHER][d];
 #pragma unroll
-            for (int p = 0; p < d; ++p) acc[p] = acc[p] + Acc(v[j][p]);
+            for (int j = 0; j < GATHER; ++j)
+                if (q + j < q1)
+                {
+#pragma unroll
+                    for (int p = 0; p < d; ++p) v[j][p] = eg2[sl[j] * d + p];
+                }
+#pragma unroll
+            for (int j = 0; j < GATHER; ++j)
+            {
+                if (q + j >= q1) break;
+#pragma unroll
+                for (int p = 0; p < d; ++p) acc[p] = acc[p] + tad::DoubleFloatValue(v[j][p].x, v[j][p].y);
+            }
+        }
+        else
+        {
+            double v[GATHER][d];
+#pragma unroll
+            for (int j = 0; j < GATHER; ++j)
+                if (q + j < q1)
+                {
+#pragma unroll
+                    for (int p = 0; p < d; ++p) v[j][p] = eg[sl[j] * d + p];
+                }
+#pragma unroll
+            for (int j = 0; j < GATHER; ++j)
+            {
+                if (q + j >= q1) break;
+#pragma unroll
+                for (int p = 0; p < d; ++p) acc[p] = acc[p] + Acc(v[j][p]);
+            }
         }
     }
 #pragma unroll
     for (int p = 0; p < d; ++p) out[p] = (double)acc[p];
 }
 
-template <int d, typename Acc>
+template <int d, typename Acc, bool Pairs>
 __global__ void k_assemble_grad(int64_t nh, const int32_t* __restrict__ gptr, const int32_t* __restrict__ gidx,
                                 const double* __restrict__ eg, double* __restrict__ g)
 {
     const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (u >= nh) return;
     double gv[d];
-    gather_gradient<d, Acc>(u, gptr, gidx, eg, gv);
+    gather_gradient<d, Acc, Pairs>(u, gptr, gidx, eg, gv);
 #pragma unroll
     for (int p = 0; p < d; ++p) g[u * d + p] = gv[p];
 }
 
 /* The Newton variant: also rhs = -g and g.g (the PCG right-hand side and
    |g|^2), grid-stride over a capped grid for the fixed-order grid sum */
-template <int d, typename Acc>
+template <int d, typename Acc, bool Pairs>
 __global__ void __launch_bounds__(RED_THREADS) k_assemble_grad_newton(int64_t nh, const int32_t* __restrict__ gptr,
                                                                        const int32_t* __restrict__ gidx,
                                                                        const double* __restrict__ eg, double* __restrict__ g,
@@ -153,7 +176,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_assemble_grad_newton(int64_t nh
     GRID_STRIDE(u, nh)
     {
         double gv[d];
-        gather_gradient<d, Acc>(u, gptr, gidx, eg, gv);
+        gather_gradient<d, Acc, Pairs>(u, gptr, gidx, eg, gv);
 #pragma unroll
         for (int p = 0; p < d; ++p)
         {
@@ -167,43 +190,45 @@ __global__ void __launch_bounds__(RED_THREADS) k_assemble_grad_newton(int64_t nh
     if (threadIdx.x == 0) ds->gg = tot[0];
 }
 
-template <typename Acc>
+template <typename Acc, bool Pairs>
 static void assemble_grad_as(Problem& P)
 {
     const unsigned grid = (unsigned)((P.n_handles + 255) / 256);
     switch (P.d)
     {
-    case 1: k_assemble_grad<1, Acc><<<grid, 256, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g); break;
-    case 2: k_assemble_grad<2, Acc><<<grid, 256, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g); break;
-    default: k_assemble_grad<3, Acc><<<grid, 256, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g); break;
+    case 1: k_assemble_grad<1, Acc, Pairs><<<grid, 256, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g); break;
+    case 2: k_assemble_grad<2, Acc, Pairs><<<grid, 256, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g); break;
+    default: k_assemble_grad<3, Acc, Pairs><<<grid, 256, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g); break;
     }
 }
 
-void launch_assemble_grad(Problem& P, int precision)
+void launch_assemble_grad(Problem& P, int precision, bool pairs)
 {
-    if (precision == TAD_PREC_MIXED) assemble_grad_as<tad::DoubleFloatValue>(P);
-    else assemble_grad_as<double>(P);
+    if (precision != TAD_PREC_MIXED) assemble_grad_as<double, false>(P);
+    else if (pairs) assemble_grad_as<tad::DoubleFloatValue, true>(P);
+    else assemble_grad_as<tad::DoubleFloatValue, false>(P);
 }
 
-template <typename Acc>
+template <typename Acc, bool Pairs>
 static void assemble_grad_newton_as(Problem& P)
 {
     const unsigned grid = (unsigned)std::min<int64_t>(4 * RED_BLOCKS, std::max<int64_t>(1, (P.n_handles + RED_THREADS - 1) / RED_THREADS));
     switch (P.d)
     {
-    case 1: k_assemble_grad_newton<1, Acc><<<grid, RED_THREADS, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g, P.rhs,
-                                                                               P.partials, P.counters + 5, P.ds); break;
-    case 2: k_assemble_grad_newton<2, Acc><<<grid, RED_THREADS, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g, P.rhs,
-                                                                               P.partials, P.counters + 5, P.ds); break;
-    default: k_assemble_grad_newton<3, Acc><<<grid, RED_THREADS, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g, P.rhs,
-                                                                                P.partials, P.counters + 5, P.ds); break;
+    case 1: k_assemble_grad_newton<1, Acc, Pairs><<<grid, RED_THREADS, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g, P.rhs,
+                                                                                      P.partials, P.counters + 5, P.ds); break;
+    case 2: k_assemble_grad_newton<2, Acc, Pairs><<<grid, RED_THREADS, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g, P.rhs,
+                                                                                      P.partials, P.counters + 5, P.ds); break;
+    default: k_assemble_grad_newton<3, Acc, Pairs><<<grid, RED_THREADS, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g, P.rhs,
+                                                                                       P.partials, P.counters + 5, P.ds); break;
     }
 }
 
-void launch_assemble_grad_newton(Problem& P, int precision)
+void launch_assemble_grad_newton(Problem& P, int precision, bool pairs)
 {
-    if (precision == TAD_PREC_MIXED) assemble_grad_newton_as<tad::DoubleFloatValue>(P);
-    else assemble_grad_newton_as<double>(P);
+    if (precision != TAD_PREC_MIXED) assemble_grad_newton_as<double, false>(P);
+    else if (pairs) assemble_grad_newton_as<tad::DoubleFloatValue, true>(P);
+    else assemble_grad_newton_as<tad::DoubleFloatValue, false>(P);
 }
 
 template <int d, typename T>

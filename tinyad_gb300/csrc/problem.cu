@@ -325,8 +325,10 @@ tad_status eval_elements(Problem& P, int mode, const double* x, double eps, int 
 tad_status assemble(Problem& P, bool gradient, bool hessian, int precision, double* f_dst, bool newton_rhs)
 {
     launch_reduce_f(P, 1, f_dst ? f_dst : &P.ds->f);
-    if (gradient && newton_rhs) launch_assemble_grad_newton(P, precision);
-    else if (gradient) launch_assemble_grad(P, precision);
+    // the mixed second-order element kernels write double-float gradient pairs
+    const bool pairs = precision == TAD_PREC_MIXED && hessian;
+    if (gradient && newton_rhs) launch_assemble_grad_newton(P, precision, pairs);
+    else if (gradient) launch_assemble_grad(P, precision, pairs);
     if (hessian) launch_assemble_hess(P, precision);
     P.n_launches += 1 + (gradient ? 1 : 0) + (hessian ? 1 : 0);
     TAD_CUDA_TRY(cudaGetLastError());

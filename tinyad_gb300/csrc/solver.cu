@@ -35,10 +35,21 @@
 #include <vector>
 
 #include "internal.hh"
+#include "../../include/tad/Scalar.cuh"
 #include "grid_reduce.cuh"
 #include "bsr_kernels.cuh"
 
 namespace tadlib {
+
+/* conversions between the FP64 vectors and the PCG precision: on this GPU
+   float <-> double conversion instructions run on the FP64 pipe, so the FP32
+   side uses bit constructions (exact float -> double; double -> nearest
+   float through the double-float split) */
+template <typename T> __device__ __forceinline__ T from_double(double v);
+template <> __device__ __forceinline__ double from_double<double>(double v) { return v; }
+template <> __device__ __forceinline__ float from_double<float>(double v) { return (float)tad::DoubleFloatValue(v); }
+__device__ __forceinline__ double as_double(double v) { return v; }
+__device__ __forceinline__ double as_double(float v) { return tad::DoubleFloat::float_to_double(v); }
 
 /* x = 0, r = b, z = M^-1 r, p = Ap = 0, beta = 0 (the first fused SpMV then
    forms p = z, Ap = A z); rz = r.z, bb = b.b.  With H given (block Jacobi),
@@ -56,7 +67,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_init(int64_t nh, const doub
     {
         T rv[d], zv[d];
 #pragma unroll
-        for (int i = 0; i < d; ++i) { rv[i] = (T)b[u * d + i]; x[u * d + i] = T(0); r[u * d + i] = rv[i]; }
+        for (int i = 0; i < d; ++i) { rv[i] = from_double<T>(b[u * d + i]); x[u * d + i] = T(0); r[u * d + i] = rv[i]; }
         if (H)
         {
             T I[d * d];
@@ -81,7 +92,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_init(int64_t nh, const doub
             acc_bb += rv[i] * rv[i];
         }
     }
-    double part[2] = {(double)acc_rz, (double)acc_bb};
+    double part[2] = {as_double(acc_rz), as_double(acc_bb)};
     double tot[2];
     if (!grid_sum<2>(part, partials, counter, tot)) return;
     if (threadIdx.x == 0)
@@ -130,7 +141,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_spmv(int64_t nh, const int3
             part += p[u * d + i] * y[i];
         }
     }
-    double v[1] = {(double)part}, tot[1];
+    double v[1] = {as_double(part)}, tot[1];
     if (!grid_sum<1>(v, partials, counter, tot)) return;
     if (threadIdx.x == 0)
     {
@@ -197,7 +208,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_spmv_fused(int64_t nh, cons
                                                                 double* partials, unsigned* counter, DevScalars* ds)
 {
     if (*(volatile int32_t*)&ds->done) return;
-    const T beta = (T)ds->beta;
+    const T beta = from_double<T>(ds->beta);
     T part = T(0);
     GRID_STRIDE(u, nh)
     {
@@ -245,7 +256,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_spmv_fused(int64_t nh, cons
             part += pn * apn;
         }
     }
-    double v[1] = {(double)part}, tot[1];
+    double v[1] = {as_double(part)}, tot[1];
     if (!grid_sum<1>(v, partials, counter, tot)) return;
     if (threadIdx.x == 0)
     {
@@ -267,7 +278,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_update(int64_t nh, T* x, T*
                                                             const T* __restrict__ dinv, double* partials, unsigned* counter, DevScalars* ds)
 {
     if (*(volatile int32_t*)&ds->done) return;
-    const T alpha = (T)ds->alpha;
+    const T alpha = from_double<T>(ds->alpha);
     T part0 = T(0), part1 = T(0);
     GRID_STRIDE(u, nh)
     {
@@ -288,7 +299,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_update(int64_t nh, T* x, T*
             part1 += rv[i] * rv[i];
         }
     }
-    double v[2] = {(double)part0, (double)part1}, tot[2];
+    double v[2] = {as_double(part0), as_double(part1)}, tot[2];
     if (!grid_sum<2>(v, partials, counter, tot)) return;
     if (threadIdx.x == 0)
     {
@@ -304,7 +315,7 @@ template <int d, typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_pcg_pupdate(int64_t n, const T* __restrict__ z, T* __restrict__ p, const DevScalars* ds)
 {
     if (*(volatile const int32_t*)&ds->done) return;
-    const T beta = (T)ds->beta;
+    const T beta = from_double<T>(ds->beta);
     GRID_STRIDE(i, n) p[i] = z[i] + beta * p[i];
 }
 
@@ -324,7 +335,11 @@ template <typename T>
 __global__ void k_to_double(int64_t n, const T* __restrict__ a, double* __restrict__ out, int accumulate)
 {
     // accumulate: 0 = set, 1 = add, -1 = subtract
-    GRID_STRIDE(i, n) out[i] = (accumulate ? out[i] : 0.0) + (accumulate < 0 ? -(double)a[i] : (double)a[i]);
+    GRID_STRIDE(i, n)
+    {
+        const double v = as_double(a[i]);
+        out[i] = accumulate == 0 ? v : out[i] + (accumulate < 0 ? -v : v);
+    }
 }
 
 /* res = b - (H + wI) y with FP64 accumulation; partial |res|^2 -> ds->rr */
@@ -412,20 +427,26 @@ __global__ void k_add(int64_t n, const double* __restrict__ a, const double* __r
 }
 
 /* A mixed solution left in FP32 (d32) to FP64 d, the trial point
-   xt = x + d and d.g (with the Newton decrement), in one pass */
+   xt = x + d and d.g (with the Newton decrement), in one pass.  The float ->
+   double conversions are bit constructions and d.g is accumulated per thread
+   in FP32 (the Armijo test scales it by c = 1e-4, so its ~1e-7 relative
+   error is immaterial), leaving one FP64 add per entry: the FP64 pipe bound
+   this kernel otherwise. */
 __global__ void __launch_bounds__(RED_THREADS) k_step_prepare(int64_t n, const float* __restrict__ d32, const double* __restrict__ x,
                                                               const double* __restrict__ g, double* __restrict__ d,
                                                               double* __restrict__ xt, double* partials, unsigned* counter,
                                                               DevScalars* ds)
 {
-    double part[1] = {0.0};
+    float pf = 0.0f;
     GRID_STRIDE(i, n)
     {
-        const double v = (double)d32[i];
+        const float vf = d32[i];
+        const double v = tad::DoubleFloat::float_to_double(vf);
         d[i] = v;
         xt[i] = x[i] + v;
-        part[0] += v * g[i];
+        pf = fmaf(vf, tad::DoubleFloatValue(g[i]).hi, pf);
     }
+    double part[1] = {tad::DoubleFloat::float_to_double(pf)};
     double tot[1];
     if (!grid_sum<1>(part, partials, counter, tot)) return;
     if (threadIdx.x == 0) { ds->dg = tot[0]; ds->decrement = -0.5 * tot[0]; }
@@ -450,7 +471,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_update_nopc(int64_t n, T* x
                                                                  DevScalars* ds)
 {
     if (*(volatile int32_t*)&ds->done) return;
-    const T alpha = (T)ds->alpha;
+    const T alpha = from_double<T>(ds->alpha);
     T part = T(0);
     GRID_STRIDE(i, n)
     {
@@ -459,7 +480,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_update_nopc(int64_t n, T* x
         r[i] = ri;
         part += ri * ri;
     }
-    double v[1] = {(double)part}, tot[1];
+    double v[1] = {as_double(part)}, tot[1];
     if (!grid_sum<1>(v, partials, counter, tot)) return;
     if (threadIdx.x == 0)
     {
@@ -477,7 +498,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_rz(int64_t n, const T* __re
     if (*(volatile int32_t*)&ds->done) return;
     T part = T(0);
     GRID_STRIDE(i, n) part += r[i] * z[i];
-    double v[1] = {(double)part}, tot[1];
+    double v[1] = {as_double(part)}, tot[1];
     if (!grid_sum<1>(v, partials, counter, tot)) return;
     if (threadIdx.x == 0)
     {
@@ -1150,7 +1171,7 @@ TAD_API tad_status tad_profile_kernels(tad_problem* P, const double* x_d, int re
         return (double)ms / reps;
     };
     ms5[0] = timed([&] { eval_elements(Q, TAD_MODE_HESSIAN_PROJ, x_d, 1e-9, prec); });
-    ms5[1] = timed([&] { launch_assemble_grad(Q, prec); launch_assemble_hess(Q, prec); });
+    ms5[1] = timed([&] { launch_assemble_grad(Q, prec, prec == TAD_PREC_MIXED); launch_assemble_hess(Q, prec); });
     const int64_t nh = Q.n_handles, n = Q.n_vars;
 #define TAD_PROF(D)                                                                                                  \
     if (prec == TAD_PREC_MIXED)                                                                                     \
