@@ -596,15 +596,22 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
     // Newton iterations converge in one); after that, CHUNK iterations
     // captured once per (precision, solution buffer) are replayed, with the
     // replays between host checks doubling up to 8.  With the AMG policy,
-    // a solve still far from its tolerance after the first 1 + CHUNK
-    // iterations restarts with the AMG-preconditioned CG (w must be 0 there:
-    // the hierarchy is built from H itself).  An FP32 solve (mixed precision)
+    // a solve that after the first 1 + CHUNK iterations is still far from its
+    // tolerance, or whose block-Jacobi rate predicts more than
+    // AMG_SWITCH_ITERS further iterations, restarts with the
+    // AMG-preconditioned CG (w must be 0 there: the hierarchy is built from H
+    // itself).  An FP32 solve (mixed precision)
     // whose V-cycles break down or stall -- FP32 V-cycles on systems nearly
     // singular at FP32 rounding level (the eps-regularised rigid motions of
     // an unconstrained mesh) do not converge reliably -- falls back to block
     // Jacobi alone, from zero.
     constexpr int CHUNK = 8;
     constexpr double AMG_SWITCH_RATIO = 16.0;
+    // an AMG iteration costs ~4 block-Jacobi ones plus the hierarchy's values
+    // (measured on the 1.64M-face disk: 0.26 vs 0.06 ms); switching pays when
+    // block Jacobi still needs more than this many iterations
+    constexpr double AMG_SWITCH_ITERS = 64.0;
+    double rr_first = 0.0;
     auto launch_iteration = [&]() {
         k_pcg_spmv_fused<d, T, SpmvGroup<d>::value><<<PCG_BLOCKS, RED_THREADS, 0, s>>>(nh, P.bptr, P.bcol, H, z, p, Ap,
                                                                                   P.partials, P.counters + 1, P.ds);
@@ -642,12 +649,24 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
         TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
         TAD_CUDA_TRY(cudaStreamSynchronize(s));
         if (P.hs->done) break;
-        if (allow_amg && replays == 1 && P.settings.preconditioner == 1 && w == 0.0 &&
-            P.hs->rr > AMG_SWITCH_RATIO * P.hs->tol2)
+        if (replays == 0) rr_first = P.hs->rr;
+        bool slow = false;
+        if (replays == 1)
         {
-            // still more than a factor sqrt(AMG_SWITCH_RATIO) above the target
-            // after 1 + CHUNK iterations: block Jacobi's fast start (the high
-            // frequencies) is over, what is left converges at its slow rate
+            // the residual rate over iterations 1 .. 1 + CHUNK predicts how many
+            // more block-Jacobi iterations the target needs
+            const double rr = P.hs->rr, tol2 = P.hs->tol2;
+            if (rr > AMG_SWITCH_RATIO * tol2) slow = true;
+            else if (rr > tol2 && rr_first > rr && tol2 > 0.0)
+                slow = CHUNK * std::log(rr / tol2) / std::log(rr_first / rr) > AMG_SWITCH_ITERS;
+            else if (rr > tol2) slow = true;   // no progress over the chunk
+        }
+        if (allow_amg && slow && P.settings.preconditioner == 1 && w == 0.0)
+        {
+            // block Jacobi's fast start (the high frequencies) is over, and what
+            // is left would take more than AMG_SWITCH_ITERS iterations at the
+            // observed rate (or the residual is still more than a factor
+            // sqrt(AMG_SWITCH_RATIO) above the target): restart with AMG
             const int it = P.hs->iters;
             if (iters_out) *iters_out = it;
             const int left = std::max(1, max_iters - it);
