@@ -118,17 +118,15 @@ __global__ void __launch_bounds__(128) k_elem_gradient(ElemLaunch L, Energy ener
 }
 
 /* value and gradient types of the second-order kernel: FP64 for the plain
-   path.  For the mixed path (FP32 Hessian) the value is double-float
-   (FP32-pipe arithmetic, ~48-bit significand) for elements up to k = 12, and
-   the gradient is double-float up to 9 derivatives -- which covers the
-   reduced tetrahedron (3 active vertices) -- and FP64 beyond (a 12-entry
-   double-float gradient next to 78-entry Hessians compiled for minutes and
-   only grew the register spills).  On this GPU FP64 runs at 1/70 of the FP32
-   rate, so an FP64 gradient bounds the kernel. */
+   path; for the mixed path double-float (FP32-pipe arithmetic, ~48-bit
+   significand) up to k = 8 and FP64 beyond.  The tetrahedron (k = 12, 9
+   derivatives after the translation reduction) is bound by register spills
+   of its Hessians, not by the FP64 pipe: with a double-float value and
+   gradient it measured 8.33 instead of 6.60 ms on 663,552 tets. */
 template <typename T, int K> struct ValOf { using type = double; };
-template <int K> struct ValOf<float, K> { using type = std::conditional_t<(K <= 12), DoubleFloatValue, double>; };
+template <int K> struct ValOf<float, K> { using type = std::conditional_t<(K <= 8), DoubleFloatValue, double>; };
 template <typename T, int K> struct GradOf { using type = double; };
-template <int K> struct GradOf<float, K> { using type = std::conditional_t<(K <= 9), DoubleFloat, double>; };
+template <int K> struct GradOf<float, K> { using type = std::conditional_t<(K <= 8), DoubleFloat, double>; };
 
 /* For k <= 8 the PSD projection runs in its own kernel (k_project_blocks)
    over the element blocks the evaluation kernel wrote: the evaluation needs
