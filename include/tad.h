@@ -194,6 +194,10 @@ typedef struct tad_term_eval_args {
        element kernels list there the elements whose Hessian is not
        translation invariant, which then get the general projection */
     uint32_t* proj_list_d;
+    /* LINESEARCH: NULL, or a device counter read at the start of the launch;
+       0 means no line search is still open (every group of a batched solve
+       has accepted a step) and the launch returns without work */
+    const int32_t* active_d;
 } tad_term_eval_args;
 
 typedef enum tad_eval_mode {

@@ -54,6 +54,7 @@ struct ElemLaunch
     double* out_J;           /* vector terms: residual gradients [n_elem][M][k] */
     double* out_Hv;          /* vector terms: packed residual Hessians [n_elem][M][k(k+1)/2] */
     uint32_t* proj_list;     /* HESSIAN_PROJ: [0] count, [1..] elements left for the general projection */
+    const int32_t* active;   /* LINESEARCH: NULL or a device counter; 0 = nothing to do */
 };
 
 template <int d, int N, typename Energy>
@@ -71,7 +72,7 @@ template <int d, int N, typename Energy, typename P = double>
 __global__ void __launch_bounds__(128) k_elem_linesearch(ElemLaunch L, Energy energy)
 {
     const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (e >= L.n_elem) return;
+    if (e >= L.n_elem || (L.active && *L.active == 0)) return;
     for (int j = 0; j < L.n_steps; ++j)
     {
         LineSearchElement<d, N, P> el{e, L.x, L.dir, P(L.steps[j])};
@@ -398,6 +399,7 @@ inline ElemLaunch make_launch(const tad_term_eval_args& a)
     L.out_J = a.out_J_d;
     L.out_Hv = a.out_Hv_d;
     L.proj_list = a.proj_list_d;
+    L.active = a.active_d;
     return L;
 }
 
@@ -485,7 +487,7 @@ template <int d, int N, int M, typename Energy>
 __global__ void __launch_bounds__(128) k_vec_linesearch(ElemLaunch L, Energy energy)
 {
     const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (e >= L.n_elem) return;
+    if (e >= L.n_elem || (L.active && *L.active == 0)) return;
     for (int j = 0; j < L.n_steps; ++j)
     {
         LineSearchElement<d, N, double> el{e, L.x, L.dir, L.steps[j]};

@@ -50,6 +50,7 @@ struct BatchScalars
     int32_t* iters;   // [m]
     int32_t* choice;  // [m] accepted trial, -1 none
     double* step;     // [m]
+    int32_t* searching;   // meshes without an accepted trial after the last selection
 };
 
 constexpr int LS_TRIALS = 16;
@@ -128,8 +129,12 @@ __device__ bool seg_finish(int ci, int m, double (&v)[NV], double* partials, int
 
 /* per-mesh sums of element-energy rows: out[m * stride_out + row] */
 __global__ void k_b_reduce_rows(const Chunk* ch, int n_chunks, const int32_t* mcb, const int32_t* mce, const double* ef,
-                                int64_t row_stride, double* partials, unsigned* counters, double* out, int out_stride)
+                                int64_t row_stride, double* partials, unsigned* counters, double* out, int out_stride,
+                                const int32_t* active = nullptr)
 {
+    // active: as for the line-search element kernels, 0 = nothing to sum (every block
+    // returns before touching the segment counters)
+    if (active && *active == 0) return;
     const int row = blockIdx.y;
     for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x)
     {
@@ -340,6 +345,7 @@ __global__ void k_b_ls_select(int n_meshes, int t0, int nt, const double* steps,
             return;
         }
     }
+    atomicAdd(S.searching, 1);   // the later trial launches return at once when none search
 }
 
 template <int d>
@@ -480,18 +486,27 @@ static tad_status record_iteration(Batch& B, int prec, double eps)
         k_b_settle<<<(B.n_meshes + 255) / 256, 256, 0, s>>>(B.n_meshes, B.S);
     }
     k_b_to_double<T><<<G, TH, 0, s>>>(n, xs, P.dx);
-    // 3. line search: d.g per mesh, 2 batches of 8 trials, per-mesh choice and step
+    // 3. line search: d.g per mesh; the full step alone, then batches of up to
+    // 8 trials that run only while some mesh has not accepted a step (the
+    // trial kernels read the count the selection leaves and return at once
+    // when it is 0); per-mesh choice and step
     k_b_dot<d><<<G, TH, 0, s>>>(B.vch, B.n_vch, B.vmcb, B.vmce, P.dx, P.g, B.partials, B.counters, B.S.dg);
-    for (int t0 = 0; t0 < LS_TRIALS; t0 += LS_BATCH)
+    for (int t0 = 0; t0 < LS_TRIALS;)
     {
+        const int nb = t0 == 0 ? 1 : std::min(LS_BATCH, LS_TRIALS - t0);
         double* save = P.steps;
         P.steps = B.steps + t0;
-        st = eval_elements(P, TAD_MODE_LINESEARCH, B.x, 0.0, P.precision, P.dx, LS_BATCH);
+        P.ls_active = t0 == 0 ? nullptr : B.S.searching;
+        st = eval_elements(P, TAD_MODE_LINESEARCH, B.x, 0.0, P.precision, P.dx, nb);
         P.steps = save;
+        P.ls_active = nullptr;
         if (st != TAD_OK) return st;
-        k_b_reduce_rows<<<dim3(G, LS_BATCH), TH, 0, s>>>(B.ech, B.n_ech, B.emcb, B.emce, P.ef, P.n_elem_total,
-                                                         B.partials, B.counters, B.S.ftr + t0, LS_TRIALS);
-        k_b_ls_select<<<(B.n_meshes + 255) / 256, 256, 0, s>>>(B.n_meshes, t0, LS_BATCH, B.steps, P.settings.ls_armijo, B.S);
+        k_b_reduce_rows<<<dim3(G, nb), TH, 0, s>>>(B.ech, B.n_ech, B.emcb, B.emce, P.ef, P.n_elem_total,
+                                                   B.partials, B.counters, B.S.ftr + t0, LS_TRIALS,
+                                                   t0 == 0 ? nullptr : B.S.searching);
+        TAD_CUDA_TRY(cudaMemsetAsync(B.S.searching, 0, sizeof(int32_t), s));
+        k_b_ls_select<<<(B.n_meshes + 255) / 256, 256, 0, s>>>(B.n_meshes, t0, nb, B.steps, P.settings.ls_armijo, B.S);
+        t0 += nb;
     }
     k_b_axpy<d><<<G, TH, 0, s>>>(B.vch, B.n_vch, B.x, P.dx, B.S, 0);
     (void)nh;
@@ -656,6 +671,7 @@ static tad_status batch_prepare(tad_batch* B)
         B->S.done = B->iscal;
         B->S.iters = B->iscal + nm;
         B->S.choice = B->iscal + 2 * nm;
+        B->S.searching = B->iscal + 3 * nm;
         TAD_CUDA_TRY(cudaMalloc(&B->steps, LS_TRIALS * sizeof(double)));
         std::vector<double> st(LS_TRIALS);
         double sv = 1.0;

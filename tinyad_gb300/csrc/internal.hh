@@ -152,6 +152,7 @@ struct Problem
     float *r32 = nullptr, *z32 = nullptr, *p32 = nullptr, *Ap32 = nullptr, *dx32 = nullptr, *dinv32 = nullptr;
     double *rhs = nullptr, *res = nullptr;
     double* x_trial = nullptr;   // Newton: the speculative full-step state x + d (n_vars, allocated on first use)
+    const int32_t* ls_active = nullptr;   // line-search launches: tad_term_eval_args.active_d (batched solves)
     bool defer_fp32 = false;     // Newton asks a loose mixed solve to leave its solution in dx32 ...
     bool solution_in_dx32 = false;   // ... and the solve says it did (P.dx not written)
     double* steps = nullptr;   // LS_BATCH trial step sizes (device)
