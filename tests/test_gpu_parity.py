@@ -416,3 +416,34 @@ def test_mixed_tight_newton_unconstrained(tad):
     # the function stays usable after such solves
     f, g, _ = fmx.eval_with_hessian_proj(xm)
     assert np.isfinite(f) and np.all(np.isfinite(g))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_newton_calls_continue(tad, precision):
+    """A solve stepped one call per iteration (the library then carries the
+    derivatives its speculative full step assembled into the next call) ends
+    where one multi-iteration call ends; an evaluation between calls, or a
+    changed x, falls back to evaluating at the call's start."""
+    w = meshes.disk_param(48, seed=3)
+    prec = tad.PREC_MIXED if precision == "mixed" else tad.PREC_FP64
+    kw = dict(precision=prec, pcg_rel_tol=1e-2, pcg_max_iters=2000, forcing=0)
+    fa = tad.ScalarFunction.from_workload(w, **kw)
+    fb = tad.ScalarFunction.from_workload(w, **kw)
+    xa, fha = fa.newton_solve(w.x0, 12)
+    xb = w.x0.copy()
+    fhb = []
+    for it in range(12):
+        if it == 6:
+            fb.eval_with_hessian_proj(xb)      # other evaluations invalidate the carried derivatives
+        if it == 9:
+            xb = xb + 0.0                      # same values: still a continuation
+        xb, fh = fb.newton_solve(xb, 1)
+        fhb.append(fh[0])
+    fhb.append(fh[-1])
+    assert rel_err(xb, xa) <= 1e-12, rel_err(xb, xa)
+    assert rel_err(np.array(fhb), fha) <= 1e-12
+    # a changed x is not a continuation: the call evaluates at its own start
+    xc = xb.copy()
+    xc[0] += 1e-7
+    xc2, fhc = fb.newton_solve(xc, 1)
+    assert abs(fhc[0] - fb.eval(xc)) <= 1e-12 * abs(fhc[0])

@@ -153,6 +153,18 @@ struct Problem
     double *rhs = nullptr, *res = nullptr;
     double* x_trial = nullptr;   // Newton: the speculative full-step state x + d (n_vars, allocated on first use)
     const int32_t* ls_active = nullptr;   // line-search launches: tad_term_eval_args.active_d (batched solves)
+    // Newton state kept across solver calls: the last call's final x and,
+    // when its last iteration took the speculative trial, the derivatives
+    // assembled there (valid for spec_eps / spec_prec until any other
+    // evaluation or a settings change)
+    double* last_x = nullptr;
+    bool last_x_valid = false;
+    bool spec_valid = false;
+    double spec_eps = 0.0;
+    int spec_prec = -1;
+    int streak = 0;                  // consecutive calls that continued from the previous call's x
+    int32_t* diff_flag = nullptr;    // device: x differs from last_x
+    int32_t* diff_flag_h = nullptr;  // pinned mirror
     bool defer_fp32 = false;     // Newton asks a loose mixed solve to leave its solution in dx32 ...
     bool solution_in_dx32 = false;   // ... and the solve says it did (P.dx not written)
     double* steps = nullptr;   // LS_BATCH trial step sizes (device)

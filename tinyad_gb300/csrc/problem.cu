@@ -290,6 +290,7 @@ tad_status ensure_finalized(Problem& P)
 tad_status eval_elements(Problem& P, int mode, const double* x, double eps, int precision,
                          const double* dir, int n_steps)
 {
+    P.spec_valid = false;   // the element and assembled buffers are about to change
     for (Term& T : P.terms)
     {
         tad_term_eval_args a{};
@@ -417,10 +418,12 @@ TAD_API tad_status tad_problem_destroy(tad_problem* P)
     void* bufs[] = {P->ef, P->eg, P->eH, P->bptr, P->bcol, P->diag, P->cptr, P->cidx, P->gptr, P->gidx,
                     P->x, P->g, P->H, P->H64, P->csr_tmp, P->r, P->z, P->p, P->Ap, P->dx, P->dinv,
                     P->r32, P->z32, P->p32, P->Ap32, P->dx32, P->dinv32, P->rhs, P->res, P->steps,
-                    P->partials, P->counters, P->ds, P->err, P->proj_list, P->steps_seq, P->x_trial};
+                    P->partials, P->counters, P->ds, P->err, P->proj_list, P->steps_seq, P->x_trial,
+                    P->last_x, P->diff_flag};
     for (void* b : bufs) dfree(b);
     if (P->hs) cudaFreeHost(P->hs);
     if (P->err_h) cudaFreeHost(P->err_h);
+    if (P->diff_flag_h) cudaFreeHost(P->diff_flag_h);
     if (P->pcg_graph) cudaGraphExecDestroy(P->pcg_graph);
     if (P->amg_graph) cudaGraphExecDestroy(P->amg_graph);
     if (P->Hd) cudaFree(P->Hd);
@@ -438,6 +441,8 @@ TAD_API tad_status tad_problem_set_settings(tad_problem* P, const tad_settings* 
     P->settings = *s;
     P->precision = s->precision;
     P->g0_norm = 0.0;
+    P->spec_valid = false;
+    P->last_x_valid = false;
     return TAD_OK;
 }
 

@@ -420,6 +420,14 @@ __global__ void k_ls_select(int n, const double* __restrict__ steps, double c, D
     }
 }
 
+/* *flag = 1 if a and b differ in any bit */
+__global__ void k_differs(int64_t n, const double* __restrict__ a, const double* __restrict__ b, int32_t* flag)
+{
+    bool diff = false;
+    GRID_STRIDE(i, n) diff = diff || (__double_as_longlong(a[i]) != __double_as_longlong(b[i]));
+    if (__any_sync(0xffffffffu, diff) && (threadIdx.x & 31) == 0) *flag = 1;
+}
+
 /* out = a + b */
 __global__ void k_add(int64_t n, const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ out)
 {
@@ -991,19 +999,50 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
     // last iteration of a call does not speculate (its derivatives would be
     // discarded).  The accepted state alternates between x and P.x_trial; x
     // holds it on return.
+    //
+    // Across calls: a call that starts from the exact x the previous call
+    // returned (a device compare, one host round trip) continues that
+    // solve.  Once calls have continued each other twice in a row, the last
+    // iteration of a call speculates too, and the next continuing call starts
+    // from the derivatives it assembled (as an iteration inside one call
+    // would), provided nothing else has evaluated on the problem since and
+    // eps and precision are the same.
     const bool forcing = P.settings.forcing == 1;
     const int ls_max = P.settings.ls_max_iters > 0 ? P.settings.ls_max_iters : 64;
-    if (!P.x_trial) TAD_CUDA_TRY(cudaMalloc(&P.x_trial, std::max<int64_t>(P.n_vars, 1) * sizeof(double)));
+    const int64_t n = P.n_vars;
+    if (!P.x_trial) TAD_CUDA_TRY(cudaMalloc(&P.x_trial, std::max<int64_t>(n, 1) * sizeof(double)));
+    if (!P.last_x) TAD_CUDA_TRY(cudaMalloc(&P.last_x, std::max<int64_t>(n, 1) * sizeof(double)));
+    if (!P.diff_flag) TAD_CUDA_TRY(cudaMalloc(&P.diff_flag, sizeof(int32_t)));
+    if (!P.diff_flag_h) TAD_CUDA_TRY(cudaMallocHost(&P.diff_flag_h, sizeof(int32_t)));
     s = ensure_step_sequence(P, 1.0, ls_max);
     if (s != TAD_OK) return s;
+    bool continues = false;
+    if (P.last_x_valid)
+    {
+        TAD_CUDA_TRY(cudaMemsetAsync(P.diff_flag, 0, sizeof(int32_t), st));
+        k_differs<<<RED_BLOCKS, RED_THREADS, 0, st>>>(n, x, P.last_x, P.diff_flag);
+        P.n_launches += 1;
+        TAD_CUDA_TRY(cudaMemcpyAsync(P.diff_flag_h, P.diff_flag, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        TAD_CUDA_TRY(cudaStreamSynchronize(st));
+        continues = *P.diff_flag_h == 0;
+    }
+    P.streak = continues ? P.streak + 1 : 0;
+    const bool reuse = continues && P.spec_valid && P.spec_eps == eps && P.spec_prec == prec;
+    P.spec_valid = false;
     double* cur = x;
     double* spare = P.x_trial;
+    bool have_derivs = reuse;   // derivatives at cur already assembled (accepted speculative step)
     auto finish = [&](tad_status rs) {
-        if (cur != x) cudaMemcpyAsync(x, cur, P.n_vars * sizeof(double), cudaMemcpyDeviceToDevice, st);
+        if (cur != x) cudaMemcpyAsync(x, cur, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
+        const bool ok = rs == TAD_OK;
+        if (ok) cudaMemcpyAsync(P.last_x, x, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
         cudaStreamSynchronize(st);
+        P.last_x_valid = ok;
+        P.spec_valid = ok && have_derivs;
+        P.spec_eps = eps;
+        P.spec_prec = prec;
         return rs;
     };
-    bool have_derivs = false;   // derivatives at cur already assembled (accepted speculative step)
     bool speculate = true;
     double f = 0.0;
     int it = 0;
@@ -1034,7 +1073,9 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
             if (P.g0_norm == 0.0) P.g0_norm = gnorm;   // first iteration since create / set_settings
             if (P.g0_norm > 0.0) tol = std::max(tol, std::min(0.5, std::sqrt(gnorm / P.g0_norm)));
         }
-        const bool spec_now = speculate && it + 1 < n_iters;   // the last iteration has no next one to evaluate for
+        // the last iteration speculates only once calls have continued each
+        // other twice in a row (a caller stepping a solve call by call)
+        const bool spec_now = speculate && (it + 1 < n_iters || P.streak >= 2);
         int pit = 0;
         P.defer_fp32 = spec_now;
         P.solution_in_dx32 = false;
