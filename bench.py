@@ -42,7 +42,7 @@ UNIT = "Newton iters/s"
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one
 # ncu --set full capture of the same workload (profiles/k_elem_hessian_k_project_blocks_mixed_disk1024.md,
 # profiles/k_pcg_spmv_fused_fp32_disk1024.md); workloads without a capture report null
-NCU_TRAFFIC = {("disk1024", "mixed"): {"elem": (131.3e6 + 190.8e6) + (157.5e6 + 92.7e6), "spmv": 138.0e6 + 5.7e6}}
+NCU_TRAFFIC = {("disk1024", "mixed"): {"elem": (131.3e6 + 195.9e6) + (157.5e6 + 100.1e6), "spmv": 138.0e6 + 5.1e6}}
 
 
 def parse():
@@ -510,12 +510,16 @@ def main():
     ms = reduce_max(ms, dist, "cuda")
     value = aggregate_rate(world, args.steps, ms / 1e3)
 
-    # end to end through the C ABI with host buffers (pinned), the same K
-    # iterations from the same post-warm-up state, one call per step
+    # end to end through the C ABI with host buffers (pinned), one call per
+    # step, the same protocol as the timed region: W untimed warm-up calls
+    # from the initial state, then the K timed calls (Newton iterations
+    # W+1..W+K, as above); every call copies x in and out
     n = w.n_vars
     xh = torch.empty(n, dtype=torch.float64, pin_memory=True)
-    xh.copy_(x_warm.cpu())
+    xh.copy_(torch.from_numpy(w.x0))
     xh_np = xh.numpy()
+    for _ in range(args.warmup):
+        fn.newton_solve_inplace(xh_np, 1)
     torch.cuda.synchronize()
     barrier()
     t0 = time.perf_counter()
@@ -524,7 +528,9 @@ def main():
     t_e2e = time.perf_counter() - t0
     t_e2e = reduce_max(t_e2e, dist, "cuda")
     e2e = {"value": aggregate_rate(world, args.steps, t_e2e), "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n + 8,
-           "path": "tad_newton_solve (C ABI) with pinned host x in and out every step, same iterations as the timed region"}
+           "path": "tad_newton_solve (C ABI), one call per Newton iteration with pinned host x copied in and out every "
+                   "call; W untimed warm-up calls from the initial state, then the K timed calls (iterations W+1..W+K, "
+                   "as the timed region)"}
 
     # kernel figures at the final state (CUDA events on the library stream)
     prof = fn.profile_kernels(x.data_ptr(), reps=5)
