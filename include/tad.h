@@ -194,9 +194,11 @@ typedef struct tad_term_eval_args {
        element kernels list there the elements whose Hessian is not
        translation invariant, which then get the general projection */
     uint32_t* proj_list_d;
-    /* LINESEARCH: NULL, or a device counter read at the start of the launch;
-       0 means no line search is still open (every group of a batched solve
-       has accepted a step) and the launch returns without work */
+    /* LINESEARCH, HESSIAN, HESSIAN_PROJ: NULL, or a device int read at the
+       start of the launch; 0 means the launch has nothing to do (every group
+       of a batched line search has accepted a step; a speculative evaluation
+       whose linear solve has not converged) and it returns without work or
+       outputs */
     const int32_t* active_d;
 } tad_term_eval_args;
 

@@ -54,7 +54,7 @@ struct ElemLaunch
     double* out_J;           /* vector terms: residual gradients [n_elem][M][k] */
     double* out_Hv;          /* vector terms: packed residual Hessians [n_elem][M][k(k+1)/2] */
     uint32_t* proj_list;     /* HESSIAN_PROJ: [0] count, [1..] elements left for the general projection */
-    const int32_t* active;   /* LINESEARCH: NULL or a device counter; 0 = nothing to do */
+    const int32_t* active;   /* NULL or a device int; 0 = nothing to do (line search, second order) */
 };
 
 template <int d, int N, typename Energy>
@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(128, ElemHessianMinBlocks<d * N, T>::value) k_
     using G = typename GradOf<T, kd>::type;
     using S = Scalar<kd, T, true, typename ValOf<T, k>::type, G>;
     const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (e >= L.n_elem) return;
+    if (e >= L.n_elem || (L.active && *L.active == 0)) return;
     ActiveElement<d, N, S, reduced> el;
     el.handle = e;
     el.x = L.x;
@@ -343,7 +343,7 @@ __global__ void __launch_bounds__(128) k_project_blocks(ElemLaunch L, T eps)
     constexpr int k = d * N;
     constexpr int BS = N * (N + 1) / 2 * d * d;
     const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (e >= L.n_elem) return;
+    if (e >= L.n_elem || (L.active && *L.active == 0)) return;
     T* Hblocks = (T*)L.out_H;
     T hb[BS];
     load_row<T, BS>(Hblocks, e, hb);
@@ -508,7 +508,7 @@ __global__ void __launch_bounds__(128) k_vec_first_order(ElemLaunch L, Energy en
     constexpr int NP = N * (N + 1) / 2;
     using S = Scalar<k, double, false>;
     const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (e >= L.n_elem) return;
+    if (e >= L.n_elem || (L.active && *L.active == 0)) return;
     ActiveElement<d, N, S> el;
     el.handle = e;
     el.x = L.x;

@@ -496,10 +496,10 @@ static tad_status record_iteration(Batch& B, int prec, double eps)
         const int nb = t0 == 0 ? 1 : std::min(LS_BATCH, LS_TRIALS - t0);
         double* save = P.steps;
         P.steps = B.steps + t0;
-        P.ls_active = t0 == 0 ? nullptr : B.S.searching;
+        P.launch_guard = t0 == 0 ? nullptr : B.S.searching;
         st = eval_elements(P, TAD_MODE_LINESEARCH, B.x, 0.0, P.precision, P.dx, nb);
         P.steps = save;
-        P.ls_active = nullptr;
+        P.launch_guard = nullptr;
         if (st != TAD_OK) return st;
         k_b_reduce_rows<<<dim3(G, nb), TH, 0, s>>>(B.ech, B.n_ech, B.emcb, B.emce, P.ef, P.n_elem_total,
                                                    B.partials, B.counters, B.S.ftr + t0, LS_TRIALS,

@@ -37,6 +37,12 @@ constexpr int RED_BLOCKS = 608;    // 4 x 152 SMs: fixed grid of the reductions
    reduction grid: measured faster there) */
 constexpr int PCG_BLOCKS = 1216;
 constexpr int RED_THREADS = 256;
+/* mixed-precision solves at least this loose are one FP32 PCG pass, with no
+   FP64 refinement */
+constexpr double MIXED_LOOSE_TOL = 1e-4;
+/* internal status of pcg_solve under pcg_async: the first iteration is
+   enqueued and not yet checked */
+constexpr tad_status PCG_PENDING = (tad_status)1000;
 
 void set_error(const std::string& msg);
 
@@ -152,7 +158,11 @@ struct Problem
     float *r32 = nullptr, *z32 = nullptr, *p32 = nullptr, *Ap32 = nullptr, *dx32 = nullptr, *dinv32 = nullptr;
     double *rhs = nullptr, *res = nullptr;
     double* x_trial = nullptr;   // Newton: the speculative full-step state x + d (n_vars, allocated on first use)
-    const int32_t* ls_active = nullptr;   // line-search launches: tad_term_eval_args.active_d (batched solves)
+    // tad_term_eval_args.active_d of element launches: NULL, or a device int
+    // that is 0 when the launch has nothing to do (batched line searches whose
+    // meshes all accepted; the Newton loop's speculative evaluation before the
+    // PCG has converged)
+    const int32_t* launch_guard = nullptr;
     // Newton state kept across solver calls: the last call's final x and,
     // when its last iteration took the speculative trial, the derivatives
     // assembled there (valid for spec_eps / spec_prec until any other
@@ -167,6 +177,8 @@ struct Problem
     int32_t* diff_flag_h = nullptr;  // pinned mirror
     bool defer_fp32 = false;     // Newton asks a loose mixed solve to leave its solution in dx32 ...
     bool solution_in_dx32 = false;   // ... and the solve says it did (P.dx not written)
+    bool pcg_async = false;      // Newton: return PCG_PENDING after the first iteration, without a host check
+    bool pcg_resume = false;     // Newton: continue a PCG_PENDING solve (its first check is in P.hs)
     double* steps = nullptr;   // LS_BATCH trial step sizes (device)
     double* steps_seq = nullptr;   // the line search's whole step sequence (device), for steps_key
     int steps_seq_cap = 0;

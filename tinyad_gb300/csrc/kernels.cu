@@ -48,8 +48,10 @@ __device__ __forceinline__ double block_sum(double v, double* sh)
 }
 
 __global__ void __launch_bounds__(RED_THREADS) k_reduce_rows(const double* ef, int64_t n, int64_t stride,
-                                                             double* partials, unsigned* counters, double* out)
+                                                             double* partials, unsigned* counters, double* out,
+                                                             const int32_t* guard)
 {
+    if (guard && *guard == 0) return;   // every block returns before touching the counters
     __shared__ double sh[32];
     __shared__ bool last;
     const int row = blockIdx.y;
@@ -85,7 +87,7 @@ void launch_reduce_f(Problem& P, int n_rows, double* out)
     const int64_t n = P.n_elem_total;
     int blocks = (int)std::min<int64_t>(RED_BLOCKS, std::max<int64_t>(1, (n + 4095) / 4096));
     dim3 grid(blocks, n_rows);
-    k_reduce_rows<<<grid, RED_THREADS, 0, P.stream>>>(P.ef, n, n, P.partials, P.counters, out);
+    k_reduce_rows<<<grid, RED_THREADS, 0, P.stream>>>(P.ef, n, n, P.partials, P.counters, out, P.launch_guard);
 }
 
 /* g[u] = sum of handle u's element gradient slots, in element order.  Acc =
@@ -170,8 +172,9 @@ __global__ void __launch_bounds__(RED_THREADS) k_assemble_grad_newton(int64_t nh
                                                                        const int32_t* __restrict__ gidx,
                                                                        const double* __restrict__ eg, double* __restrict__ g,
                                                                        double* __restrict__ rhs, double* partials,
-                                                                       unsigned* counter, DevScalars* ds)
+                                                                       unsigned* counter, DevScalars* ds, const int32_t* guard)
 {
+    if (guard && *guard == 0) return;   // every block returns before touching the counter
     double part[1] = {0.0};
     GRID_STRIDE(u, nh)
     {
@@ -216,11 +219,11 @@ static void assemble_grad_newton_as(Problem& P)
     switch (P.d)
     {
     case 1: k_assemble_grad_newton<1, Acc, Pairs><<<grid, RED_THREADS, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g, P.rhs,
-                                                                                      P.partials, P.counters + 5, P.ds); break;
+                                                                                      P.partials, P.counters + 5, P.ds, P.launch_guard); break;
     case 2: k_assemble_grad_newton<2, Acc, Pairs><<<grid, RED_THREADS, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g, P.rhs,
-                                                                                      P.partials, P.counters + 5, P.ds); break;
+                                                                                      P.partials, P.counters + 5, P.ds, P.launch_guard); break;
     default: k_assemble_grad_newton<3, Acc, Pairs><<<grid, RED_THREADS, 0, P.stream>>>(P.n_handles, P.gptr, P.gidx, P.eg, P.g, P.rhs,
-                                                                                       P.partials, P.counters + 5, P.ds); break;
+                                                                                       P.partials, P.counters + 5, P.ds, P.launch_guard); break;
     }
 }
 
@@ -233,10 +236,10 @@ void launch_assemble_grad_newton(Problem& P, int precision, bool pairs)
 
 template <int d, typename T>
 __global__ void k_assemble_hess(int64_t nb, const int32_t* __restrict__ cptr, const int32_t* __restrict__ cidx,
-                                const T* __restrict__ eH, T* __restrict__ H)
+                                const T* __restrict__ eH, T* __restrict__ H, const int32_t* guard)
 {
     const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (b >= nb) return;
+    if (b >= nb || (guard && *guard == 0)) return;
     T acc[d * d];
 #pragma unroll
     for (int i = 0; i < d * d; ++i) acc[i] = T(0);
@@ -280,9 +283,9 @@ void launch_assemble_hess(Problem& P, int precision)
     if (P.nb == 0) return;
 #define TAD_ASM(D)                                                                                         \
     if (precision == TAD_PREC_MIXED)                                                                       \
-        k_assemble_hess<D, float><<<grid, 256, 0, P.stream>>>(P.nb, P.cptr, P.cidx, (const float*)P.eH, (float*)P.H); \
+        k_assemble_hess<D, float><<<grid, 256, 0, P.stream>>>(P.nb, P.cptr, P.cidx, (const float*)P.eH, (float*)P.H, P.launch_guard); \
     else                                                                                                   \
-        k_assemble_hess<D, double><<<grid, 256, 0, P.stream>>>(P.nb, P.cptr, P.cidx, (const double*)P.eH, (double*)P.H);
+        k_assemble_hess<D, double><<<grid, 256, 0, P.stream>>>(P.nb, P.cptr, P.cidx, (const double*)P.eH, (double*)P.H, P.launch_guard);
     switch (P.d)
     {
     case 1: TAD_ASM(1); break;

@@ -306,7 +306,7 @@ tad_status eval_elements(Problem& P, int mode, const double* x, double eps, int 
         a.error_d = P.err;
         a.stream = P.stream;
         a.proj_list_d = P.proj_list;
-        a.active_d = mode == TAD_MODE_LINESEARCH ? P.ls_active : nullptr;
+        a.active_d = P.launch_guard;
         a.n_outputs = T.M;
         if (T.M > 0)
         {

@@ -375,8 +375,10 @@ __global__ void __launch_bounds__(RED_THREADS) k_residual(int64_t nh, const int3
 
 /* dg = d.g, decrement = -0.5 dg */
 __global__ void __launch_bounds__(RED_THREADS) k_dot_dg(int64_t n, const double* __restrict__ a, const double* __restrict__ b,
-                                                        double* partials, unsigned* counter, DevScalars* ds)
+                                                        double* partials, unsigned* counter, DevScalars* ds,
+                                                        const int32_t* guard = nullptr)
 {
+    if (guard && *guard == 0) return;   // guard: a device int, 0 = skip (every block, before the counter)
     double part[1] = {0.0};
     GRID_STRIDE(i, n) part[0] += a[i] * b[i];
     double tot[1];
@@ -401,9 +403,10 @@ __global__ void __launch_bounds__(RED_THREADS) k_neg_gg(int64_t n, const double*
 }
 
 /* first trial j (of n) with f_trial[j] <= f + c s_j dg (LineSearch.hh:14-24, :53) */
-__global__ void k_ls_select(int n, const double* __restrict__ steps, double c, DevScalars* ds, int adopt = 0)
+__global__ void k_ls_select(int n, const double* __restrict__ steps, double c, DevScalars* ds, int adopt = 0,
+                            const int32_t* guard = nullptr)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (threadIdx.x != 0 || blockIdx.x != 0 || (guard && *guard == 0)) return;
     ds->ls_choice = -1;
     for (int j = 0; j < n; ++j)
     {
@@ -429,8 +432,10 @@ __global__ void k_differs(int64_t n, const double* __restrict__ a, const double*
 }
 
 /* out = a + b */
-__global__ void k_add(int64_t n, const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ out)
+__global__ void k_add(int64_t n, const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ out,
+                      const int32_t* guard = nullptr)
 {
+    if (guard && *guard == 0) return;
     GRID_STRIDE(i, n) out[i] = a[i] + b[i];
 }
 
@@ -443,8 +448,9 @@ __global__ void k_add(int64_t n, const double* __restrict__ a, const double* __r
 __global__ void __launch_bounds__(RED_THREADS) k_step_prepare(int64_t n, const float* __restrict__ d32, const double* __restrict__ x,
                                                               const double* __restrict__ g, double* __restrict__ d,
                                                               double* __restrict__ xt, double* partials, unsigned* counter,
-                                                              DevScalars* ds)
+                                                              DevScalars* ds, const int32_t* guard)
 {
+    if (guard && *guard == 0) return;   // every block, before the counter
     float pf = 0.0f;
     GRID_STRIDE(i, n)
     {
@@ -596,10 +602,18 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
     const T* H = (const T*)P.H;
     const int64_t nh = P.n_handles;
     cudaStream_t s = P.stream;
-    k_pcg_init<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, b, xs, r, z, p, Ap, dinv, P.diag, H, w, P.partials, P.counters, P.ds,
-                                                        rel_tol, max_iters);
-    P.n_launches += 1;
-    TAD_CUDA_TRY(cudaGetLastError());
+    // P.pcg_async: enqueue init and the first iteration and return PCG_PENDING
+    // (the caller checks P.hs->done after its own host round trip);
+    // P.pcg_resume: that first iteration ran and P.hs holds its check
+    const bool resume = P.pcg_resume;
+    P.pcg_resume = false;
+    if (!resume)
+    {
+        k_pcg_init<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, b, xs, r, z, p, Ap, dinv, P.diag, H, w, P.partials, P.counters,
+                                                            P.ds, rel_tol, max_iters);
+        P.n_launches += 1;
+        TAD_CUDA_TRY(cudaGetLastError());
+    }
     // The first iteration is launched directly and checked at once (early
     // Newton iterations converge in one); after that, CHUNK iterations
     // captured once per (precision, solution buffer) are replayed, with the
@@ -630,9 +644,13 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
     {
         if (replays == 0)
         {
-            launch_iteration();
-            P.n_launches += 2;
-            TAD_CUDA_TRY(cudaGetLastError());
+            if (!resume)
+            {
+                launch_iteration();
+                P.n_launches += 2;
+                TAD_CUDA_TRY(cudaGetLastError());
+                if (P.pcg_async) return PCG_PENDING;
+            }
         }
         else
         {
@@ -654,8 +672,11 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
             for (int k = 0; k < replays; ++k) TAD_CUDA_TRY(cudaGraphLaunch(P.pcg_graph, s));
             P.n_launches += 2 * CHUNK * replays;
         }
-        TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
-        TAD_CUDA_TRY(cudaStreamSynchronize(s));
+        if (!(resume && replays == 0))
+        {
+            TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
+            TAD_CUDA_TRY(cudaStreamSynchronize(s));
+        }
         if (P.hs->done) break;
         if (replays == 0) rr_first = P.hs->rr;
         bool slow = false;
@@ -741,12 +762,13 @@ static tad_status pcg_dispatch(Problem& P, const double* b, double* xsol, int pr
     // MIN_PASS_GAIN (or the passes run out) the rest is solved in FP64 on an
     // FP64 copy of the FP32 Hessian (same matrix, so the result is still exact
     // to the FP32-evaluated Hessian).
-    constexpr double LOOSE_TOL = 1e-4;
+    constexpr double LOOSE_TOL = MIXED_LOOSE_TOL;
     constexpr double MIN_PASS_GAIN = 100.0;
     const double tol = P.settings.refine_rel_tol;
     const double inner_tol = std::max(rel_tol, 1e-6);
     int total = 0;
     tad_status st = pcg_core<d, float>(P, b, P.dx32, 0.0, inner_tol, max_iters, &total, P.r32, P.z32, P.p32, P.Ap32, P.dinv32, 1);
+    if (st == PCG_PENDING) return st;   // async first iteration (loose tolerances only)
     const double bb = P.hs->bb;
     if (rel_tol >= LOOSE_TOL || bb == 0.0)
     {
@@ -949,25 +971,29 @@ tad_status line_search_device(Problem& P, double* x, const double* d, double f, 
    current energy if it passes).  Returns the selection in P.hs after one
    host round trip; the caller adopts x_t (its derivatives are then already
    assembled) or continues the line search at trial 2. */
-static tad_status speculative_first_trial(Problem& P, const double* x, double* d, double* xt, double eps, bool d_in_fp32)
+static tad_status speculative_first_trial(Problem& P, const double* x, double* d, double* xt, double eps, bool d_in_fp32,
+                                         const int32_t* guard = nullptr)
 {
+    // guard (the PCG's done flag): every kernel here returns at once while it
+    // is 0, so the block can be enqueued behind an unchecked PCG iteration
     cudaStream_t s = P.stream;
     if (d_in_fp32)
     {
-        k_step_prepare<<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_vars, P.dx32, x, P.g, d, xt, P.partials, P.counters + 4, P.ds);
+        k_step_prepare<<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_vars, P.dx32, x, P.g, d, xt, P.partials, P.counters + 4, P.ds, guard);
         P.n_launches += 1;
     }
     else
     {
-        k_dot_dg<<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_vars, d, P.g, P.partials, P.counters + 4, P.ds);
-        k_add<<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_vars, x, d, xt);
+        k_dot_dg<<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_vars, d, P.g, P.partials, P.counters + 4, P.ds, guard);
+        k_add<<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_vars, x, d, xt, guard);
         P.n_launches += 2;
     }
+    P.launch_guard = guard;
     tad_status st = eval_elements(P, TAD_MODE_HESSIAN_PROJ, xt, eps, P.precision);
+    if (st == TAD_OK) st = assemble(P, true, true, P.precision, P.ds->f_trial, true);
+    P.launch_guard = nullptr;
     if (st != TAD_OK) return st;
-    st = assemble(P, true, true, P.precision, P.ds->f_trial, true);
-    if (st != TAD_OK) return st;
-    k_ls_select<<<1, 32, 0, s>>>(1, P.steps_seq, P.settings.ls_armijo, P.ds, 1);
+    k_ls_select<<<1, 32, 0, s>>>(1, P.steps_seq, P.settings.ls_armijo, P.ds, 1, guard);
     P.n_launches += 1;
     TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
     TAD_CUDA_TRY(cudaMemcpyAsync(P.err_h, P.err, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
@@ -1044,6 +1070,8 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
         return rs;
     };
     bool speculate = true;
+    bool all_builtin = true;
+    for (const Term& T : P.terms) all_builtin = all_builtin && T.energy >= 0;
     double f = 0.0;
     int it = 0;
     for (; it < n_iters; ++it)
@@ -1076,11 +1104,43 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
         // the last iteration speculates only once calls have continued each
         // other twice in a row (a caller stepping a solve call by call)
         const bool spec_now = speculate && (it + 1 < n_iters || P.streak >= 2);
+        // The speculative trial is enqueued right behind the PCG's first
+        // iteration, guarded by its done flag, so that one host round trip
+        // serves both when the first iteration converges (it does in most
+        // iterations of a solve).  Only for one-pass solves (FP64, or mixed at
+        // a loose tolerance) and built-in energies, whose kernels honour the
+        // guard.
+        const bool async = spec_now && !forcing && all_builtin && (prec != TAD_PREC_MIXED || tol >= MIXED_LOOSE_TOL);
         int pit = 0;
         P.defer_fp32 = spec_now;
         P.solution_in_dx32 = false;
+        P.pcg_async = async;
         s = pcg_solve(P, P.rhs, P.dx, 0.0, prec, tol, P.settings.pcg_max_iters, &pit);
-        const bool d_in_fp32 = P.solution_in_dx32;
+        P.pcg_async = false;
+        bool trial_done = false;
+        bool d_in_fp32 = P.solution_in_dx32;
+        if (s == PCG_PENDING)
+        {
+            // a loose mixed solve leaves its solution in dx32, FP64 in P.dx
+            d_in_fp32 = prec == TAD_PREC_MIXED;
+            s = speculative_first_trial(P, cur, P.dx, spare, eps, d_in_fp32, &P.ds->done);
+            if (s != TAD_OK) return finish(s);
+            if (P.hs->done)
+            {
+                trial_done = true;
+                pit = P.hs->iters;
+                s = (P.hs->breakdown || !(P.hs->rr <= P.hs->tol2)) ? TAD_ERR_PCG_NOCONV : TAD_OK;
+            }
+            else
+            {
+                // not converged in one iteration: the guarded block did nothing
+                P.pcg_resume = true;
+                P.solution_in_dx32 = false;
+                s = pcg_solve(P, P.rhs, P.dx, 0.0, prec, tol, P.settings.pcg_max_iters, &pit);
+                P.pcg_resume = false;
+                d_in_fp32 = P.solution_in_dx32;
+            }
+        }
         P.defer_fp32 = false;
         P.solution_in_dx32 = false;
         P.pcg_iters_total += pit;
@@ -1092,8 +1152,8 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
         have_derivs = false;
         if (spec_now)
         {
-            s = speculative_first_trial(P, cur, P.dx, spare, eps, d_in_fp32);
-            if (s != TAD_OK) return finish(s);
+            if (!trial_done) s = speculative_first_trial(P, cur, P.dx, spare, eps, d_in_fp32);
+            if (s != TAD_OK && s != TAD_ERR_PCG_NOCONV) return finish(s);
             const int choice = P.hs->ls_choice;
             if (choice == -2)
                 return finish(fail(TAD_ERR_NONFINITE, "Assertion failed: f_new == f_new (NaN energy in line search)"));
