@@ -210,6 +210,10 @@ struct Problem
     double g0_norm = 0.0;      // |g| at the first iteration of the last solve
     int64_t n_launches = 0;    // kernels launched by this problem (cumulative)
     cudaEvent_t ev[8] = {};
+    // Newton stage timing: 5 events per iteration, read after the loop (no
+    // per-iteration event wait on the host's critical path)
+    static constexpr int STAGE_ITERS = 256;
+    std::vector<cudaEvent_t> stage_ev;
     bool timing = false;
 };
 

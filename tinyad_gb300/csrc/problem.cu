@@ -430,6 +430,7 @@ TAD_API tad_status tad_problem_destroy(tad_problem* P)
     if (P->corr) cudaFree(P->corr);
     amg_free(*P);
     for (auto& e : P->ev) if (e) cudaEventDestroy(e);
+    for (auto& e : P->stage_ev) if (e) cudaEventDestroy(e);
     if (P->stream) cudaStreamDestroy(P->stream);
     delete P;
     return TAD_OK;

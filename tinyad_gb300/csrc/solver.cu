@@ -271,6 +271,80 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_spmv_fused(int64_t nh, cons
     }
 }
 
+/* The same SpMV with L lanes per block row (CSR-vector form): lane l of a
+   row's group handles blocks l, l + L, ...; consecutive lanes read
+   consecutive blocks and column ids (coalesced), and the partial products
+   are summed by xor shuffles within the group.  Warps loop over uniform row
+   bases (32 / L rows each), so every lane takes part in every shuffle. */
+template <int d, typename T, int L>
+__global__ void __launch_bounds__(RED_THREADS) k_pcg_spmv_vec(int64_t nh, const int32_t* __restrict__ bptr,
+                                                              const int32_t* __restrict__ bcol, const T* __restrict__ H,
+                                                              const T* __restrict__ z, T* __restrict__ p, T* __restrict__ Ap,
+                                                              double* partials, unsigned* counter, DevScalars* ds)
+{
+    static_assert(L >= d && 32 % L == 0, "lanes per row");
+    if (*(volatile int32_t*)&ds->done) return;
+    const T beta = from_double<T>(ds->beta);
+    T part = T(0);
+    constexpr int RPW = 32 / L;   // rows per warp pass
+    const int lane = threadIdx.x & (L - 1);
+    const int sub = (threadIdx.x & 31) / L;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t base = warp * RPW; base < nh; base += n_warps * RPW)
+    {
+        const int64_t u = base + sub;
+        T y[d];
+#pragma unroll
+        for (int i = 0; i < d; ++i) y[i] = T(0);
+        if (u < nh)
+        {
+            const int32_t b1 = bptr[u + 1];
+            for (int32_t b = bptr[u] + lane; b < b1; b += L)
+            {
+                const int64_t v = __ldg(bcol + b);
+                T B[d * d], zv[d];
+                load_block<d, T>(H + (int64_t)b * d * d, B);
+                load_vec<d, T>(z + v * d, zv);
+#pragma unroll
+                for (int i = 0; i < d; ++i)
+#pragma unroll
+                    for (int j = 0; j < d; ++j) y[i] += B[i * d + j] * zv[j];
+            }
+        }
+#pragma unroll
+        for (int off = L / 2; off > 0; off >>= 1)
+#pragma unroll
+            for (int i = 0; i < d; ++i) y[i] += __shfl_xor_sync(0xffffffffu, y[i], off, L);
+        if (u < nh && lane < d)
+        {
+            // lane i of the group owns entry i of the row
+            T yi = y[0];
+#pragma unroll
+            for (int i = 1; i < d; ++i) if (lane == i) yi = y[i];
+            const int64_t q = u * d + lane;
+            const T apn = yi + beta * Ap[q];
+            const T pn = z[q] + beta * p[q];
+            Ap[q] = apn;
+            p[q] = pn;
+            part += pn * apn;
+        }
+    }
+    double v[1] = {as_double(part)}, tot[1];
+    if (!grid_sum<1>(v, partials, counter, tot)) return;
+    if (threadIdx.x == 0)
+    {
+        ds->pAp = tot[0];
+        if (!(tot[0] > 0.0) || !isfinite(tot[0]))
+        {
+            ds->breakdown = 1;
+            ds->done = 1;
+            ds->alpha = 0.0;
+        }
+        else ds->alpha = ds->rz / tot[0];
+    }
+}
+
 template <int d> struct SpmvGroup { static constexpr int value = d == 3 ? 16 : 8; };
 
 template <int d, typename T>
@@ -1069,6 +1143,12 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
         P.spec_prec = prec;
         return rs;
     };
+    if (P.stage_ev.empty())
+    {
+        P.stage_ev.resize(5 * Problem::STAGE_ITERS, nullptr);
+        for (auto& e : P.stage_ev) TAD_CUDA_TRY(cudaEventCreate(&e));
+    }
+    auto ev = [&](int i, int k) { return P.stage_ev[5 * std::min(i, Problem::STAGE_ITERS - 1) + k]; };
     bool speculate = true;
     bool all_builtin = true;
     for (const Term& T : P.terms) all_builtin = all_builtin && T.energy >= 0;
@@ -1076,20 +1156,20 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
     int it = 0;
     for (; it < n_iters; ++it)
     {
-        cudaEventRecord(P.ev[0], st);
+        cudaEventRecord(ev(it, 0), st);
         if (!have_derivs)
         {
             s = eval_elements(P, TAD_MODE_HESSIAN_PROJ, cur, eps, prec);
             if (s != TAD_OK) return finish(s);
         }
-        cudaEventRecord(P.ev[1], st);
+        cudaEventRecord(ev(it, 1), st);
         if (!have_derivs)
         {
             // f, g, H, and rhs = -g with |g|^2 (an accepted speculative step assembled them already)
             s = assemble(P, true, true, prec, nullptr, true);
             if (s != TAD_OK) return finish(s);
         }
-        cudaEventRecord(P.ev[2], st);
+        cudaEventRecord(ev(it, 2), st);
         double tol = P.settings.pcg_rel_tol;
         if (forcing)
         {
@@ -1145,7 +1225,7 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
         P.solution_in_dx32 = false;
         P.pcg_iters_total += pit;
         if (s != TAD_OK && s != TAD_ERR_PCG_NOCONV) return finish(s);
-        cudaEventRecord(P.ev[3], st);
+        cudaEventRecord(ev(it, 3), st);
         bool found = false;
         double fn = 0.0;
         int trials = 0;
@@ -1186,13 +1266,7 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
         // speculative step replaced there)
         f = have_derivs ? P.hs->f_prev : P.hs->f;
         if (f_hist) f_hist[it] = f;
-        cudaEventRecord(P.ev[4], st);
-        TAD_CUDA_TRY(cudaEventSynchronize(P.ev[4]));
-        float ms;
-        cudaEventElapsedTime(&ms, P.ev[0], P.ev[1]); P.ms_stage[0] += ms;
-        cudaEventElapsedTime(&ms, P.ev[1], P.ev[2]); P.ms_stage[1] += ms;
-        cudaEventElapsedTime(&ms, P.ev[2], P.ev[3]); P.ms_stage[2] += ms;
-        cudaEventElapsedTime(&ms, P.ev[3], P.ev[4]); P.ms_stage[3] += ms;
+        cudaEventRecord(ev(it, 4), st);
         P.ls_trials_total += trials;
         f = fn;
         if (stop_decrement > 0.0 && P.hs->decrement < stop_decrement) { ++it; break; }
@@ -1200,7 +1274,17 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
     }
     if (f_hist) f_hist[it] = f;
     if (iters_done) *iters_done = it;
-    return finish(TAD_OK);
+    const tad_status rs = finish(TAD_OK);   // synchronises the stream
+    // stage times, from the events the iterations recorded (the last slot is
+    // shared by iterations beyond STAGE_ITERS - 1, which are not counted)
+    for (int i = 0; i < std::min(it, Problem::STAGE_ITERS - 1); ++i)
+        for (int k = 0; k < 4; ++k)
+        {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, ev(i, k), ev(i, k + 1)) == cudaSuccess) P.ms_stage[k] += ms;
+        }
+    cudaGetLastError();
+    return rs;
 }
 
 } // namespace tadlib
