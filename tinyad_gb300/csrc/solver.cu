@@ -347,6 +347,22 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_spmv_vec(int64_t nh, const 
 
 template <int d> struct SpmvGroup { static constexpr int value = d == 3 ? 16 : 8; };
 
+/* The PCG SpMV for d x d blocks: thread per block row for d <= 2 (rows of
+   ~7 2x2 blocks on triangle meshes: 41.1 us; the 4- and 8-lane vector form
+   45.5 / 76.3 us on the 1.64M-face disk), 8 lanes per row for d = 3 (rows
+   of ~15 3x3 blocks on tet meshes: 27.1 instead of 37.4 us on 663,552
+   tets). */
+template <int d, typename T>
+inline void launch_pcg_spmv(cudaStream_t s, int64_t nh, const int32_t* bptr, const int32_t* bcol, const T* H, const T* z,
+                            T* p, T* Ap, double* partials, unsigned* counter, DevScalars* ds)
+{
+    if constexpr (d == 3)
+        k_pcg_spmv_vec<d, T, 8><<<PCG_BLOCKS, RED_THREADS, 0, s>>>(nh, bptr, bcol, H, z, p, Ap, partials, counter, ds);
+    else
+        k_pcg_spmv_fused<d, T, SpmvGroup<d>::value><<<PCG_BLOCKS, RED_THREADS, 0, s>>>(nh, bptr, bcol, H, z, p, Ap, partials,
+                                                                                  counter, ds);
+}
+
 template <int d, typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_pcg_update(int64_t nh, T* x, T* r, T* z, const T* __restrict__ p, const T* __restrict__ Ap,
                                                             const T* __restrict__ dinv, double* partials, unsigned* counter, DevScalars* ds)
@@ -616,8 +632,7 @@ static tad_status pcg_core_amg(Problem& P, const double* b, T* xs, double rel_to
     TAD_CUDA_TRY(cudaGetLastError());
     constexpr int CHUNK = 4;
     auto launch_iteration = [&]() {
-        k_pcg_spmv_fused<d, T, SpmvGroup<d>::value><<<PCG_BLOCKS, RED_THREADS, 0, s>>>(nh, P.bptr, P.bcol, H, z, p, Ap,
-                                                                                  P.partials, P.counters + 1, P.ds);
+        launch_pcg_spmv<d, T>(s, nh, P.bptr, P.bcol, H, z, p, Ap, P.partials, P.counters + 1, P.ds);
         k_pcg_update_nopc<T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, xs, r, p, Ap, P.partials, P.counters + 2, P.ds);
         amg_vcycle(P, prec, r, z);
         k_pcg_rz<T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, r, z, P.partials, P.counters + 9, P.ds, 0);
@@ -709,8 +724,7 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
     constexpr double AMG_SWITCH_ITERS = 64.0;
     double rr_first = 0.0;
     auto launch_iteration = [&]() {
-        k_pcg_spmv_fused<d, T, SpmvGroup<d>::value><<<PCG_BLOCKS, RED_THREADS, 0, s>>>(nh, P.bptr, P.bcol, H, z, p, Ap,
-                                                                                  P.partials, P.counters + 1, P.ds);
+        launch_pcg_spmv<d, T>(s, nh, P.bptr, P.bcol, H, z, p, Ap, P.partials, P.counters + 1, P.ds);
         k_pcg_update<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, xs, r, z, p, Ap, dinv, P.partials, P.counters + 2, P.ds);
     };
     int replays = 0;
@@ -1383,9 +1397,8 @@ TAD_API tad_status tad_profile_kernels(tad_problem* P, const double* x_d, int re
         k_pcg_init<D, float><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.rhs, Q.dx32, Q.r32, Q.z32, Q.p32, Q.Ap32,    \
                                                                  Q.dinv32, Q.diag, (const float*)Q.H, 0.0,         \
                                                                  Q.partials, Q.counters, Q.ds, 1e-30, 1 << 30);    \
-        ms5[2] = timed([&] { k_pcg_spmv_fused<D, float, SpmvGroup<D>::value><<<PCG_BLOCKS, RED_THREADS, 0, st>>>(   \
-                               nh, Q.bptr, Q.bcol, (const float*)Q.H, Q.z32, Q.p32, Q.Ap32, Q.partials,              \
-                               Q.counters + 1, Q.ds); });                                                             \
+        ms5[2] = timed([&] { launch_pcg_spmv<D, float>(st, nh, Q.bptr, Q.bcol, (const float*)Q.H, Q.z32, Q.p32,     \
+                                                       Q.Ap32, Q.partials, Q.counters + 1, Q.ds); });                 \
         ms5[3] = timed([&] { k_pcg_update<D, float><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.dx32, Q.r32, Q.z32,  \
                                Q.p32, Q.Ap32, Q.dinv32, Q.partials, Q.counters + 2, Q.ds); });                       \
     }                                                                                                               \
@@ -1394,9 +1407,8 @@ TAD_API tad_status tad_profile_kernels(tad_problem* P, const double* x_d, int re
         k_pcg_init<D, double><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.rhs, Q.dx, Q.r, Q.z, Q.p, Q.Ap, Q.dinv,     \
                                                                   Q.diag, (const double*)Q.H, 0.0,                  \
                                                                   Q.partials, Q.counters, Q.ds, 1e-30, 1 << 30);    \
-        ms5[2] = timed([&] { k_pcg_spmv_fused<D, double, SpmvGroup<D>::value><<<PCG_BLOCKS, RED_THREADS, 0, st>>>(  \
-                               nh, Q.bptr, Q.bcol, (const double*)Q.H, Q.z, Q.p, Q.Ap, Q.partials,                   \
-                               Q.counters + 1, Q.ds); });                                                             \
+        ms5[2] = timed([&] { launch_pcg_spmv<D, double>(st, nh, Q.bptr, Q.bcol, (const double*)Q.H, Q.z, Q.p, Q.Ap, \
+                                                        Q.partials, Q.counters + 1, Q.ds); });                        \
         ms5[3] = timed([&] { k_pcg_update<D, double><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.dx, Q.r, Q.z,       \
                                Q.p, Q.Ap, Q.dinv, Q.partials, Q.counters + 2, Q.ds); });                             \
     }
