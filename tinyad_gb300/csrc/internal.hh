@@ -92,6 +92,7 @@ struct DevScalars
     double ls_s;         // accepted step
     double decrement;    // -0.5 d.g
     double gg;           // g.g
+    int32_t spec_ok;     // Newton: the PCG is done and x is the state the carried derivatives belong to
 };
 
 /* one level of the AMG hierarchy (amg.cu); level 0 borrows the problem's
@@ -175,6 +176,8 @@ struct Problem
     int streak = 0;                  // consecutive calls that continued from the previous call's x
     int32_t* diff_flag = nullptr;    // device: x differs from last_x
     int32_t* diff_flag_h = nullptr;  // pinned mirror
+    cudaStream_t stream2 = nullptr;  // side stream: host copies of x and the continuation test beside the compute
+    cudaEvent_t ev_in = nullptr, ev_xt = nullptr, ev_out = nullptr;
     bool defer_fp32 = false;     // Newton asks a loose mixed solve to leave its solution in dx32 ...
     bool solution_in_dx32 = false;   // ... and the solve says it did (P.dx not written)
     bool pcg_async = false;      // Newton: return PCG_PENDING after the first iteration, without a host check
@@ -263,8 +266,10 @@ tad_status pcg_solve(Problem& P, const double* b, double* xsol, double w_identit
    t_start > 0 resumes the trial sequence there with ds->dg already set */
 tad_status line_search_device(Problem& P, double* x, const double* d, double f, double s_max,
                               bool* found, double* f_out, int* trials, bool f_on_device = false, int t_start = 0);
+/* x_in_h / x_out_h (host API): x is copied in from and out to these host
+   buffers by the solve itself, overlapped with the compute where it can */
 tad_status newton_solve(Problem& P, double* x_d, int n_iters, double eps, double stop_decrement,
-                        double* f_hist, int* iters_done);
+                        double* f_hist, int* iters_done, const double* x_in_h = nullptr, double* x_out_h = nullptr);
 
 } // namespace tadlib
 

@@ -391,6 +391,8 @@ TAD_API tad_status tad_problem_create(int var_dim, int64_t n_handles, const tad_
     P->precision = P->settings.precision;
     TAD_CUDA_TRY(cudaGetDevice(&P->device));
     TAD_CUDA_TRY(cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking));
+    TAD_CUDA_TRY(cudaStreamCreateWithFlags(&P->stream2, cudaStreamNonBlocking));
+    for (cudaEvent_t* e : {&P->ev_in, &P->ev_xt, &P->ev_out}) TAD_CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     TAD_CUDA_TRY(cudaMalloc(&P->ds, sizeof(DevScalars)));
     TAD_CUDA_TRY(cudaMemset(P->ds, 0, sizeof(DevScalars)));
     TAD_CUDA_TRY(cudaMallocHost(&P->hs, sizeof(DevScalars)));
@@ -431,6 +433,8 @@ TAD_API tad_status tad_problem_destroy(tad_problem* P)
     amg_free(*P);
     for (auto& e : P->ev) if (e) cudaEventDestroy(e);
     for (auto& e : P->stage_ev) if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : {P->ev_in, P->ev_xt, P->ev_out}) if (e) cudaEventDestroy(e);
+    if (P->stream2) { cudaStreamSynchronize(P->stream2); cudaStreamDestroy(P->stream2); }
     if (P->stream) cudaStreamDestroy(P->stream);
     delete P;
     return TAD_OK;

@@ -513,6 +513,12 @@ __global__ void k_ls_select(int n, const double* __restrict__ steps, double c, D
     }
 }
 
+/* spec_ok = the PCG is done and (diff == NULL or x did not change) */
+__global__ void k_spec_guard(DevScalars* ds, const int32_t* diff)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) ds->spec_ok = (ds->done != 0 && (!diff || *diff == 0)) ? 1 : 0;
+}
+
 /* *flag = 1 if a and b differ in any bit */
 __global__ void k_differs(int64_t n, const double* __restrict__ a, const double* __restrict__ b, int32_t* flag)
 {
@@ -1060,8 +1066,10 @@ tad_status line_search_device(Problem& P, double* x, const double* d, double f, 
    host round trip; the caller adopts x_t (its derivatives are then already
    assembled) or continues the line search at trial 2. */
 static tad_status speculative_first_trial(Problem& P, const double* x, double* d, double* xt, double eps, bool d_in_fp32,
-                                         const int32_t* guard = nullptr)
+                                         const int32_t* guard = nullptr, double* out_h = nullptr)
 {
+    // out_h: xt is copied to this host buffer on the side stream as soon as it
+    // is formed, beside the element kernels (ordered after any earlier copy)
     // guard (the PCG's done flag): every kernel here returns at once while it
     // is 0, so the block can be enqueued behind an unchecked PCG iteration
     cudaStream_t s = P.stream;
@@ -1076,6 +1084,13 @@ static tad_status speculative_first_trial(Problem& P, const double* x, double* d
         k_add<<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_vars, x, d, xt, guard);
         P.n_launches += 2;
     }
+    if (out_h)
+    {
+        cudaEventRecord(P.ev_xt, s);   // xt is final from here on
+        cudaStreamWaitEvent(P.stream2, P.ev_xt, 0);
+        cudaMemcpyAsync(out_h, xt, P.n_vars * sizeof(double), cudaMemcpyDeviceToHost, P.stream2);
+        cudaEventRecord(P.ev_out, P.stream2);
+    }
     P.launch_guard = guard;
     tad_status st = eval_elements(P, TAD_MODE_HESSIAN_PROJ, xt, eps, P.precision);
     if (st == TAD_OK) st = assemble(P, true, true, P.precision, P.ds->f_trial, true);
@@ -1089,7 +1104,8 @@ static tad_status speculative_first_trial(Problem& P, const double* x, double* d
     return TAD_OK;
 }
 
-tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double stop_decrement, double* f_hist, int* iters_done)
+tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double stop_decrement, double* f_hist, int* iters_done,
+                        const double* x_in_h, double* x_out_h)
 {
     tad_status s = ensure_finalized(P);
     if (s != TAD_OK) return s;
@@ -1110,47 +1126,81 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
     // (speculative_first_trial).  A rejection falls back to the energy-only
     // line search from trial 2, with the same trial sequence and Armijo test,
     // and turns the speculation off until a full step is accepted again.  The
-    // last iteration of a call does not speculate (its derivatives would be
-    // discarded).  The accepted state alternates between x and P.x_trial; x
-    // holds it on return.
+    // accepted state alternates between x and P.x_trial; x holds it on return.
     //
     // Across calls: a call that starts from the exact x the previous call
-    // returned (a device compare, one host round trip) continues that
-    // solve.  Once calls have continued each other twice in a row, the last
-    // iteration of a call speculates too, and the next continuing call starts
-    // from the derivatives it assembled (as an iteration inside one call
-    // would), provided nothing else has evaluated on the problem since and
-    // eps and precision are the same.
+    // returned (a bitwise device compare) continues that solve.  Once calls
+    // have continued each other twice in a row, the last iteration of a call
+    // speculates too, and the next continuing call starts from the
+    // derivatives it assembled (as an iteration inside one call would),
+    // provided nothing else has evaluated on the problem since and eps and
+    // precision are the same.  Such a call is predicted to continue: its
+    // PCG starts on the carried derivatives while x is copied in and
+    // compared on the side stream, and the speculative block waits for the
+    // compare and runs only if x is unchanged; a call whose x changed reruns
+    // its first iteration from an evaluation.  A one-iteration call copies
+    // its result out on the side stream as soon as the trial point x + d is
+    // formed, beside the speculative evaluation.
     const bool forcing = P.settings.forcing == 1;
     const int ls_max = P.settings.ls_max_iters > 0 ? P.settings.ls_max_iters : 64;
     const int64_t n = P.n_vars;
+    cudaStream_t st2 = P.stream2;
     if (!P.x_trial) TAD_CUDA_TRY(cudaMalloc(&P.x_trial, std::max<int64_t>(n, 1) * sizeof(double)));
     if (!P.last_x) TAD_CUDA_TRY(cudaMalloc(&P.last_x, std::max<int64_t>(n, 1) * sizeof(double)));
     if (!P.diff_flag) TAD_CUDA_TRY(cudaMalloc(&P.diff_flag, sizeof(int32_t)));
     if (!P.diff_flag_h) TAD_CUDA_TRY(cudaMallocHost(&P.diff_flag_h, sizeof(int32_t)));
     s = ensure_step_sequence(P, 1.0, ls_max);
     if (s != TAD_OK) return s;
-    bool continues = false;
+    // input copy and continuation test on the side stream (ordered after the
+    // main stream's earlier work on x)
+    const bool predicted = P.last_x_valid && P.spec_valid && P.spec_eps == eps && P.spec_prec == prec;
+    P.spec_valid = false;
+    TAD_CUDA_TRY(cudaEventRecord(P.ev_in, st));
+    TAD_CUDA_TRY(cudaStreamWaitEvent(st2, P.ev_in, 0));
+    if (x_in_h) TAD_CUDA_TRY(cudaMemcpyAsync(x, x_in_h, n * sizeof(double), cudaMemcpyHostToDevice, st2));
+    TAD_CUDA_TRY(cudaMemsetAsync(P.diff_flag, 0, sizeof(int32_t), st2));
     if (P.last_x_valid)
     {
-        TAD_CUDA_TRY(cudaMemsetAsync(P.diff_flag, 0, sizeof(int32_t), st));
-        k_differs<<<RED_BLOCKS, RED_THREADS, 0, st>>>(n, x, P.last_x, P.diff_flag);
+        k_differs<<<RED_BLOCKS, RED_THREADS, 0, st2>>>(n, x, P.last_x, P.diff_flag);
         P.n_launches += 1;
-        TAD_CUDA_TRY(cudaMemcpyAsync(P.diff_flag_h, P.diff_flag, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-        TAD_CUDA_TRY(cudaStreamSynchronize(st));
-        continues = *P.diff_flag_h == 0;
     }
-    P.streak = continues ? P.streak + 1 : 0;
-    const bool reuse = continues && P.spec_valid && P.spec_eps == eps && P.spec_prec == prec;
-    P.spec_valid = false;
+    TAD_CUDA_TRY(cudaEventRecord(P.ev_in, st2));
+    bool continues = false;
+    bool pending_test = predicted;   // the continuation test is read after iteration 0's first sync
+    if (!predicted)
+    {
+        TAD_CUDA_TRY(cudaStreamWaitEvent(st, P.ev_in, 0));   // the evaluation reads x
+        if (P.last_x_valid)
+        {
+            TAD_CUDA_TRY(cudaMemcpyAsync(P.diff_flag_h, P.diff_flag, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+            TAD_CUDA_TRY(cudaStreamSynchronize(st));
+            continues = *P.diff_flag_h == 0;
+        }
+        P.streak = continues ? P.streak + 1 : 0;
+    }
     double* cur = x;
     double* spare = P.x_trial;
-    bool have_derivs = reuse;   // derivatives at cur already assembled (accepted speculative step)
+    bool have_derivs = predicted;   // derivatives at cur already assembled (accepted speculative step)
+    bool early_out = false;         // a copy of spare to x_out_h was issued on the side stream
+    double* early_buf = nullptr;
     auto finish = [&](tad_status rs) {
         if (cur != x) cudaMemcpyAsync(x, cur, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
         const bool ok = rs == TAD_OK;
         if (ok) cudaMemcpyAsync(P.last_x, x, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
+        if (x_out_h)
+        {
+            // the early copy holds the result when it was taken of the accepted
+            // trial point; otherwise (after it, if any) copy x out -- on an
+            // error x still holds the call's input (one-iteration calls)
+            const bool early_good = ok && early_out && early_buf == cur && have_derivs;
+            if (!early_good && (ok || early_out))
+            {
+                if (early_out) cudaStreamWaitEvent(st, P.ev_out, 0);
+                cudaMemcpyAsync(x_out_h, x, n * sizeof(double), cudaMemcpyDeviceToHost, st);
+            }
+        }
         cudaStreamSynchronize(st);
+        cudaStreamSynchronize(st2);
         P.last_x_valid = ok;
         P.spec_valid = ok && have_derivs;
         P.spec_eps = eps;
@@ -1197,7 +1247,10 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
         }
         // the last iteration speculates only once calls have continued each
         // other twice in a row (a caller stepping a solve call by call)
-        const bool spec_now = speculate && (it + 1 < n_iters || P.streak >= 2);
+        const int streak_now = pending_test ? P.streak + 1 : P.streak;   // a predicted call continues
+        const bool spec_now = speculate && (it + 1 < n_iters || streak_now >= 2);
+        // one-iteration calls with a host output copy it out early (beside the speculative evaluation)
+        double* const out_early = (x_out_h && n_iters == 1 && spec_now) ? x_out_h : nullptr;
         // The speculative trial is enqueued right behind the PCG's first
         // iteration, guarded by its done flag, so that one host round trip
         // serves both when the first iteration converges (it does in most
@@ -1213,11 +1266,30 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
         P.pcg_async = false;
         bool trial_done = false;
         bool d_in_fp32 = P.solution_in_dx32;
+        // the speculative block of a predicted call's first iteration waits for
+        // the input copy and the continuation test, and runs only if x is the
+        // state the carried derivatives belong to
+        auto spec_guard = [&](const int32_t* pcg_done) -> const int32_t* {
+            if (!pending_test) return pcg_done;
+            cudaStreamWaitEvent(st, P.ev_in, 0);   // errors surface at the next checked call
+            k_spec_guard<<<1, 32, 0, st>>>(P.ds, P.last_x_valid ? P.diff_flag : nullptr);
+            cudaMemcpyAsync(P.diff_flag_h, P.diff_flag, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+            P.n_launches += 1;
+            return &P.ds->spec_ok;
+        };
+        auto launch_early_out = [&]() {
+            if (!out_early) return;
+            early_out = true;   // speculative_first_trial issued the copy of spare
+            early_buf = spare;
+        };
+        bool spec_issued = false;
         if (s == PCG_PENDING)
         {
             // a loose mixed solve leaves its solution in dx32, FP64 in P.dx
             d_in_fp32 = prec == TAD_PREC_MIXED;
-            s = speculative_first_trial(P, cur, P.dx, spare, eps, d_in_fp32, &P.ds->done);
+            s = speculative_first_trial(P, cur, P.dx, spare, eps, d_in_fp32, spec_guard(&P.ds->done), out_early);
+            launch_early_out();
+            spec_issued = true;
             if (s != TAD_OK) return finish(s);
             if (P.hs->done)
             {
@@ -1244,9 +1316,52 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
         double fn = 0.0;
         int trials = 0;
         have_derivs = false;
+        if (spec_now && !trial_done)
+        {
+            // the PCG was checked on the host (not pending, or resumed)
+            const int32_t* g = nullptr;
+            if (pending_test)
+            {
+                if (!spec_issued) g = spec_guard(&P.ds->done);
+                else
+                {
+                    // the guarded block already ran without effect: the test result is known
+                    g = nullptr;
+                }
+            }
+            if (pending_test && spec_issued && *P.diff_flag_h != 0) { /* handled below */ }
+            else
+            {
+                tad_status s2 = speculative_first_trial(P, cur, P.dx, spare, eps, d_in_fp32, g, out_early);
+                if (s2 != TAD_OK) return finish(s2);
+                launch_early_out();
+            }
+        }
+        if (pending_test)
+        {
+            // the continuation test (copied with the first host round trip; a
+            // first iteration that did not speculate reads it here)
+            if (!spec_now)
+            {
+                TAD_CUDA_TRY(cudaStreamWaitEvent(st, P.ev_in, 0));
+                TAD_CUDA_TRY(cudaMemcpyAsync(P.diff_flag_h, P.diff_flag, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+                TAD_CUDA_TRY(cudaStreamSynchronize(st));
+            }
+            pending_test = false;
+            continues = *P.diff_flag_h == 0;
+            if (!continues)
+            {
+                // x changed: everything above used derivatives of another state
+                P.streak = 0;
+                have_derivs = false;
+                speculate = true;
+                --it;
+                continue;
+            }
+            P.streak = P.streak + 1;
+        }
         if (spec_now)
         {
-            if (!trial_done) s = speculative_first_trial(P, cur, P.dx, spare, eps, d_in_fp32);
             if (s != TAD_OK && s != TAD_ERR_PCG_NOCONV) return finish(s);
             const int choice = P.hs->ls_choice;
             if (choice == -2)
@@ -1443,12 +1558,8 @@ TAD_API tad_status tad_newton_solve(tad_problem* P, double* x_h, int n_iters, do
     TAD_CUDA_TRY(cudaSetDevice(P->device));
     tad_status s = ensure_finalized(*P);
     if (s != TAD_OK) return s;
-    TAD_CUDA_TRY(cudaMemcpyAsync(P->x, x_h, P->n_vars * 8, cudaMemcpyHostToDevice, P->stream));
-    s = newton_solve(*P, P->x, n_iters, eps, stop_decrement, f_hist_h, iters_done);
-    if (s != TAD_OK) return s;
-    TAD_CUDA_TRY(cudaMemcpyAsync(x_h, P->x, P->n_vars * 8, cudaMemcpyDeviceToHost, P->stream));
-    TAD_CUDA_TRY(cudaStreamSynchronize(P->stream));
-    return TAD_OK;
+    // x is copied in and out by the solve, beside its compute where it can
+    return newton_solve(*P, P->x, n_iters, eps, stop_decrement, f_hist_h, iters_done, x_h, x_h);
 }
 
 } // extern "C"
