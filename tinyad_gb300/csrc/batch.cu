@@ -51,6 +51,7 @@ struct BatchScalars
     int32_t* choice;  // [m] accepted trial, -1 none
     double* step;     // [m]
     int32_t* searching;   // meshes without an accepted trial after the last selection
+    int32_t* pcg_active;  // meshes still iterating after the last PCG settle (0: the remaining budget is idle)
 };
 
 constexpr int LS_TRIALS = 16;
@@ -220,6 +221,7 @@ __global__ void k_b_spmv(const Chunk* ch, int n_chunks, const int32_t* mcb, cons
                          const int32_t* bcol, const T* H, const T* p, T* Ap, double* partials, unsigned* counters,
                          BatchScalars S)
 {
+    if (*S.pcg_active == 0) return;   // every mesh is done: the rest of the iteration budget is idle
     for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x)
     {
         const Chunk c = ch[ci];
@@ -257,6 +259,7 @@ __global__ void k_b_update(const Chunk* ch, int n_chunks, const int32_t* mcb, co
                            const T* p, const T* Ap, const T* dinv, double* partials, unsigned* counters, BatchScalars S,
                            int max_iters)
 {
+    if (*S.pcg_active == 0) return;
     for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x)
     {
         const Chunk c = ch[ci];
@@ -300,6 +303,7 @@ __global__ void k_b_update(const Chunk* ch, int n_chunks, const int32_t* mcb, co
 template <int d, typename T>
 __global__ void k_b_pupdate(const Chunk* ch, int n_chunks, const T* z, T* p, BatchScalars S)
 {
+    if (*S.pcg_active == 0) return;
     for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x)
     {
         const Chunk c = ch[ci];
@@ -309,10 +313,14 @@ __global__ void k_b_pupdate(const Chunk* ch, int n_chunks, const T* z, T* p, Bat
     }
 }
 
+/* meshes that finished in this iteration (done == 2) become done (1); the
+   meshes still iterating are counted into pcg_active (zeroed before) */
 __global__ void k_b_settle(int n_meshes, BatchScalars S)
 {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m < n_meshes && S.done[m] == 2) S.done[m] = 1;
+    if (m >= n_meshes) return;
+    if (S.done[m] == 2) S.done[m] = 1;
+    if (S.done[m] == 0) atomicAdd(S.pcg_active, 1);
 }
 
 template <typename T>
@@ -476,6 +484,7 @@ static tad_status record_iteration(Batch& B, int prec, double eps)
     launch_diag_inv(P, prec, s);
     k_b_pcg_init<d, T><<<G, TH, 0, s>>>(B.vch, B.n_vch, B.vmcb, B.vmce, P.rhs, xs, r, z, p, dinv, B.partials,
                                         B.counters, B.S, B.pcg_tol);
+    TAD_CUDA_TRY(cudaMemsetAsync(B.S.pcg_active, 1, sizeof(int32_t), s));   // nonzero: the first iteration runs
     for (int it = 0; it < B.pcg_iters; ++it)
     {
         k_b_spmv<d, T><<<G, TH, 0, s>>>(B.vch, B.n_vch, B.vmcb, B.vmce, P.bptr, P.bcol, H, p, Ap, B.partials,
@@ -483,6 +492,7 @@ static tad_status record_iteration(Batch& B, int prec, double eps)
         k_b_update<d, T><<<G, TH, 0, s>>>(B.vch, B.n_vch, B.vmcb, B.vmce, xs, r, z, p, Ap, dinv, B.partials,
                                           B.counters, B.S, B.pcg_iters);
         k_b_pupdate<d, T><<<G, TH, 0, s>>>(B.vch, B.n_vch, z, p, B.S);
+        TAD_CUDA_TRY(cudaMemsetAsync(B.S.pcg_active, 0, sizeof(int32_t), s));
         k_b_settle<<<(B.n_meshes + 255) / 256, 256, 0, s>>>(B.n_meshes, B.S);
     }
     k_b_to_double<T><<<G, TH, 0, s>>>(n, xs, P.dx);
@@ -654,8 +664,8 @@ static tad_status batch_prepare(tad_batch* B)
         const int nm = B->n_meshes;
         TAD_CUDA_TRY(cudaMalloc(&B->scal, (size_t)nm * (LS_TRIALS + 12) * sizeof(double)));
         TAD_CUDA_TRY(cudaMemset(B->scal, 0, (size_t)nm * (LS_TRIALS + 12) * sizeof(double)));
-        TAD_CUDA_TRY(cudaMalloc(&B->iscal, (size_t)nm * 4 * sizeof(int32_t)));
-        TAD_CUDA_TRY(cudaMemset(B->iscal, 0, (size_t)nm * 4 * sizeof(int32_t)));
+        TAD_CUDA_TRY(cudaMalloc(&B->iscal, (size_t)(nm * 4 + 1) * sizeof(int32_t)));
+        TAD_CUDA_TRY(cudaMemset(B->iscal, 0, (size_t)(nm * 4 + 1) * sizeof(int32_t)));
         double* q = B->scal;
         B->S.f = q; q += nm;
         B->S.ftr = q; q += (size_t)nm * LS_TRIALS;
@@ -672,6 +682,7 @@ static tad_status batch_prepare(tad_batch* B)
         B->S.iters = B->iscal + nm;
         B->S.choice = B->iscal + 2 * nm;
         B->S.searching = B->iscal + 3 * nm;
+        B->S.pcg_active = B->iscal + 4 * nm;
         TAD_CUDA_TRY(cudaMalloc(&B->steps, LS_TRIALS * sizeof(double)));
         std::vector<double> st(LS_TRIALS);
         double sv = 1.0;

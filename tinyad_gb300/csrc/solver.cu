@@ -1318,21 +1318,16 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
         have_derivs = false;
         if (spec_now && !trial_done)
         {
-            // the PCG was checked on the host (not pending, or resumed)
-            const int32_t* g = nullptr;
-            if (pending_test)
+            // The PCG was checked on the host (not pending, or resumed after a
+            // guarded block that ran without effect).  A predicted call whose
+            // test result is already known runs the trial unguarded, unless x
+            // changed (the iteration then reruns, below); one whose test is
+            // still on the side stream guards the trial with it.
+            const bool test_known = pending_test && spec_issued;
+            if (!(test_known && *P.diff_flag_h != 0))
             {
-                if (!spec_issued) g = spec_guard(&P.ds->done);
-                else
-                {
-                    // the guarded block already ran without effect: the test result is known
-                    g = nullptr;
-                }
-            }
-            if (pending_test && spec_issued && *P.diff_flag_h != 0) { /* handled below */ }
-            else
-            {
-                tad_status s2 = speculative_first_trial(P, cur, P.dx, spare, eps, d_in_fp32, g, out_early);
+                const int32_t* g = (pending_test && !test_known) ? spec_guard(&P.ds->done) : nullptr;
+                const tad_status s2 = speculative_first_trial(P, cur, P.dx, spare, eps, d_in_fp32, g, out_early);
                 if (s2 != TAD_OK) return finish(s2);
                 launch_early_out();
             }
