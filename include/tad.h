@@ -371,6 +371,9 @@ TAD_API tad_status tad_batch_newton_solve_d(tad_batch* b, double* x_d, int n_ite
 /* times candidate (block rows per chunk, threads per block) pairs on the
    batch at x_d and keeps the fastest; best3 = [rows, threads, ms] */
 TAD_API tad_status tad_batch_autotune(tad_batch* b, const double* x_d, double proj_eps, double* best3);
+/* sets the chunking directly: chunk_rows block rows per PCG chunk (4x as many
+   elements per element chunk), threads per block; the next solve recaptures */
+TAD_API tad_status tad_batch_set_chunking(tad_batch* b, int chunk_rows, int threads);
 /* the underlying concatenated problem (for evaluations, stats, the stream) */
 TAD_API tad_status tad_batch_problem(tad_batch* b, tad_problem** p);
 TAD_API tad_status tad_batch_destroy(tad_batch* b);

@@ -13,10 +13,15 @@ def _meshes():
     return [meshes.disk_param(g, seed=100 + i) for i, g in enumerate((8, 14, 20, 11, 24))]
 
 
+@pytest.mark.parametrize("chunking", [None, (32, 64)])
 @pytest.mark.parametrize("precision,tol", [(0, 1e-10), (1, 1e-5)])
-def test_batch_matches_single_solves(tad, oracle, precision, tol):
+def test_batch_matches_single_solves(tad, oracle, precision, tol, chunking):
+    """chunking (32 block rows, 64 threads) splits every mesh over several
+    chunks, so the per-mesh reductions combine partials of many blocks"""
     ws = _meshes()
     b = tad.Batch(ws, precision=precision, pcg_rel_tol=tol, pcg_max_iters=400)
+    if chunking:
+        b.set_chunking(*chunking)
     x, fh = b.newton_solve(b.x0(), 40)
     assert fh.shape == (41, len(ws))
     assert np.all(np.isfinite(fh))
@@ -30,6 +35,12 @@ def test_batch_matches_single_solves(tad, oracle, precision, tol):
 
 
 def test_batch_deterministic_and_autotune(tad):
+    """A fixed launch shape reproduces bit for bit.  Another shape groups the
+    per-mesh partial sums differently; CG iterates carry such rounding
+    differences into where each inexact solve stops, so trajectories of
+    different shapes agree only to the solve tolerance, and what is compared
+    across shapes is convergence (test_batch_matches_single_solves with and
+    without chunking)."""
     import torch
     ws = _meshes()
     b = tad.Batch(ws, precision=1, pcg_rel_tol=1e-3, pcg_max_iters=64)
@@ -40,5 +51,13 @@ def test_batch_deterministic_and_autotune(tad):
     best = b.autotune(xd.data_ptr())
     assert best["chunk_rows"] in (256, 512, 1024, 2048, 4096) and best["threads"] in (128, 256)
     assert best["ms_per_iteration"] > 0
-    x3, f3 = b.newton_solve(b.x0(), 5)          # results do not depend on the tuned launch shape
-    assert np.allclose(f3, f1, rtol=1e-6, atol=0)
+    x3, f3 = b.newton_solve(b.x0(), 5)
+    x4, f4 = b.newton_solve(b.x0(), 5)
+    assert np.array_equal(x3, x4) and np.array_equal(f3, f4)
+    b.set_chunking(32, 64)
+    x5, f5 = b.newton_solve(b.x0(), 5)
+    x6, f6 = b.newton_solve(b.x0(), 5)
+    assert np.array_equal(x5, x6) and np.array_equal(f5, f6)
+    assert np.all(f5[-1] < f5[0])
+    with pytest.raises(tad.TinyADError):
+        b.set_chunking(16, 64)

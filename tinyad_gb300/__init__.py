@@ -71,7 +71,7 @@ EXPORTS = [
     "tad_get_stream", "tad_measure_fma_peak", "tad_profile_kernels",
     "tad_launch_count", "tad_adjoint_rest_gradient", "tad_eval_symmetric_dirichlet_tri_noalloc",
     "tad_batch_create", "tad_batch_add_elements", "tad_batch_newton_solve", "tad_batch_newton_solve_d",
-    "tad_batch_autotune", "tad_batch_problem", "tad_batch_destroy",
+    "tad_batch_autotune", "tad_batch_set_chunking", "tad_batch_problem", "tad_batch_destroy",
 ]
 
 
@@ -136,6 +136,7 @@ def load(build_if_missing: bool = True):
     L.tad_batch_newton_solve.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_double, _dp]
     L.tad_batch_newton_solve_d.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_double, _dp]
     L.tad_batch_autotune.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, _dp]
+    L.tad_batch_set_chunking.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
     L.tad_batch_problem.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]
     L.tad_batch_destroy.argtypes = [ctypes.c_void_p]
     L.tad_eval_symmetric_dirichlet_tri_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -618,6 +619,9 @@ class Batch:
         out = np.zeros(3)
         self._check(self.L.tad_batch_autotune(self.h, ctypes.c_void_p(x_ptr), projection_eps, _d(out)))
         return {"chunk_rows": int(out[0]), "threads": int(out[1]), "ms_per_iteration": float(out[2])}
+
+    def set_chunking(self, chunk_rows: int, threads: int):
+        self._check(self.L.tad_batch_set_chunking(self.h, chunk_rows, threads))
 
     @property
     def stream_ptr(self) -> int:

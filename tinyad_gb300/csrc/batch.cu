@@ -1,7 +1,9 @@
 /*
  * Batched Projected Newton: many independent meshes of uneven sizes solved
  * together.  No reference counterpart (TinyAD solves one ScalarFunction at a
- * time); each mesh follows exactly the single-problem algorithm.
+ * time); each mesh follows the single-problem algorithm with the block-Jacobi
+ * preconditioner (settings.preconditioner = 0: no AMG restart) and at most
+ * 16 Armijo trials.
  *
  * Layout: the meshes are concatenated into one block-diagonal problem
  * (handles offset per mesh), so the element kernels, the assembly and the
@@ -11,12 +13,18 @@
  * of block rows (or elements) that each belong to one mesh.  A kernel walks
  * the chunk list with a fixed grid (grid-stride over chunks); the last
  * chunk of a mesh to finish sums that mesh's chunk partials in chunk order,
- * so every per-mesh reduction is deterministic.
+ * so every per-mesh reduction is deterministic.  The PCG kernels use a chunk
+ * list rebuilt on the device from the meshes still iterating (at PCG
+ * iterations 0-4, 6, 8, 12, 16, ...), cut so that the remaining rows spread
+ * over the whole grid, one block per chunk.
  *
  * One Newton iteration (elements -> f -> assembly -> PCG with a fixed number
- * of iterations, each mesh stopping at its own tolerance -> two batches of 8
- * line-search trials -> per-mesh step) has a fixed launch sequence and is
- * captured once as a CUDA graph; the host replays one graph per iteration.
+ * of iterations, each mesh stopping at its own tolerance -> the full step,
+ * then batches of 8 and 7 line-search trials while some mesh has not
+ * accepted one -> per-mesh step) has a fixed launch sequence and is captured
+ * once as a CUDA graph; the host replays one graph per iteration.  Kernels
+ * of the PCG iterations after every mesh has converged, and of the trials
+ * after every mesh has accepted a step, return at once (device counters).
  * A small autotuner times candidate chunk sizes / block sizes on the batch
  * itself and keeps the fastest.
  */
@@ -26,6 +34,7 @@
 #include <vector>
 
 #include "internal.hh"
+#include "bsr_kernels.cuh"
 
 namespace tadlib {
 
@@ -51,7 +60,7 @@ struct BatchScalars
     int32_t* choice;  // [m] accepted trial, -1 none
     double* step;     // [m]
     int32_t* searching;   // meshes without an accepted trial after the last selection
-    int32_t* pcg_active;  // meshes still iterating after the last PCG settle (0: the remaining budget is idle)
+    int32_t* pcg_active;  // [2] meshes still iterating after the last two PCG updates (ping-pong)
 };
 
 constexpr int LS_TRIALS = 16;
@@ -165,44 +174,112 @@ __global__ void k_b_dot(const Chunk* ch, int n_chunks, const int32_t* mcb, const
     }
 }
 
-template <int d, typename T>
-__device__ __forceinline__ void bapply_dinv(const T* dinv, int64_t u, const T (&r)[d], T (&z)[d])
+/* The PCG kernels' chunk list, rebuilt on the device from the meshes still
+   iterating: their rows are cut into chunks of C = max(min_rows,
+   ceil(R / (2 G))) rows for R active rows and a grid of G blocks, so the
+   remaining work spreads over the whole grid however few meshes are left
+   (the last meshes to converge are the largest ones, whose rows would
+   otherwise sit in a few long chunks, one block each).  At most 2 G +
+   n_meshes chunks.  One block; thread t owns a contiguous run of meshes,
+   and the chunk offsets are an exclusive scan of the per-thread counts.
+   active: skip the rebuild when no mesh is iterating (0). */
+constexpr int CHUNK_BUILD_THREADS = 1024;
+
+template <typename V>
+__device__ __forceinline__ V block_exclusive_scan(V v, V* warp_tot, V& total)
 {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    V inc = v;
 #pragma unroll
-    for (int i = 0; i < d; ++i)
+    for (int o = 1; o < 32; o <<= 1)
     {
-        T acc = T(0);
-#pragma unroll
-        for (int j = 0; j < d; ++j) acc += dinv[u * d * d + i * d + j] * r[j];
-        z[i] = acc;
+        const V u = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += u;
     }
+    if (lane == 31) warp_tot[w] = inc;
+    __syncthreads();
+    if (w == 0)
+    {
+        V x = lane < nw ? warp_tot[lane] : V(0);
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const V u = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += u;
+        }
+        warp_tot[lane] = x;   // inclusive over warps
+    }
+    __syncthreads();
+    const V before = w == 0 ? V(0) : warp_tot[w - 1];
+    total = warp_tot[nw - 1];
+    __syncthreads();
+    return before + inc - v;
 }
 
+__global__ void __launch_bounds__(CHUNK_BUILD_THREADS) k_b_pcg_chunks(int n_meshes, const int64_t* __restrict__ row_off,
+                                                                      const int32_t* __restrict__ done, int grid,
+                                                                      int min_rows, const int32_t* active, Chunk* ch,
+                                                                      int32_t* mcb, int32_t* mce, int32_t* n_ch)
+{
+    if (active && *active == 0) return;
+    __shared__ long long tot_ll[32];
+    __shared__ int tot_i[32];
+    const int per = (n_meshes + CHUNK_BUILD_THREADS - 1) / CHUNK_BUILD_THREADS;
+    const int m0 = min(n_meshes, (int)threadIdx.x * per), m1 = min(n_meshes, m0 + per);
+    long long rows = 0;
+    for (int m = m0; m < m1; ++m)
+        if (!done[m]) rows += row_off[m + 1] - row_off[m];
+    long long R;
+    (void)block_exclusive_scan<long long>(rows, tot_ll, R);
+    const long long C = max((long long)min_rows, (R + 2LL * grid - 1) / (2LL * grid));
+    int cnt = 0;
+    for (int m = m0; m < m1; ++m)
+        if (!done[m]) cnt += (int)((row_off[m + 1] - row_off[m] + C - 1) / C);
+    int total;
+    int off = block_exclusive_scan<int>(cnt, tot_i, total);
+    for (int m = m0; m < m1; ++m)
+    {
+        mcb[m] = off;
+        if (!done[m])
+            for (long long b = row_off[m]; b < row_off[m + 1]; b += C)
+                ch[off++] = Chunk{m, (int32_t)b, (int32_t)min((long long)row_off[m + 1], b + C)};
+        mce[m] = off;
+    }
+    if (threadIdx.x == 0) *n_ch = total;
+}
+
+/* per mesh: x = 0, r = b, z = D^-1 r with the diagonal blocks inverted here
+   in the PCG precision (D^-1 stored), p = Ap = 0, beta = 0 (the first fused
+   SpMV then forms p = z, Ap = H z); rz, bb, tol2, iters = 0, done = (b == 0) */
 template <int d, typename T>
 __global__ void k_b_pcg_init(const Chunk* ch, int n_chunks, const int32_t* mcb, const int32_t* mce, const double* b,
-                             T* x, T* r, T* z, T* p, const T* dinv, double* partials, unsigned* counters,
-                             BatchScalars S, double rel_tol)
+                             const int32_t* __restrict__ diag, const T* __restrict__ H, T* x, T* r, T* z, T* p, T* Ap,
+                             T* dinv, double* partials, unsigned* counters, BatchScalars S, double rel_tol)
 {
     for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x)
     {
         const Chunk c = ch[ci];
-        double v[2] = {0.0, 0.0};
+        T acc_rz = T(0), acc_bb = T(0);
         for (int64_t u = c.begin + threadIdx.x; u < c.end; u += blockDim.x)
         {
-            T rv[d], zv[d];
+            T rv[d], I[d * d];
+            diag_block_inverse<d, T>(diag, H, 0.0, u, I);
 #pragma unroll
-            for (int i = 0; i < d; ++i) { rv[i] = (T)b[u * d + i]; x[u * d + i] = T(0); r[u * d + i] = rv[i]; }
-            bapply_dinv<d, T>(dinv, u, rv, zv);
+            for (int i = 0; i < d; ++i) { rv[i] = from_double<T>(b[u * d + i]); x[u * d + i] = T(0); r[u * d + i] = rv[i]; }
 #pragma unroll
             for (int i = 0; i < d; ++i)
             {
-                z[u * d + i] = zv[i];
-                p[u * d + i] = zv[i];
-                v[0] += (double)rv[i] * (double)zv[i];
-                v[1] += b[u * d + i] * b[u * d + i];
+                T acc = T(0);
+#pragma unroll
+                for (int j = 0; j < d; ++j) { acc += I[i * d + j] * rv[j]; dinv[u * d * d + i * d + j] = I[i * d + j]; }
+                z[u * d + i] = acc;
+                p[u * d + i] = T(0);
+                Ap[u * d + i] = T(0);
+                acc_rz += rv[i] * acc;
+                acc_bb += rv[i] * rv[i];
             }
         }
-        double tot[2];
+        double v[2] = {as_double(acc_rz), as_double(acc_bb)}, tot[2];
         if (seg_finish<2>(ci, c.mesh, v, partials, n_chunks, counters, mcb, mce, tot) && threadIdx.x == 0)
         {
             const int m = c.mesh;
@@ -211,41 +288,45 @@ __global__ void k_b_pcg_init(const Chunk* ch, int n_chunks, const int32_t* mcb, 
             S.rr[m] = tot[1];
             S.tol2[m] = rel_tol * rel_tol * tot[1];
             S.iters[m] = 0;
+            S.beta[m] = 0.0;
             S.done[m] = tot[1] == 0.0 ? 1 : 0;
         }
     }
 }
 
+/* per mesh still iterating: Ap = H z + beta Ap, p = z + beta p (H p_new =
+   H z + beta H p_old, as in the single-problem PCG), alpha = rz / p.Ap.
+   active: meshes still iterating after the previous update (0: every block
+   returns at once -- the rest of the iteration budget is idle) */
 template <int d, typename T>
-__global__ void k_b_spmv(const Chunk* ch, int n_chunks, const int32_t* mcb, const int32_t* mce, const int32_t* bptr,
-                         const int32_t* bcol, const T* H, const T* p, T* Ap, double* partials, unsigned* counters,
-                         BatchScalars S)
+__global__ void k_b_spmv(const Chunk* ch, const int32_t* n_ch, int stride, const int32_t* mcb, const int32_t* mce,
+                         const int32_t* bptr, const int32_t* bcol, const T* H, const T* z, T* p, T* Ap, double* partials,
+                         unsigned* counters, BatchScalars S, const int32_t* active)
 {
-    if (*S.pcg_active == 0) return;   // every mesh is done: the rest of the iteration budget is idle
+    if (*active == 0) return;
+    const int n_chunks = *n_ch;
     for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x)
     {
         const Chunk c = ch[ci];
         if (S.done[c.mesh]) continue;
-        double v[1] = {0.0};
+        const T beta = from_double<T>(S.beta[c.mesh]);
+        T part = T(0);
         for (int64_t u = c.begin + threadIdx.x; u < c.end; u += blockDim.x)
         {
             T y[d];
+            bsr_row_product<d, T>(bptr, bcol, H, z, u, y);
 #pragma unroll
-            for (int i = 0; i < d; ++i) y[i] = T(0);
-            for (int32_t bb = bptr[u]; bb < bptr[u + 1]; ++bb)
+            for (int i = 0; i < d; ++i)
             {
-                const int64_t w = bcol[bb];
-                const T* B = H + (int64_t)bb * d * d;
-#pragma unroll
-                for (int i = 0; i < d; ++i)
-#pragma unroll
-                    for (int j = 0; j < d; ++j) y[i] += B[i * d + j] * p[w * d + j];
+                const T apn = y[i] + beta * Ap[u * d + i];
+                const T pn = z[u * d + i] + beta * p[u * d + i];
+                Ap[u * d + i] = apn;
+                p[u * d + i] = pn;
+                part += pn * apn;
             }
-#pragma unroll
-            for (int i = 0; i < d; ++i) { Ap[u * d + i] = y[i]; v[0] += (double)(p[u * d + i] * y[i]); }
         }
-        double tot[1];
-        if (seg_finish<1>(ci, c.mesh, v, partials, n_chunks, counters, mcb, mce, tot) && threadIdx.x == 0)
+        double v[1] = {as_double(part)}, tot[1];
+        if (seg_finish<1>(ci, c.mesh, v, partials, stride, counters, mcb, mce, tot) && threadIdx.x == 0)
         {
             const int m = c.mesh;
             if (!(tot[0] > 0.0) || !isfinite(tot[0])) { S.done[m] = 1; S.alpha[m] = 0.0; }
@@ -254,18 +335,23 @@ __global__ void k_b_spmv(const Chunk* ch, int n_chunks, const int32_t* mcb, cons
     }
 }
 
+/* x += alpha p, r -= alpha Ap, z = D^-1 r; rz, rr and beta per mesh.  A mesh
+   that converged, reached max_iters or went non-finite is done; the others
+   are counted into active_out (zeroed before), which the next SpMV and
+   update read as their active_in */
 template <int d, typename T>
-__global__ void k_b_update(const Chunk* ch, int n_chunks, const int32_t* mcb, const int32_t* mce, T* x, T* r, T* z,
-                           const T* p, const T* Ap, const T* dinv, double* partials, unsigned* counters, BatchScalars S,
-                           int max_iters)
+__global__ void k_b_update(const Chunk* ch, const int32_t* n_ch, int stride, const int32_t* mcb, const int32_t* mce,
+                           T* x, T* r, T* z, const T* p, const T* Ap, const T* dinv, double* partials, unsigned* counters,
+                           BatchScalars S, int max_iters, const int32_t* active_in, int32_t* active_out)
 {
-    if (*S.pcg_active == 0) return;
+    if (*active_in == 0) return;
+    const int n_chunks = *n_ch;
     for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x)
     {
         const Chunk c = ch[ci];
         if (S.done[c.mesh]) continue;
-        const T alpha = (T)S.alpha[c.mesh];
-        double v[2] = {0.0, 0.0};
+        const T alpha = from_double<T>(S.alpha[c.mesh]);
+        T acc_rz = T(0), acc_rr = T(0);
         for (int64_t u = c.begin + threadIdx.x; u < c.end; u += blockDim.x)
         {
             T rv[d], zv[d];
@@ -276,58 +362,34 @@ __global__ void k_b_update(const Chunk* ch, int n_chunks, const int32_t* mcb, co
                 rv[i] = r[u * d + i] - alpha * Ap[u * d + i];
                 r[u * d + i] = rv[i];
             }
-            bapply_dinv<d, T>(dinv, u, rv, zv);
+            apply_dinv<d, T>(dinv, u, rv, zv);
 #pragma unroll
             for (int i = 0; i < d; ++i)
             {
                 z[u * d + i] = zv[i];
-                v[0] += (double)(rv[i] * zv[i]);
-                v[1] += (double)(rv[i] * rv[i]);
+                acc_rz += rv[i] * zv[i];
+                acc_rr += rv[i] * rv[i];
             }
         }
-        double tot[2];
-        if (seg_finish<2>(ci, c.mesh, v, partials, n_chunks, counters, mcb, mce, tot) && threadIdx.x == 0)
+        double v[2] = {as_double(acc_rz), as_double(acc_rr)}, tot[2];
+        if (seg_finish<2>(ci, c.mesh, v, partials, stride, counters, mcb, mce, tot) && threadIdx.x == 0)
         {
             const int m = c.mesh;
             S.beta[m] = tot[0] / S.rz[m];
             S.rz[m] = tot[0];
             S.rr[m] = tot[1];
             S.iters[m] += 1;
-            if (tot[1] <= S.tol2[m] || S.iters[m] >= max_iters || !isfinite(tot[1])) S.done[m] = 2;
+            if (tot[1] <= S.tol2[m] || S.iters[m] >= max_iters || !isfinite(tot[1])) S.done[m] = 1;
+            else atomicAdd(active_out, 1);
         }
     }
-}
-
-/* p = z + beta p for meshes still iterating (done == 0); a mesh that finished
-   in this iteration's update (done == 2) keeps p, then is marked 1 */
-template <int d, typename T>
-__global__ void k_b_pupdate(const Chunk* ch, int n_chunks, const T* z, T* p, BatchScalars S)
-{
-    if (*S.pcg_active == 0) return;
-    for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x)
-    {
-        const Chunk c = ch[ci];
-        if (S.done[c.mesh]) continue;
-        const T beta = (T)S.beta[c.mesh];
-        for (int64_t i = (int64_t)c.begin * d + threadIdx.x; i < (int64_t)c.end * d; i += blockDim.x) p[i] = z[i] + beta * p[i];
-    }
-}
-
-/* meshes that finished in this iteration (done == 2) become done (1); the
-   meshes still iterating are counted into pcg_active (zeroed before) */
-__global__ void k_b_settle(int n_meshes, BatchScalars S)
-{
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= n_meshes) return;
-    if (S.done[m] == 2) S.done[m] = 1;
-    if (S.done[m] == 0) atomicAdd(S.pcg_active, 1);
 }
 
 template <typename T>
 __global__ void k_b_to_double(int64_t n, const T* a, double* out)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        out[i] = (double)a[i];
+        out[i] = as_double(a[i]);
 }
 
 __global__ void k_b_neg(int64_t n, const double* a, double* out)
@@ -382,6 +444,12 @@ struct Batch
     Chunk *vch = nullptr, *ech = nullptr;
     int n_vch = 0, n_ech = 0;
     int32_t *vmcb = nullptr, *vmce = nullptr, *emcb = nullptr, *emce = nullptr;
+    // PCG chunk list built on the device (k_b_pcg_chunks): capacity, list,
+    // per-mesh ranges, count; per-mesh row offsets
+    int pch_cap = 0;
+    Chunk* pch = nullptr;
+    int32_t *pmcb = nullptr, *pmce = nullptr, *n_pch = nullptr;
+    int64_t* row_off = nullptr;
     double* partials = nullptr;
     unsigned* counters = nullptr;   // [LS_TRIALS * 4096]
     double* scal = nullptr;
@@ -454,12 +522,31 @@ static tad_status batch_setup_chunks(Batch& B)
     TAD_CUDA_TRY(upload(&B.vmce, vmce));
     TAD_CUDA_TRY(upload(&B.emcb, emcb));
     TAD_CUDA_TRY(upload(&B.emce, emce));
+    B.pch_cap = 2 * B.grid + B.n_meshes;
+    if (B.pch) { cudaFree(B.pch); B.pch = nullptr; }
+    TAD_CUDA_TRY(cudaMalloc(&B.pch, (size_t)B.pch_cap * sizeof(Chunk)));
+    if (!B.pmcb)
+    {
+        TAD_CUDA_TRY(cudaMalloc(&B.pmcb, (size_t)B.n_meshes * sizeof(int32_t)));
+        TAD_CUDA_TRY(cudaMalloc(&B.pmce, (size_t)B.n_meshes * sizeof(int32_t)));
+        TAD_CUDA_TRY(cudaMalloc(&B.n_pch, sizeof(int32_t)));
+        TAD_CUDA_TRY(upload(&B.row_off, B.vert_off));
+    }
     if (B.partials) cudaFree(B.partials);
-    TAD_CUDA_TRY(cudaMalloc(&B.partials, (size_t)std::max(B.n_vch, B.n_ech) * LS_TRIALS * 2 * sizeof(double)));
+    const size_t n_part = std::max<size_t>((size_t)std::max(B.n_vch, B.n_ech) * LS_TRIALS, (size_t)B.pch_cap) * 2;
+    TAD_CUDA_TRY(cudaMalloc(&B.partials, n_part * sizeof(double)));
     return TAD_OK;
 }
 
-void launch_diag_inv(Problem& P, int prec, cudaStream_t s);
+/* PCG iterations before which the chunk list is rebuilt (0, 1, 2, 3, 4, 6,
+   8, 12, 16, 24, 32, 48, ...): between rebuilds the list is a superset of
+   the meshes still iterating, whose finished chunks are skipped */
+static bool rebuild_chunks_before(int it)
+{
+    if (it <= 4) return true;
+    const int q = it % 3 == 0 ? it / 3 : it;
+    return (q & (q - 1)) == 0;
+}
 
 /* record one batched Newton iteration on the problem's stream (captured) */
 template <int d, typename T>
@@ -480,20 +567,26 @@ static tad_status record_iteration(Batch& B, int prec, double eps)
     launch_assemble_grad(P, prec, prec == TAD_PREC_MIXED);
     launch_assemble_hess(P, prec);
     k_b_neg<<<G, TH, 0, s>>>(n, P.g, P.rhs);
-    // 2. PCG, per-mesh tolerance
-    launch_diag_inv(P, prec, s);
-    k_b_pcg_init<d, T><<<G, TH, 0, s>>>(B.vch, B.n_vch, B.vmcb, B.vmce, P.rhs, xs, r, z, p, dinv, B.partials,
-                                        B.counters, B.S, B.pcg_tol);
-    TAD_CUDA_TRY(cudaMemsetAsync(B.S.pcg_active, 1, sizeof(int32_t), s));   // nonzero: the first iteration runs
+    // 2. PCG, per-mesh tolerance.  Iteration it reads the active count the
+    // previous update left in pcg_active[it & 1] and counts into the other
+    // slot; the first count is set nonzero so the first iteration runs.
+    k_b_pcg_init<d, T><<<G, TH, 0, s>>>(B.vch, B.n_vch, B.vmcb, B.vmce, P.rhs, P.diag, H, xs, r, z, p, Ap, dinv,
+                                        B.partials, B.counters, B.S, B.pcg_tol);
+    TAD_CUDA_TRY(cudaMemsetAsync(B.S.pcg_active, 1, sizeof(int32_t), s));
     for (int it = 0; it < B.pcg_iters; ++it)
     {
-        k_b_spmv<d, T><<<G, TH, 0, s>>>(B.vch, B.n_vch, B.vmcb, B.vmce, P.bptr, P.bcol, H, p, Ap, B.partials,
-                                        B.counters, B.S);
-        k_b_update<d, T><<<G, TH, 0, s>>>(B.vch, B.n_vch, B.vmcb, B.vmce, xs, r, z, p, Ap, dinv, B.partials,
-                                          B.counters, B.S, B.pcg_iters);
-        k_b_pupdate<d, T><<<G, TH, 0, s>>>(B.vch, B.n_vch, z, p, B.S);
-        TAD_CUDA_TRY(cudaMemsetAsync(B.S.pcg_active, 0, sizeof(int32_t), s));
-        k_b_settle<<<(B.n_meshes + 255) / 256, 256, 0, s>>>(B.n_meshes, B.S);
+        const int32_t* in = B.S.pcg_active + (it & 1);
+        int32_t* out = B.S.pcg_active + ((it + 1) & 1);
+        if (rebuild_chunks_before(it))
+            k_b_pcg_chunks<<<1, CHUNK_BUILD_THREADS, 0, s>>>(B.n_meshes, B.row_off, B.S.done, G, TH, in, B.pch, B.pmcb,
+                                                             B.pmce, B.n_pch);
+        // one block per chunk slot (blocks past the list's length return at
+        // once): the block scheduler balances chunks of uneven length
+        k_b_spmv<d, T><<<B.pch_cap, TH, 0, s>>>(B.pch, B.n_pch, B.pch_cap, B.pmcb, B.pmce, P.bptr, P.bcol, H, z, p,
+                                                Ap, B.partials, B.counters, B.S, in);
+        TAD_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(int32_t), s));
+        k_b_update<d, T><<<B.pch_cap, TH, 0, s>>>(B.pch, B.n_pch, B.pch_cap, B.pmcb, B.pmce, xs, r, z, p, Ap, dinv,
+                                                  B.partials, B.counters, B.S, B.pcg_iters, in, out);
     }
     k_b_to_double<T><<<G, TH, 0, s>>>(n, xs, P.dx);
     // 3. line search: d.g per mesh; the full step alone, then batches of up to
@@ -558,58 +651,6 @@ using namespace tadlib;
 
 struct tad_batch : public tadlib::Batch {};
 
-namespace tadlib {
-// diag inverse with the single-problem kernels (defined in solver.cu)
-template <int d, typename T>
-__global__ void k_diag_inv_b(int64_t nh, const int32_t* __restrict__ diag, const T* __restrict__ H, T* __restrict__ dinv)
-{
-    for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < nh; u += (int64_t)gridDim.x * blockDim.x)
-    {
-        double A[d * d], I[d * d];
-        const int32_t b = diag[u];
-#pragma unroll
-        for (int i = 0; i < d * d; ++i) A[i] = b >= 0 ? (double)H[(int64_t)b * d * d + i] : 0.0;
-        double det;
-        if (d == 1) { det = A[0]; I[0] = 1.0 / A[0]; }
-        else if (d == 2)
-        {
-            det = A[0] * A[3] - A[1] * A[2];
-            const double id = 1.0 / det;
-            I[0] = A[3] * id; I[1] = -A[1] * id; I[2] = -A[2] * id; I[3] = A[0] * id;
-        }
-        else
-        {
-            const double c00 = A[4] * A[8] - A[5] * A[7], c01 = A[5] * A[6] - A[3] * A[8], c02 = A[3] * A[7] - A[4] * A[6];
-            det = A[0] * c00 + A[1] * c01 + A[2] * c02;
-            const double id = 1.0 / det;
-            I[0] = c00 * id; I[3] = c01 * id; I[6] = c02 * id;
-            I[1] = (A[2] * A[7] - A[1] * A[8]) * id; I[4] = (A[0] * A[8] - A[2] * A[6]) * id; I[7] = (A[1] * A[6] - A[0] * A[7]) * id;
-            I[2] = (A[1] * A[5] - A[2] * A[4]) * id; I[5] = (A[2] * A[3] - A[0] * A[5]) * id; I[8] = (A[0] * A[4] - A[1] * A[3]) * id;
-        }
-        const bool ok = det > 0.0 && isfinite(det);
-#pragma unroll
-        for (int i = 0; i < d; ++i)
-#pragma unroll
-            for (int j = 0; j < d; ++j)
-                dinv[u * d * d + i * d + j] = (T)(ok ? I[i * d + j] : (i == j ? (A[i * d + i] > 0.0 ? 1.0 / A[i * d + i] : 1.0) : 0.0));
-    }
-}
-
-void launch_diag_inv(Problem& P, int prec, cudaStream_t s)
-{
-#define TAD_DI(D)                                                                                          \
-    if (prec == TAD_PREC_MIXED) k_diag_inv_b<D, float><<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_handles, P.diag, (const float*)P.H, P.dinv32); \
-    else k_diag_inv_b<D, double><<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_handles, P.diag, (const double*)P.H, P.dinv);
-    switch (P.d)
-    {
-    case 1: TAD_DI(1); break;
-    case 2: TAD_DI(2); break;
-    default: TAD_DI(3); break;
-    }
-#undef TAD_DI
-}
-} // namespace tadlib
-
 extern "C" {
 
 TAD_API tad_status tad_batch_create(int var_dim, int n_meshes, const int64_t* n_handles, const tad_settings* settings,
@@ -664,8 +705,8 @@ static tad_status batch_prepare(tad_batch* B)
         const int nm = B->n_meshes;
         TAD_CUDA_TRY(cudaMalloc(&B->scal, (size_t)nm * (LS_TRIALS + 12) * sizeof(double)));
         TAD_CUDA_TRY(cudaMemset(B->scal, 0, (size_t)nm * (LS_TRIALS + 12) * sizeof(double)));
-        TAD_CUDA_TRY(cudaMalloc(&B->iscal, (size_t)(nm * 4 + 1) * sizeof(int32_t)));
-        TAD_CUDA_TRY(cudaMemset(B->iscal, 0, (size_t)(nm * 4 + 1) * sizeof(int32_t)));
+        TAD_CUDA_TRY(cudaMalloc(&B->iscal, (size_t)(nm * 4 + 2) * sizeof(int32_t)));
+        TAD_CUDA_TRY(cudaMemset(B->iscal, 0, (size_t)(nm * 4 + 2) * sizeof(int32_t)));
         double* q = B->scal;
         B->S.f = q; q += nm;
         B->S.ftr = q; q += (size_t)nm * LS_TRIALS;
@@ -758,8 +799,9 @@ TAD_API tad_status tad_batch_newton_solve(tad_batch* B, double* x_h, int n_iters
 
 /* Autotuner: times one captured batched Newton iteration for each candidate
    (block rows per chunk x threads per block) on the batch's current x and
-   keeps the fastest.  Candidates are measured after one warm replay, with
-   CUDA events on the batch's stream; the state x is restored afterwards.
+   keeps the fastest.  Candidates are measured over three iterations after
+   one warm replay, with CUDA events on the batch's stream; the state x is
+   restored afterwards.
    best3 (optional): [chunk_rows, threads, ms]. */
 TAD_API tad_status tad_batch_autotune(tad_batch* B, const double* x_d, double eps, double* best3)
 {
@@ -770,6 +812,10 @@ TAD_API tad_status tad_batch_autotune(tad_batch* B, const double* x_d, double ep
     Problem& P = *B->P;
     B->pcg_iters = std::max(1, std::min(P.settings.pcg_max_iters, 4096));
     B->pcg_tol = P.settings.pcg_rel_tol;
+    // each candidate is timed over TUNE_ITERS consecutive iterations from x:
+    // the linear solves get harder as the meshes converge, and the first
+    // iteration alone favours the launch shape of the easy solves
+    constexpr int TUNE_ITERS = 3;
     const int rows_c[] = {256, 512, 1024, 2048, 4096};
     const int thr_c[] = {128, 256};
     double best = 1e30;
@@ -789,10 +835,11 @@ TAD_API tad_status tad_batch_autotune(tad_batch* B, const double* x_d, double ep
             TAD_CUDA_TRY(cudaGraphLaunch(B->graph, P.stream));
             TAD_CUDA_TRY(cudaMemcpyAsync(B->x, x_d, P.n_vars * 8, cudaMemcpyDeviceToDevice, P.stream));
             cudaEventRecord(P.ev[5], P.stream);
-            TAD_CUDA_TRY(cudaGraphLaunch(B->graph, P.stream));
+            for (int k = 0; k < TUNE_ITERS; ++k) TAD_CUDA_TRY(cudaGraphLaunch(B->graph, P.stream));
             cudaEventRecord(P.ev[6], P.stream);
             TAD_CUDA_TRY(cudaEventSynchronize(P.ev[6]));
             cudaEventElapsedTime(&ms, P.ev[5], P.ev[6]);
+            ms /= TUNE_ITERS;
             if (ms < best) { best = ms; br = rows; bt = thr; }
         }
     B->chunk_rows = br;
@@ -804,6 +851,19 @@ TAD_API tad_status tad_batch_autotune(tad_batch* B, const double* x_d, double ep
     TAD_CUDA_TRY(cudaMemcpyAsync(B->x, x_d, P.n_vars * 8, cudaMemcpyDeviceToDevice, P.stream));
     TAD_CUDA_TRY(cudaStreamSynchronize(P.stream));
     if (best3) { best3[0] = br; best3[1] = bt; best3[2] = best; }
+    return TAD_OK;
+}
+
+TAD_API tad_status tad_batch_set_chunking(tad_batch* B, int chunk_rows, int threads)
+{
+    if (!B) return batch_fail(TAD_ERR_ARG, "NULL argument");
+    if (chunk_rows < 32 || chunk_rows > (1 << 20) || threads < 32 || threads > 1024 || threads % 32 != 0)
+        return batch_fail(TAD_ERR_ARG, "chunk_rows in [32, 2^20], threads a multiple of 32 in [32, 1024]");
+    TAD_CUDA_TRY(cudaSetDevice(B->P->device));
+    B->chunk_rows = chunk_rows;
+    B->threads = threads;
+    if (B->graph) { TAD_CUDA_TRY(cudaStreamSynchronize(B->P->stream)); cudaGraphExecDestroy(B->graph); B->graph = nullptr; }
+    if (B->counters) return batch_setup_chunks(*B);   // prepared: rebuild the chunk lists now
     return TAD_OK;
 }
 
@@ -820,7 +880,7 @@ TAD_API tad_status tad_batch_destroy(tad_batch* B)
     if (B->P) cudaStreamSynchronize(B->P->stream);
     if (B->graph) cudaGraphExecDestroy(B->graph);
     void* bufs[] = {B->vch, B->ech, B->vmcb, B->vmce, B->emcb, B->emce, B->partials, B->counters, B->scal, B->iscal,
-                    B->steps, B->x};
+                    B->steps, B->x, B->pch, B->pmcb, B->pmce, B->n_pch, B->row_off};
     for (void* b : bufs) if (b) cudaFree(b);
     if (B->fh) cudaFreeHost(B->fh);
     tad_problem_destroy(B->P);

@@ -1,14 +1,108 @@
 /*
- * bsr_kernels.cuh -- block-Jacobi pieces shared by the PCG (solver.cu) and
- * the AMG hierarchy (amg.cu): inversion of the d x d diagonal blocks and
- * their application to a block row.
+ * bsr_kernels.cuh -- pieces shared by the PCG (solver.cu), the batched PCG
+ * (batch.cu) and the AMG hierarchy (amg.cu): precision conversions, BSR
+ * block and row loads, inversion of the d x d diagonal blocks and their
+ * application to a block row.
  */
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "grid_reduce.cuh"
+#include "../../include/tad/Scalar.cuh"
 
 namespace tadlib {
+
+/* conversions between the FP64 vectors and the PCG precision: on this GPU
+   float <-> double conversion instructions run on the FP64 pipe, so the FP32
+   side uses bit constructions (exact float -> double; double -> nearest
+   float through the double-float split) */
+template <typename T> __device__ __forceinline__ T from_double(double v);
+template <> __device__ __forceinline__ double from_double<double>(double v) { return v; }
+template <> __device__ __forceinline__ float from_double<float>(double v) { return (float)tad::DoubleFloatValue(v); }
+__device__ __forceinline__ double as_double(double v) { return v; }
+__device__ __forceinline__ double as_double(float v) { return tad::DoubleFloat::float_to_double(v); }
+
+/* the d entries of one block row of a vector (one 8-byte load for 2D FP32) */
+template <int d, typename T>
+__device__ __forceinline__ void load_vec(const T* __restrict__ src, T (&v)[d])
+{
+    if constexpr (d == 2 && sizeof(T) == 4)
+    {
+        const float2 q = *reinterpret_cast<const float2*>(src);
+        v[0] = q.x; v[1] = q.y;
+    }
+    else
+    {
+#pragma unroll
+        for (int j = 0; j < d; ++j) v[j] = src[j];
+    }
+}
+
+/* one d x d block of H into registers (16-byte vector loads where the
+   block size allows) */
+template <int d, typename T>
+__device__ __forceinline__ void load_block(const T* __restrict__ B, T (&v)[d * d])
+{
+    if constexpr (d == 2 && sizeof(T) == 4)
+    {
+        const float4 q = __ldg(reinterpret_cast<const float4*>(B));
+        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    }
+    else if constexpr (d == 2 && sizeof(T) == 8)
+    {
+        const double2 q0 = __ldg(reinterpret_cast<const double2*>(B));
+        const double2 q1 = __ldg(reinterpret_cast<const double2*>(B) + 1);
+        v[0] = q0.x; v[1] = q0.y; v[2] = q1.x; v[3] = q1.y;
+    }
+    else
+    {
+#pragma unroll
+        for (int i = 0; i < d * d; ++i) v[i] = __ldg(B + i);
+    }
+}
+
+/* y = (row u of the BSR matrix) z.  The block loop is unrolled four ways
+   so four column ids, four blocks and four z gathers are in flight at once
+   (the block-at-a-time loop was latency-bound on the bcol -> z dependency). */
+template <int d, typename T>
+__device__ __forceinline__ void bsr_row_product(const int32_t* __restrict__ bptr, const int32_t* __restrict__ bcol,
+                                                const T* __restrict__ H, const T* __restrict__ z, int64_t u, T (&y)[d])
+{
+#pragma unroll
+    for (int i = 0; i < d; ++i) y[i] = T(0);
+    int32_t b = bptr[u];
+    const int32_t b1 = bptr[u + 1];
+    for (; b + 4 <= b1; b += 4)
+    {
+        int64_t v[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) v[k] = __ldg(bcol + b + k);
+        T B[4][d * d], zv[4][d];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+        {
+            load_block<d, T>(H + (int64_t)(b + k) * d * d, B[k]);
+            load_vec<d, T>(z + v[k] * d, zv[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+#pragma unroll
+            for (int i = 0; i < d; ++i)
+#pragma unroll
+                for (int j = 0; j < d; ++j) y[i] += B[k][i * d + j] * zv[k][j];
+    }
+    for (; b < b1; ++b)
+    {
+        const int64_t v = __ldg(bcol + b);
+        T B[d * d];
+        load_block<d, T>(H + (int64_t)b * d * d, B);
+#pragma unroll
+        for (int i = 0; i < d; ++i)
+#pragma unroll
+            for (int j = 0; j < d; ++j) y[i] += B[i * d + j] * z[v * d + j];
+    }
+}
+
 
 /* ---- block-Jacobi preconditioner: invert (H_uu + w I) ------------------- */
 /* inverse of block row u's diagonal block (+ w I) into I; a block that is not

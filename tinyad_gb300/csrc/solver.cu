@@ -41,16 +41,6 @@
 
 namespace tadlib {
 
-/* conversions between the FP64 vectors and the PCG precision: on this GPU
-   float <-> double conversion instructions run on the FP64 pipe, so the FP32
-   side uses bit constructions (exact float -> double; double -> nearest
-   float through the double-float split) */
-template <typename T> __device__ __forceinline__ T from_double(double v);
-template <> __device__ __forceinline__ double from_double<double>(double v) { return v; }
-template <> __device__ __forceinline__ float from_double<float>(double v) { return (float)tad::DoubleFloatValue(v); }
-__device__ __forceinline__ double as_double(double v) { return v; }
-__device__ __forceinline__ double as_double(float v) { return tad::DoubleFloat::float_to_double(v); }
-
 /* x = 0, r = b, z = M^-1 r, p = Ap = 0, beta = 0 (the first fused SpMV then
    forms p = z, Ap = A z); rz = r.z, bb = b.b.  With H given (block Jacobi),
    the inverted diagonal blocks of H + w I are formed here and stored in dinv;
@@ -156,51 +146,10 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_spmv(int64_t nh, const int3
     }
 }
 
-/* one d x d block of H into registers (16-byte vector loads where the
-   block size allows) */
-/* the d entries of one block row of a vector (one 8-byte load for 2D FP32) */
-template <int d, typename T>
-__device__ __forceinline__ void load_vec(const T* __restrict__ src, T (&v)[d])
-{
-    if constexpr (d == 2 && sizeof(T) == 4)
-    {
-        const float2 q = *reinterpret_cast<const float2*>(src);
-        v[0] = q.x; v[1] = q.y;
-    }
-    else
-    {
-#pragma unroll
-        for (int j = 0; j < d; ++j) v[j] = src[j];
-    }
-}
-
-template <int d, typename T>
-__device__ __forceinline__ void load_block(const T* __restrict__ B, T (&v)[d * d])
-{
-    if constexpr (d == 2 && sizeof(T) == 4)
-    {
-        const float4 q = __ldg(reinterpret_cast<const float4*>(B));
-        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
-    }
-    else if constexpr (d == 2 && sizeof(T) == 8)
-    {
-        const double2 q0 = __ldg(reinterpret_cast<const double2*>(B));
-        const double2 q1 = __ldg(reinterpret_cast<const double2*>(B) + 1);
-        v[0] = q0.x; v[1] = q0.y; v[2] = q1.x; v[3] = q1.y;
-    }
-    else
-    {
-#pragma unroll
-        for (int i = 0; i < d * d; ++i) v[i] = __ldg(B + i);
-    }
-}
-
 /* SpMV fused with the p update and the p.Ap reduction:
      Ap = A z + beta Ap,  p = z + beta p  (A p_new = A z + beta A p_old),
    so p is never gathered and the separate p = z + beta p pass disappears.
-   One thread per block row; the block loop is unrolled four ways so four
-   column ids, four blocks and four z gathers are in flight at once (the
-   row-at-a-time loop was latency-bound on the bcol -> z dependency). */
+   One thread per block row (bsr_row_product). */
 template <int d, typename T, int G>
 __global__ void __launch_bounds__(RED_THREADS) k_pcg_spmv_fused(int64_t nh, const int32_t* __restrict__ bptr,
                                                                 const int32_t* __restrict__ bcol, const T* __restrict__ H,
@@ -213,39 +162,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_spmv_fused(int64_t nh, cons
     GRID_STRIDE(u, nh)
     {
         T y[d];
-#pragma unroll
-        for (int i = 0; i < d; ++i) y[i] = T(0);
-        int32_t b = bptr[u];
-        const int32_t b1 = bptr[u + 1];
-        for (; b + 4 <= b1; b += 4)
-        {
-            int64_t v[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) v[k] = __ldg(bcol + b + k);
-            T B[4][d * d], zv[4][d];
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-            {
-                load_block<d, T>(H + (int64_t)(b + k) * d * d, B[k]);
-                load_vec<d, T>(z + v[k] * d, zv[k]);
-            }
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-#pragma unroll
-                for (int i = 0; i < d; ++i)
-#pragma unroll
-                    for (int j = 0; j < d; ++j) y[i] += B[k][i * d + j] * zv[k][j];
-        }
-        for (; b < b1; ++b)
-        {
-            const int64_t v = __ldg(bcol + b);
-            T B[d * d];
-            load_block<d, T>(H + (int64_t)b * d * d, B);
-#pragma unroll
-            for (int i = 0; i < d; ++i)
-#pragma unroll
-                for (int j = 0; j < d; ++j) y[i] += B[i * d + j] * z[v * d + j];
-        }
+        bsr_row_product<d, T>(bptr, bcol, H, z, u, y);
 #pragma unroll
         for (int i = 0; i < d; ++i)
         {
