@@ -130,10 +130,13 @@ template <typename T, int K> struct GradOf { using type = double; };
 template <int K> struct GradOf<float, K> { using type = std::conditional_t<(K <= 8), DoubleFloat, double>; };
 
 /* For k <= 8 the PSD projection runs in its own kernel (k_project_blocks)
-   over the element blocks the evaluation kernel wrote: the evaluation needs
-   ~250 registers a thread for the live Scalar<k> intermediates, the k = 6
-   projection under 70, so apart it runs at several times the occupancy for
-   the price of re-reading and re-writing the blocks once.  At k = 12 the
+   over the element blocks the evaluation kernel wrote, at 64 registers a
+   thread against the evaluation's 128.  On the 1.64M-face disk (k = 6,
+   reduced mixed evaluation, deflated 4 x 4 projection) the split pair takes
+   0.394 ms; fused into the evaluation it takes 0.395 / 0.429 / 0.510 ms
+   with launch bounds of 4 / 3 / 2 resident blocks per SM -- the
+   projection's registers cost the evaluation spills or occupancy, which
+   outweighs the block re-read.  At k = 12 the
    evaluation alone spills, and a second pass only adds traffic (13.6 ms
    fused, 18.4 ms split on 663,552 tets with the full 12 x 12 projection), so
    it stays fused. */
