@@ -61,6 +61,9 @@ struct BatchScalars
     double* step;     // [m]
     int32_t* searching;   // meshes without an accepted trial after the last selection
     int32_t* pcg_active;  // [2] meshes still iterating after the last two PCG updates (ping-pong)
+    int32_t* stalled;     // [m] no trial step passed the Armijo test: x stays, and so would every later
+                          // iteration's result; the mesh is left out of the PCG and the line search
+                          // until the next solve call
 };
 
 constexpr int LS_TRIALS = 16;
@@ -289,7 +292,7 @@ __global__ void k_b_pcg_init(const Chunk* ch, int n_chunks, const int32_t* mcb, 
             S.tol2[m] = rel_tol * rel_tol * tot[1];
             S.iters[m] = 0;
             S.beta[m] = 0.0;
-            S.done[m] = tot[1] == 0.0 ? 1 : 0;
+            S.done[m] = (tot[1] == 0.0 || S.stalled[m]) ? 1 : 0;
         }
     }
 }
@@ -398,13 +401,15 @@ __global__ void k_b_neg(int64_t n, const double* a, double* out)
         out[i] = -a[i];
 }
 
-/* per-mesh Armijo choice among trials [t0, t0 + nt) (LineSearch.hh:14-24) */
+/* per-mesh Armijo choice among trials [t0, t0 + nt) (LineSearch.hh:14-24);
+   a mesh left without a step after the last trial is stalled (the single
+   problem's Newton loop stops there) */
 __global__ void k_b_ls_select(int n_meshes, int t0, int nt, const double* steps, double c_armijo, BatchScalars S)
 {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= n_meshes) return;
     if (t0 == 0) S.choice[m] = -1;
-    if (S.choice[m] >= 0) return;
+    if (S.choice[m] >= 0 || S.stalled[m]) return;
     for (int j = 0; j < nt; ++j)
     {
         const double fn = S.ftr[m * LS_TRIALS + t0 + j];
@@ -415,7 +420,8 @@ __global__ void k_b_ls_select(int n_meshes, int t0, int nt, const double* steps,
             return;
         }
     }
-    atomicAdd(S.searching, 1);   // the later trial launches return at once when none search
+    if (t0 + nt >= LS_TRIALS) S.stalled[m] = 1;
+    else atomicAdd(S.searching, 1);   // the later trial launches return at once when none search
 }
 
 template <int d>
@@ -705,8 +711,8 @@ static tad_status batch_prepare(tad_batch* B)
         const int nm = B->n_meshes;
         TAD_CUDA_TRY(cudaMalloc(&B->scal, (size_t)nm * (LS_TRIALS + 12) * sizeof(double)));
         TAD_CUDA_TRY(cudaMemset(B->scal, 0, (size_t)nm * (LS_TRIALS + 12) * sizeof(double)));
-        TAD_CUDA_TRY(cudaMalloc(&B->iscal, (size_t)(nm * 4 + 2) * sizeof(int32_t)));
-        TAD_CUDA_TRY(cudaMemset(B->iscal, 0, (size_t)(nm * 4 + 2) * sizeof(int32_t)));
+        TAD_CUDA_TRY(cudaMalloc(&B->iscal, (size_t)(nm * 5 + 2) * sizeof(int32_t)));
+        TAD_CUDA_TRY(cudaMemset(B->iscal, 0, (size_t)(nm * 5 + 2) * sizeof(int32_t)));
         double* q = B->scal;
         B->S.f = q; q += nm;
         B->S.ftr = q; q += (size_t)nm * LS_TRIALS;
@@ -724,6 +730,7 @@ static tad_status batch_prepare(tad_batch* B)
         B->S.choice = B->iscal + 2 * nm;
         B->S.searching = B->iscal + 3 * nm;
         B->S.pcg_active = B->iscal + 4 * nm;
+        B->S.stalled = B->iscal + 4 * nm + 2;
         TAD_CUDA_TRY(cudaMalloc(&B->steps, LS_TRIALS * sizeof(double)));
         std::vector<double> st(LS_TRIALS);
         double sv = 1.0;
@@ -750,6 +757,7 @@ TAD_API tad_status tad_batch_newton_solve_d(tad_batch* B, double* x_d, int n_ite
     B->pcg_iters = std::max(1, std::min(P.settings.pcg_max_iters, 4096));
     B->pcg_tol = P.settings.pcg_rel_tol;
     TAD_CUDA_TRY(cudaMemcpyAsync(B->x, x_d, P.n_vars * 8, cudaMemcpyDeviceToDevice, P.stream));
+    TAD_CUDA_TRY(cudaMemsetAsync(B->S.stalled, 0, (size_t)nm * sizeof(int32_t), P.stream));   // a new start
     if (!B->graph)
     {
         s = batch_capture(*B, eps);
@@ -832,8 +840,10 @@ TAD_API tad_status tad_batch_autotune(tad_batch* B, const double* x_d, double ep
             if (s != TAD_OK) return s;
             float ms = 0.f;
             TAD_CUDA_TRY(cudaMemcpyAsync(B->x, x_d, P.n_vars * 8, cudaMemcpyDeviceToDevice, P.stream));
+            TAD_CUDA_TRY(cudaMemsetAsync(B->S.stalled, 0, (size_t)B->n_meshes * sizeof(int32_t), P.stream));
             TAD_CUDA_TRY(cudaGraphLaunch(B->graph, P.stream));
             TAD_CUDA_TRY(cudaMemcpyAsync(B->x, x_d, P.n_vars * 8, cudaMemcpyDeviceToDevice, P.stream));
+            TAD_CUDA_TRY(cudaMemsetAsync(B->S.stalled, 0, (size_t)B->n_meshes * sizeof(int32_t), P.stream));
             cudaEventRecord(P.ev[5], P.stream);
             for (int k = 0; k < TUNE_ITERS; ++k) TAD_CUDA_TRY(cudaGraphLaunch(B->graph, P.stream));
             cudaEventRecord(P.ev[6], P.stream);
