@@ -61,3 +61,27 @@ def test_batch_deterministic_and_autotune(tad):
     assert np.all(f5[-1] < f5[0])
     with pytest.raises(tad.TinyADError):
         b.set_chunking(16, 64)
+
+
+def test_batch_mesh_without_elements(tad, oracle):
+    """A mesh with handles but no elements (zero energy and gradient, no
+    Hessian blocks) rides along: its variables come back unchanged, its
+    energy stays 0, and the other meshes converge as they do alone.  The
+    launch shape is set before the first solve."""
+    ws = _meshes()[:3]
+    t0 = ws[0].terms[0]
+    empty = meshes.Workload(name="empty", var_dim=2, n_handles=7, x0=np.linspace(0.0, 1.0, 14),
+                            terms=[meshes.Term(t0.energy, t0.valence, np.zeros((0, t0.valence), np.int32),
+                                               np.zeros((0, t0.params.shape[1])))])
+    ws = [ws[0], empty, ws[1], ws[2]]
+    b = tad.Batch(ws, precision=1, pcg_rel_tol=1e-5, pcg_max_iters=400)
+    b.set_chunking(32, 64)
+    x, fh = b.newton_solve(b.x0(), 40)
+    xs = b.split(x)
+    assert np.array_equal(xs[1], empty.x0)
+    assert np.all(fh[:, 1] == 0.0)
+    for m in (0, 2, 3):
+        w = ws[m]
+        p = oracle.Problem.from_workload(w)
+        _, fho, _ = p.newton(w.x0, 40)
+        assert abs(p.eval(xs[m]) - fho[-1]) <= 1e-8 * abs(fho[-1]), (m, p.eval(xs[m]), fho[-1])

@@ -445,7 +445,7 @@ struct Batch
     int n_meshes = 0;
     std::vector<int64_t> vert_off;           // per mesh handle offset (n_meshes + 1)
     std::vector<std::vector<int64_t>> elem_cnt; // per term, per mesh element counts (built while adding)
-    int chunk_rows = 1024, threads = 256, grid = 608;
+    int chunk_rows = 1024, threads = 256, grid = 0;   // grid: 4 blocks per SM, set when the batch is prepared
     // device
     Chunk *vch = nullptr, *ech = nullptr;
     int n_vch = 0, n_ech = 0;
@@ -706,6 +706,9 @@ static tad_status batch_prepare(tad_batch* B)
     if (s != TAD_OK) return s;
     if (!B->counters)
     {
+        int sms = 0;
+        TAD_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, B->P->device));
+        B->grid = 4 * std::max(sms, 1);
         TAD_CUDA_TRY(cudaMalloc(&B->counters, (size_t)LS_TRIALS * 4096 * sizeof(unsigned)));
         TAD_CUDA_TRY(cudaMemset(B->counters, 0, (size_t)LS_TRIALS * 4096 * sizeof(unsigned)));
         const int nm = B->n_meshes;
@@ -833,7 +836,6 @@ TAD_API tad_status tad_batch_autotune(tad_batch* B, const double* x_d, double ep
         {
             B->chunk_rows = rows;
             B->threads = thr;
-            B->grid = 4 * 152;
             s = batch_setup_chunks(*B);
             if (s != TAD_OK) return s;
             s = batch_capture(*B, eps);
