@@ -10,7 +10,8 @@
  * preconditioner (inverted d x d diagonal blocks).  One iteration is two
  * kernels over a fixed grid (RED_BLOCKS x RED_THREADS, grid-stride):
  *   k_pcg_spmv_fused  Ap = H z + beta Ap and p = z + beta p (BSR, one thread
- *                     per block row), fused with the p.Ap reduction; the last
+ *                     per block row; k_pcg_spmv_vec, 8 lanes per row, for
+ *                     3 x 3 blocks), fused with the p.Ap reduction; the last
  *                     block computes alpha on the device
  *   k_pcg_update      x += alpha p, r -= alpha Ap, z = M^-1 r fused with the
  *                     r.z and r.r reductions; the last block computes beta and
@@ -316,14 +317,6 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_update(int64_t nh, T* x, T*
         ds->iters += 1;
         if (tot[1] <= ds->tol2 || ds->iters >= ds->max_iters || !isfinite(tot[1])) ds->done = 1;
     }
-}
-
-template <int d, typename T>
-__global__ void __launch_bounds__(RED_THREADS) k_pcg_pupdate(int64_t n, const T* __restrict__ z, T* __restrict__ p, const DevScalars* ds)
-{
-    if (*(volatile const int32_t*)&ds->done) return;
-    const T beta = from_double<T>(ds->beta);
-    GRID_STRIDE(i, n) p[i] = z[i] + beta * p[i];
 }
 
 /* ---- vector helpers ------------------------------------------------------ */
