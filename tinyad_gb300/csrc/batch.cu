@@ -64,6 +64,9 @@ struct BatchScalars
     int32_t* stalled;     // [m] no trial step passed the Armijo test: x stays, and so would every later
                           // iteration's result; the mesh is left out of the PCG and the line search
                           // until the next solve call
+    int32_t* need_eval;   // meshes that rejected the full step in the last iteration (0: the
+                          // derivatives assembled at x + d are those of every mesh's new x)
+    double* f_start;      // [m] energy at the start of the last iteration (the history)
 };
 
 constexpr int LS_TRIALS = 16;
@@ -395,12 +398,6 @@ __global__ void k_b_to_double(int64_t n, const T* a, double* out)
         out[i] = as_double(a[i]);
 }
 
-__global__ void k_b_neg(int64_t n, const double* a, double* out)
-{
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        out[i] = -a[i];
-}
-
 /* per-mesh Armijo choice among trials [t0, t0 + nt) (LineSearch.hh:14-24);
    a mesh left without a step after the last trial is stalled (the single
    problem's Newton loop stops there) */
@@ -436,6 +433,23 @@ __global__ void k_b_axpy(const Chunk* ch, int n_chunks, double* x, const double*
     }
 }
 
+/* energy of the next iteration's x: the full step's (trial 0, evaluated with
+   the derivatives at x + d) for the meshes that took it or are stalled
+   (their d is 0); the others are evaluated afresh (need_eval) */
+__global__ void k_b_adopt_f(int n_meshes, BatchScalars S)
+{
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n_meshes) return;
+    if (S.choice[m] == 0 || S.stalled[m]) S.f[m] = S.ftr[m * LS_TRIALS];
+}
+
+template <int d>
+__global__ void k_b_add(int64_t n, const double* __restrict__ x, const double* __restrict__ dx, double* __restrict__ xt)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        xt[i] = x[i] + dx[i];
+}
+
 /* line-search trial energies of meshes that have not accepted a step yet are
    computed for all meshes (one launch); k_b_ls_select ignores the rest */
 
@@ -466,6 +480,7 @@ struct Batch
     int graph_iters = 0;
     double* fh = nullptr;           // pinned [n_meshes]
     double* x = nullptr;            // device state
+    double* xt = nullptr;           // x + d, where the full step's derivatives are evaluated
     int pcg_iters = 64;
     double pcg_tol = 1e-2;
 };
@@ -566,13 +581,22 @@ static tad_status record_iteration(Batch& B, int prec, double eps)
     T *r, *z, *p, *Ap, *xs, *dinv;
     if (prec == TAD_PREC_MIXED) { r = (T*)P.r32; z = (T*)P.z32; p = (T*)P.p32; Ap = (T*)P.Ap32; xs = (T*)P.dx32; dinv = (T*)P.dinv32; }
     else { r = (T*)P.r; z = (T*)P.z; p = (T*)P.p; Ap = (T*)P.Ap; xs = (T*)P.dx; dinv = (T*)P.dinv; }
-    // 1. element Hessians (all meshes, one launch per term), f per mesh, assembly
+    // 1. element Hessians at x (all meshes, one launch per term), f per mesh,
+    // assembly of g, rhs = -g and H -- only when some mesh did not take the
+    // previous iteration's full step (or a solve call starts): otherwise the
+    // derivatives assembled at that step's x + d are current
+    P.launch_guard = B.S.need_eval;
     tad_status st = eval_elements(P, TAD_MODE_HESSIAN_PROJ, B.x, eps, prec);
+    if (st == TAD_OK)
+    {
+        k_b_reduce_rows<<<dim3(G, 1), TH, 0, s>>>(B.ech, B.n_ech, B.emcb, B.emce, P.ef, P.n_elem_total, B.partials,
+                                                  B.counters, B.S.f, 1, B.S.need_eval);
+        launch_assemble_grad_newton(P, prec, prec == TAD_PREC_MIXED);
+        launch_assemble_hess(P, prec);
+    }
+    P.launch_guard = nullptr;
     if (st != TAD_OK) return st;
-    k_b_reduce_rows<<<dim3(G, 1), TH, 0, s>>>(B.ech, B.n_ech, B.emcb, B.emce, P.ef, P.n_elem_total, B.partials, B.counters, B.S.f, 1);
-    launch_assemble_grad(P, prec, prec == TAD_PREC_MIXED);
-    launch_assemble_hess(P, prec);
-    k_b_neg<<<G, TH, 0, s>>>(n, P.g, P.rhs);
+    TAD_CUDA_TRY(cudaMemcpyAsync(B.S.f_start, B.S.f, (size_t)B.n_meshes * sizeof(double), cudaMemcpyDeviceToDevice, s));
     // 2. PCG, per-mesh tolerance.  Iteration it reads the active count the
     // previous update left in pcg_active[it & 1] and counts into the other
     // slot; the first count is set nonzero so the first iteration runs.
@@ -595,29 +619,46 @@ static tad_status record_iteration(Batch& B, int prec, double eps)
                                                   B.partials, B.counters, B.S, B.pcg_iters, in, out);
     }
     k_b_to_double<T><<<G, TH, 0, s>>>(n, xs, P.dx);
-    // 3. line search: d.g per mesh; the full step alone, then batches of up to
-    // 8 trials that run only while some mesh has not accepted a step (the
+    // 3. line search: d.g per mesh (with the g at x, before the full step's
+    // assembly replaces it).  The full step s = 1 is evaluated by the full
+    // element kernels and assembly at x + d, which are the next iteration's
+    // derivatives for every mesh that takes it (as in the single-problem
+    // loop); its energies are trial 0.  Then batches of 8 and 7 energy-only
+    // trials at x + s d run only while some mesh has not accepted a step (the
     // trial kernels read the count the selection leaves and return at once
-    // when it is 0); per-mesh choice and step
+    // when it is 0); per-mesh choice and step.
     k_b_dot<d><<<G, TH, 0, s>>>(B.vch, B.n_vch, B.vmcb, B.vmce, P.dx, P.g, B.partials, B.counters, B.S.dg);
+    k_b_add<d><<<G, TH, 0, s>>>(n, B.x, P.dx, B.xt);
+    st = eval_elements(P, TAD_MODE_HESSIAN_PROJ, B.xt, eps, prec);
+    if (st != TAD_OK) return st;
+    k_b_reduce_rows<<<dim3(G, 1), TH, 0, s>>>(B.ech, B.n_ech, B.emcb, B.emce, P.ef, P.n_elem_total, B.partials,
+                                              B.counters, B.S.ftr, LS_TRIALS);
+    launch_assemble_grad_newton(P, prec, prec == TAD_PREC_MIXED);
+    launch_assemble_hess(P, prec);
     for (int t0 = 0; t0 < LS_TRIALS;)
     {
         const int nb = t0 == 0 ? 1 : std::min(LS_BATCH, LS_TRIALS - t0);
-        double* save = P.steps;
-        P.steps = B.steps + t0;
-        P.launch_guard = t0 == 0 ? nullptr : B.S.searching;
-        st = eval_elements(P, TAD_MODE_LINESEARCH, B.x, 0.0, P.precision, P.dx, nb);
-        P.steps = save;
-        P.launch_guard = nullptr;
-        if (st != TAD_OK) return st;
-        k_b_reduce_rows<<<dim3(G, nb), TH, 0, s>>>(B.ech, B.n_ech, B.emcb, B.emce, P.ef, P.n_elem_total,
-                                                   B.partials, B.counters, B.S.ftr + t0, LS_TRIALS,
-                                                   t0 == 0 ? nullptr : B.S.searching);
+        if (t0 > 0)
+        {
+            double* save = P.steps;
+            P.steps = B.steps + t0;
+            P.launch_guard = B.S.searching;
+            st = eval_elements(P, TAD_MODE_LINESEARCH, B.x, 0.0, P.precision, P.dx, nb);
+            P.steps = save;
+            P.launch_guard = nullptr;
+            if (st != TAD_OK) return st;
+            k_b_reduce_rows<<<dim3(G, nb), TH, 0, s>>>(B.ech, B.n_ech, B.emcb, B.emce, P.ef, P.n_elem_total,
+                                                       B.partials, B.counters, B.S.ftr + t0, LS_TRIALS, B.S.searching);
+        }
         TAD_CUDA_TRY(cudaMemsetAsync(B.S.searching, 0, sizeof(int32_t), s));
         k_b_ls_select<<<(B.n_meshes + 255) / 256, 256, 0, s>>>(B.n_meshes, t0, nb, B.steps, P.settings.ls_armijo, B.S);
+        // the meshes that rejected the full step need an evaluation at their new x
+        if (t0 == 0)
+            TAD_CUDA_TRY(cudaMemcpyAsync(B.S.need_eval, B.S.searching, sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
         t0 += nb;
     }
     k_b_axpy<d><<<G, TH, 0, s>>>(B.vch, B.n_vch, B.x, P.dx, B.S, 0);
+    k_b_adopt_f<<<(B.n_meshes + 255) / 256, 256, 0, s>>>(B.n_meshes, B.S);
     (void)nh;
     TAD_CUDA_TRY(cudaGetLastError());
     return TAD_OK;
@@ -712,10 +753,10 @@ static tad_status batch_prepare(tad_batch* B)
         TAD_CUDA_TRY(cudaMalloc(&B->counters, (size_t)LS_TRIALS * 4096 * sizeof(unsigned)));
         TAD_CUDA_TRY(cudaMemset(B->counters, 0, (size_t)LS_TRIALS * 4096 * sizeof(unsigned)));
         const int nm = B->n_meshes;
-        TAD_CUDA_TRY(cudaMalloc(&B->scal, (size_t)nm * (LS_TRIALS + 12) * sizeof(double)));
-        TAD_CUDA_TRY(cudaMemset(B->scal, 0, (size_t)nm * (LS_TRIALS + 12) * sizeof(double)));
-        TAD_CUDA_TRY(cudaMalloc(&B->iscal, (size_t)(nm * 5 + 2) * sizeof(int32_t)));
-        TAD_CUDA_TRY(cudaMemset(B->iscal, 0, (size_t)(nm * 5 + 2) * sizeof(int32_t)));
+        TAD_CUDA_TRY(cudaMalloc(&B->scal, (size_t)nm * (LS_TRIALS + 13) * sizeof(double)));
+        TAD_CUDA_TRY(cudaMemset(B->scal, 0, (size_t)nm * (LS_TRIALS + 13) * sizeof(double)));
+        TAD_CUDA_TRY(cudaMalloc(&B->iscal, (size_t)(nm * 5 + 3) * sizeof(int32_t)));
+        TAD_CUDA_TRY(cudaMemset(B->iscal, 0, (size_t)(nm * 5 + 3) * sizeof(int32_t)));
         double* q = B->scal;
         B->S.f = q; q += nm;
         B->S.ftr = q; q += (size_t)nm * LS_TRIALS;
@@ -728,12 +769,14 @@ static tad_status batch_prepare(tad_batch* B)
         B->S.beta = q; q += nm;
         B->S.rr = q; q += nm;
         B->S.step = q; q += nm;
+        B->S.f_start = q; q += nm;
         B->S.done = B->iscal;
         B->S.iters = B->iscal + nm;
         B->S.choice = B->iscal + 2 * nm;
         B->S.searching = B->iscal + 3 * nm;
         B->S.pcg_active = B->iscal + 4 * nm;
         B->S.stalled = B->iscal + 4 * nm + 2;
+        B->S.need_eval = B->iscal + 5 * nm + 2;
         TAD_CUDA_TRY(cudaMalloc(&B->steps, LS_TRIALS * sizeof(double)));
         std::vector<double> st(LS_TRIALS);
         double sv = 1.0;
@@ -741,6 +784,7 @@ static tad_status batch_prepare(tad_batch* B)
         TAD_CUDA_TRY(cudaMemcpy(B->steps, st.data(), LS_TRIALS * sizeof(double), cudaMemcpyHostToDevice));
         TAD_CUDA_TRY(cudaMallocHost(&B->fh, (size_t)nm * sizeof(double)));
         TAD_CUDA_TRY(cudaMalloc(&B->x, B->P->n_vars * sizeof(double)));
+        TAD_CUDA_TRY(cudaMalloc(&B->xt, B->P->n_vars * sizeof(double)));
         s = batch_setup_chunks(*B);
         if (s != TAD_OK) return s;
     }
@@ -760,7 +804,9 @@ TAD_API tad_status tad_batch_newton_solve_d(tad_batch* B, double* x_d, int n_ite
     B->pcg_iters = std::max(1, std::min(P.settings.pcg_max_iters, 4096));
     B->pcg_tol = P.settings.pcg_rel_tol;
     TAD_CUDA_TRY(cudaMemcpyAsync(B->x, x_d, P.n_vars * 8, cudaMemcpyDeviceToDevice, P.stream));
-    TAD_CUDA_TRY(cudaMemsetAsync(B->S.stalled, 0, (size_t)nm * sizeof(int32_t), P.stream));   // a new start
+    // a new start: no mesh stalled, and the first iteration evaluates at x
+    TAD_CUDA_TRY(cudaMemsetAsync(B->S.stalled, 0, (size_t)nm * sizeof(int32_t), P.stream));
+    TAD_CUDA_TRY(cudaMemsetAsync(B->S.need_eval, 1, sizeof(int32_t), P.stream));
     if (!B->graph)
     {
         s = batch_capture(*B, eps);
@@ -772,7 +818,7 @@ TAD_API tad_status tad_batch_newton_solve_d(tad_batch* B, double* x_d, int n_ite
         P.n_launches += 1;
         if (f_hist_h)
         {
-            TAD_CUDA_TRY(cudaMemcpyAsync(B->fh, B->S.f, nm * 8, cudaMemcpyDeviceToHost, P.stream));
+            TAD_CUDA_TRY(cudaMemcpyAsync(B->fh, B->S.f_start, nm * 8, cudaMemcpyDeviceToHost, P.stream));
             TAD_CUDA_TRY(cudaStreamSynchronize(P.stream));
             std::copy(B->fh, B->fh + nm, f_hist_h + (size_t)it * nm);
         }
@@ -843,9 +889,11 @@ TAD_API tad_status tad_batch_autotune(tad_batch* B, const double* x_d, double ep
             float ms = 0.f;
             TAD_CUDA_TRY(cudaMemcpyAsync(B->x, x_d, P.n_vars * 8, cudaMemcpyDeviceToDevice, P.stream));
             TAD_CUDA_TRY(cudaMemsetAsync(B->S.stalled, 0, (size_t)B->n_meshes * sizeof(int32_t), P.stream));
+            TAD_CUDA_TRY(cudaMemsetAsync(B->S.need_eval, 1, sizeof(int32_t), P.stream));
             TAD_CUDA_TRY(cudaGraphLaunch(B->graph, P.stream));
             TAD_CUDA_TRY(cudaMemcpyAsync(B->x, x_d, P.n_vars * 8, cudaMemcpyDeviceToDevice, P.stream));
             TAD_CUDA_TRY(cudaMemsetAsync(B->S.stalled, 0, (size_t)B->n_meshes * sizeof(int32_t), P.stream));
+            TAD_CUDA_TRY(cudaMemsetAsync(B->S.need_eval, 1, sizeof(int32_t), P.stream));
             cudaEventRecord(P.ev[5], P.stream);
             for (int k = 0; k < TUNE_ITERS; ++k) TAD_CUDA_TRY(cudaGraphLaunch(B->graph, P.stream));
             cudaEventRecord(P.ev[6], P.stream);
@@ -892,7 +940,7 @@ TAD_API tad_status tad_batch_destroy(tad_batch* B)
     if (B->P) cudaStreamSynchronize(B->P->stream);
     if (B->graph) cudaGraphExecDestroy(B->graph);
     void* bufs[] = {B->vch, B->ech, B->vmcb, B->vmce, B->emcb, B->emce, B->partials, B->counters, B->scal, B->iscal,
-                    B->steps, B->x, B->pch, B->pmcb, B->pmce, B->n_pch, B->row_off};
+                    B->steps, B->x, B->xt, B->pch, B->pmcb, B->pmce, B->n_pch, B->row_off};
     for (void* b : bufs) if (b) cudaFree(b);
     if (B->fh) cudaFreeHost(B->fh);
     tad_problem_destroy(B->P);
