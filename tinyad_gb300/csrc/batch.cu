@@ -18,11 +18,14 @@
  * iterations 0-4, 6, 8, 12, 16, ...), cut so that the remaining rows spread
  * over the whole grid, one block per chunk.
  *
- * One Newton iteration (elements -> f -> assembly -> PCG with a fixed number
- * of iterations, each mesh stopping at its own tolerance -> the full step,
- * then batches of 8 and 7 line-search trials while some mesh has not
- * accepted one -> per-mesh step) has a fixed launch sequence and is captured
- * once as a CUDA graph; the host replays one graph per iteration.  Kernels
+ * One Newton iteration (elements -> f -> assembly, only when some mesh did
+ * not take the previous full step -> PCG with a fixed number of iterations,
+ * each mesh stopping at its own tolerance -> the full step, evaluated by the
+ * element kernels and assembly at x + d, which are the next iteration's
+ * derivatives -> batches of 8 and 7 energy-only trials while some mesh has
+ * not accepted one -> per-mesh step) has a fixed launch sequence and is
+ * captured once as a CUDA graph; the host replays one graph per iteration.
+ * Kernels
  * of the PCG iterations after every mesh has converged, and of the trials
  * after every mesh has accepted a step, return at once (device counters).
  * A small autotuner times candidate chunk sizes / block sizes on the batch
