@@ -25,9 +25,9 @@
  * derivatives -> batches of 8 and 7 energy-only trials while some mesh has
  * not accepted one -> per-mesh step) has a fixed launch sequence and is
  * captured once as a CUDA graph; the host replays one graph per iteration.
- * Kernels
- * of the PCG iterations after every mesh has converged, and of the trials
- * after every mesh has accepted a step, return at once (device counters).
+ * Kernels of the PCG iterations after every mesh has converged, and of the
+ * trials after every mesh has accepted a step, return at once (device
+ * counters).
  * A small autotuner times candidate chunk sizes / block sizes on the batch
  * itself and keeps the fastest.
  */
