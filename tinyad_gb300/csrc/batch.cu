@@ -579,7 +579,7 @@ static tad_status record_iteration(Batch& B, int prec, double eps)
     Problem& P = *B.P;
     cudaStream_t s = P.stream;
     const int G = B.grid, TH = B.threads;
-    const int64_t n = P.n_vars, nh = P.n_handles;
+    const int64_t n = P.n_vars;
     T* H = (T*)P.H;
     T *r, *z, *p, *Ap, *xs, *dinv;
     if (prec == TAD_PREC_MIXED) { r = (T*)P.r32; z = (T*)P.z32; p = (T*)P.p32; Ap = (T*)P.Ap32; xs = (T*)P.dx32; dinv = (T*)P.dinv32; }
@@ -662,7 +662,6 @@ static tad_status record_iteration(Batch& B, int prec, double eps)
     }
     k_b_axpy<d><<<G, TH, 0, s>>>(B.vch, B.n_vch, B.x, P.dx, B.S, 0);
     k_b_adopt_f<<<(B.n_meshes + 255) / 256, 256, 0, s>>>(B.n_meshes, B.S);
-    (void)nh;
     TAD_CUDA_TRY(cudaGetLastError());
     return TAD_OK;
 }
