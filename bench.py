@@ -225,20 +225,25 @@ class ClockSampler:
 # CPU baseline: the oracle (restatement of the reference's OpenMP path)
 # ---------------------------------------------------------------------------
 CPU_SAMPLE = "disk512"
+CPU_SAMPLE_MAX_ELEMENTS = 500_000   # a workload up to this size is timed whole
 
 
-def cpu_sample_name(full_name: str) -> str:
-    return "tet24" if full_name.startswith("tet") else CPU_SAMPLE
+def cpu_sample(full_w):
+    """The mesh the CPU legs time: the workload itself up to
+    CPU_SAMPLE_MAX_ELEMENTS elements, else a smaller mesh of the same family
+    (512-grid disk / 24^3 tet cube), scaled to the workload by element count."""
+    if full_w.n_elements <= CPU_SAMPLE_MAX_ELEMENTS:
+        return full_w
+    return make_workload("tet24" if full_w.name.startswith("tet") else CPU_SAMPLE)
 
 
 def cpu_baseline(full_w, threads: int | None = None) -> dict:
     """One oracle Projected-Newton iteration (OpenMP element eval, serial
-    scatter + triplet sort, sparse LDL^T, Armijo) on a smaller mesh of the
-    same family (512-grid disk / 24^3 tet cube), scaled to the benchmark mesh
-    by element count."""
+    scatter + triplet sort, sparse LDL^T, Armijo) on cpu_sample(full_w),
+    scaled to the benchmark mesh by element count."""
     from oracle import pyoracle
-    CPU = cpu_sample_name(full_w.name)
-    w = make_workload(CPU)
+    w = cpu_sample(full_w)
+    CPU = w.name
     nthreads = threads if threads else -1
     p = pyoracle.Problem.from_workload(w, n_threads=nthreads)
     t0 = time.perf_counter()
@@ -261,7 +266,7 @@ def run_reference(args):
         return
     from oracle import pyoracle
     full = make_workload(args.workload)
-    w = make_workload(cpu_sample_name(args.workload))
+    w = cpu_sample(full)
     threads = os.cpu_count() or 1
     p = pyoracle.Problem.from_workload(w, n_threads=threads)
     x = w.x0.copy()
