@@ -447,3 +447,15 @@ def test_newton_calls_continue(tad, precision):
     xc[0] += 1e-7
     xc2, fhc = fb.newton_solve(xc, 1)
     assert abs(fhc[0] - fb.eval(xc)) <= 1e-12 * abs(fhc[0])
+    # zero iterations return x as given, whether or not the call would have continued
+    xs, _ = fb.newton_solve(xc2, 1)
+    xz = xs.copy()
+    xz[1] += 1e-7
+    xr, _ = fb.newton_solve(xz, 0)
+    assert np.array_equal(xr, xz)
+    xr2, _ = fb.newton_solve(xr, 0)
+    assert np.array_equal(xr2, xz)
+    # and the next iteration starts from an evaluation at that x, not from
+    # derivatives carried from before it
+    _, fhz = fb.newton_solve(xr2, 1)
+    assert abs(fhz[0] - fb.eval(xz)) <= 1e-12 * abs(fhz[0])

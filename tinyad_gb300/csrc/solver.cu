@@ -1066,15 +1066,26 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
     const bool predicted = P.last_x_valid && P.spec_valid && P.spec_eps == eps && P.spec_prec == prec;
     P.spec_valid = false;
     TAD_CUDA_TRY(cudaEventRecord(P.ev_in, st));
-    TAD_CUDA_TRY(cudaStreamWaitEvent(st2, P.ev_in, 0));
-    if (x_in_h) TAD_CUDA_TRY(cudaMemcpyAsync(x, x_in_h, n * sizeof(double), cudaMemcpyHostToDevice, st2));
-    TAD_CUDA_TRY(cudaMemsetAsync(P.diff_flag, 0, sizeof(int32_t), st2));
-    if (P.last_x_valid)
-    {
-        k_differs<<<RED_BLOCKS, RED_THREADS, 0, st2>>>(n, x, P.last_x, P.diff_flag);
-        P.n_launches += 1;
-    }
-    TAD_CUDA_TRY(cudaEventRecord(P.ev_in, st2));
+    // A predicted call issues the side-stream work after its PCG's first
+    // launches (the PCG does not read x), so the GPU starts on the PCG
+    // without waiting for these API calls; the copy still waits only for the
+    // work recorded above.
+    bool input_issued = false;
+    auto issue_input = [&]() -> cudaError_t {
+        input_issued = true;
+        cudaError_t e = cudaStreamWaitEvent(st2, P.ev_in, 0);
+        if (e == cudaSuccess && x_in_h) e = cudaMemcpyAsync(x, x_in_h, n * sizeof(double), cudaMemcpyHostToDevice, st2);
+        if (e == cudaSuccess) e = cudaMemsetAsync(P.diff_flag, 0, sizeof(int32_t), st2);
+        if (e == cudaSuccess && P.last_x_valid)
+        {
+            k_differs<<<RED_BLOCKS, RED_THREADS, 0, st2>>>(n, x, P.last_x, P.diff_flag);
+            P.n_launches += 1;
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(P.ev_in, st2);
+        return e;
+    };
+    if (!predicted) TAD_CUDA_TRY(issue_input());
     bool continues = false;
     bool pending_test = predicted;   // the continuation test is read after iteration 0's first sync
     if (!predicted)
@@ -1094,6 +1105,12 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
     bool early_out = false;         // a copy of spare to x_out_h was issued on the side stream
     double* early_buf = nullptr;
     auto finish = [&](tad_status rs) {
+        if (!input_issued)
+        {
+            // a predicted call that stopped before its first PCG (no iteration
+            // asked for, or an error): x takes the input before it is used below
+            if (issue_input() == cudaSuccess) cudaStreamWaitEvent(st, P.ev_in, 0);
+        }
         if (cur != x) cudaMemcpyAsync(x, cur, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
         const bool ok = rs == TAD_OK;
         if (ok) cudaMemcpyAsync(P.last_x, x, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
@@ -1112,7 +1129,9 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
         cudaStreamSynchronize(st);
         cudaStreamSynchronize(st2);
         P.last_x_valid = ok;
-        P.spec_valid = ok && have_derivs;
+        // carried derivatives stay valid only if this call's continuation
+        // test was read (a predicted call with no iteration never reads it)
+        P.spec_valid = ok && have_derivs && !pending_test;
         P.spec_eps = eps;
         P.spec_prec = prec;
         return rs;
@@ -1174,6 +1193,7 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
         P.pcg_async = async;
         s = pcg_solve(P, P.rhs, P.dx, 0.0, prec, tol, P.settings.pcg_max_iters, &pit);
         P.pcg_async = false;
+        if (!input_issued) TAD_CUDA_TRY(issue_input());
         bool trial_done = false;
         bool d_in_fp32 = P.solution_in_dx32;
         // the speculative block of a predicted call's first iteration waits for
