@@ -36,6 +36,8 @@
  *                             include/TinyAD/Utils/GaussNewtonDirection.hh:24-64
  *   tad_line_search           line_search(x, d, f, g, func)
  *                             include/TinyAD/Utils/LineSearch.hh:26-65
+ *   tad_newton_decrement      newton_decrement(d, g)
+ *                             include/TinyAD/Utils/NewtonDecrement.hh:20-26
  *   tad_newton_solve          the Projected-Newton loop users write around the
  *                             three calls above (tests/NewtonTest.cc:69-75)
  *   tad_adjoint_rest_gradient no reference counterpart (adjoint extension)
@@ -325,10 +327,21 @@ TAD_API tad_status tad_line_search(tad_problem* p, const double* x_h,
                                    const double* d_h, double f, const double* g_h,
                                    double s_max, double* x_out_h, double* f_out);
 
+/* newton_decrement(d, g) = -d.g / 2 (one half of the squared Newton
+   decrement; the stopping test of the reference's Newton loop), computed on
+   the device with a fixed-order reduction (bitwise reproducible).  d and g
+   hold n_vars doubles: host buffers for tad_newton_decrement, device
+   buffers for tad_newton_decrement_d. */
+TAD_API tad_status tad_newton_decrement(tad_problem* p, const double* d_h, const double* g_h, double* out);
+TAD_API tad_status tad_newton_decrement_d(tad_problem* p, const double* d_d, const double* g_d, double* out);
+
 /* Run n_iters Projected-Newton iterations in place on x_h (host):
    eval_with_hessian_proj -> PCG -> Armijo line search, all on the device.
    f_hist_h (optional, n_iters+1): energy before each iteration and at the end.
-   Stops early when the Newton decrement -d.g/2 < stop_decrement (if > 0). */
+   Stops early when the Newton decrement -d.g/2 < stop_decrement (if > 0):
+   as in the reference's loop, the test is taken on the new direction before
+   the line search, so that iteration leaves x as it is; *iters_done counts
+   the steps taken and f_hist_h[*iters_done] is the final energy. */
 TAD_API tad_status tad_newton_solve(tad_problem* p, double* x_h, int n_iters,
                                     double proj_eps, double stop_decrement,
                                     double* f_hist_h, int* iters_done);

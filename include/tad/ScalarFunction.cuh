@@ -309,6 +309,17 @@ public:
         return dvec;
     }
 
+    /* newton_decrement(d, g) = -d.g / 2 (NewtonDecrement.hh:20-26), the
+       usual stopping test of a Newton loop */
+    double newton_decrement(const std::vector<double>& dvec, const std::vector<double>& g) const
+    {
+        if ((int64_t)dvec.size() != n_vars() || (int64_t)g.size() != n_vars())
+            throw std::runtime_error("d and g must hold n_vars values");
+        double out = 0.0;
+        check(tad_newton_decrement(p_, dvec.data(), g.data(), &out));
+        return out;
+    }
+
     /* line_search(x0, d, f, g, func) (LineSearch.hh:26-65) */
     std::vector<double> line_search(const std::vector<double>& x0, const std::vector<double>& dvec, double f,
                                     const std::vector<double>& g, double s_max = 1.0) const

@@ -59,6 +59,11 @@ def _d(a):
     return a.ctypes.data_as(_dp)
 
 
+def newton_decrement(d, g) -> float:
+    """newton_decrement(d, g) = -0.5 d.g (include/TinyAD/Utils/NewtonDecrement.hh:20-26)."""
+    return -0.5 * float(np.dot(np.asarray(d, np.float64), np.asarray(g, np.float64)))
+
+
 class OracleError(RuntimeError):
     pass
 

@@ -90,6 +90,13 @@ static int planar_newton()
     {
         auto [f, g, H] = func.eval_with_hessian_proj(x);
         const std::vector<double> d = func.newton_direction(x);
+        // the stopping test of the reference's loops (NewtonDecrement.hh:20-26)
+        const double dec = func.newton_decrement(d, g);
+        double ref = 0.0;
+        for (size_t j = 0; j < d.size(); ++j) ref += d[j] * g[j];
+        ref *= -0.5;
+        CHECK(std::fabs(dec - ref) <= 1e-12 * std::fabs(ref) + 1e-300);
+        if (dec < 1e-24) break;
         x = func.line_search(x, d, f, g);
         (void)H;
     }

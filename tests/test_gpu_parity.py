@@ -297,6 +297,59 @@ def test_newton_direction_api(tad, oracle):
     assert abs(d @ go - do @ go) <= 1e-8 * abs(do @ go)
 
 
+def test_newton_decrement(tad, oracle):
+    """newton_decrement (NewtonDecrement.hh:20-26) through the C ABI, host and
+    device forms, against the oracle's -d.g/2; and the reference's loop
+    (eval_with_hessian_proj -> newton_direction -> stop if the decrement is
+    below eps -> line_search) run with the library's calls and with the
+    oracle's stops after the same number of steps, as tad_newton_solve with
+    stop_decrement does (the test is taken before the step)."""
+    import torch
+    w = meshes.disk_param_pinned(12, seed=3)
+    fn, p = _pair(tad, oracle, w, pcg_rel_tol=1e-13, pcg_max_iters=5000)
+    d, f, g = fn.newton_direction(w.x0)
+    dec = fn.newton_decrement(d, g)
+    assert dec > 0.0 and abs(dec - oracle.newton_decrement(d, g)) <= 1e-14 * abs(dec)
+    dd, gd = torch.from_numpy(d).cuda(), torch.from_numpy(g).cuda()
+    assert fn.newton_decrement_device(dd.data_ptr(), gd.data_ptr()) == dec   # same fixed-order reduction
+    assert fn.newton_decrement(d, g) == dec                                   # bitwise reproducible
+    thr = 1e-12
+
+    def loop(eval_h, direction, decrement, search):
+        x, decs = w.x0.copy(), []
+        for _ in range(40):
+            f, g = eval_h(x)
+            d = direction(x, g)
+            decs.append(decrement(d, g))
+            if decs[-1] < thr:
+                break
+            x = search(x, d, f, g)
+        return x, decs
+
+    def gpu_eval(x):
+        f, g, _ = fn.eval_with_hessian_proj(x)
+        return f, g
+
+    def cpu_eval(x):
+        f, g, _ = p.eval_with_hessian_proj(x)
+        return f, g
+
+    xg, dg = loop(gpu_eval, lambda x, g: fn.newton_direction(x)[0], fn.newton_decrement,
+                  lambda x, d, f, g: fn.line_search(x, d, f, g))
+    xc, dc = loop(cpu_eval, lambda x, g: p.newton_direction(g), oracle.newton_decrement,
+                  lambda x, d, f, g: p.line_search(x, d, f, g)[0])
+    assert 2 < len(dc) < 40 and len(dg) == len(dc)
+    for a, b in zip(dg, dc):
+        if b > 1e-6:
+            assert abs(a - b) <= 1e-7 * b
+    assert rel_err(xg, xc) <= 1e-8
+    # the fused loop: the same number of steps, the same minimiser
+    steps = len(dc) - 1
+    x, fh = fn.newton_solve(w.x0, 40, stop_decrement=thr)
+    assert len(fh) - 1 == steps
+    assert rel_err(x, xc) <= 1e-8 and abs(fh[-1] - p.eval(xc)) <= 1e-12 * abs(fh[-1])
+
+
 def test_mixed_precision(tad, oracle):
     """Mixed mode: FP32 element Hessians, projection and PCG; double-float
     (~48-bit) values (edge vectors, determinant, inverse, energy) and

@@ -7,7 +7,8 @@ triangle parametrisation from the caller's device buffers with its scratch in
 a fixed device array of the library.  The test calls it through the C ABI,
 twice in a row on different inputs, and checks each result against the
 regular entry point tad_eval (which allocates at problem creation) within the
-parity tolerance of the other tests, 1e-10 relative.  It also checks the size
+parity tolerance of the other tests, 1e-10 relative, and that a repeated call
+on the same input returns the same bits.  It also checks the size
 limit is rejected with an error.  This file is collected last so that a
 failure here comes after every other test has run.
 """
@@ -47,6 +48,13 @@ def test_noalloc_energy_matches_tad_eval(tad):
         f_ref = fn.eval(x)
         assert np.isfinite(f_ref)
         assert abs(f_noalloc - f_ref) <= TOL * abs(f_ref), (f_noalloc, f_ref)
+        # the reduction has a fixed order: the same input gives the same bits
+        rc = L.tad_eval_symmetric_dirichlet_tri_noalloc(
+            ctypes.c_void_p(x_d.data_ptr()), ctypes.c_void_p(faces.data_ptr()), ctypes.c_void_p(params.data_ptr()),
+            t.handles.shape[0], ctypes.c_void_p(f_out.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
+        assert rc == 0, L.tad_last_error_message().decode()
+        stream.synchronize()
+        assert float(f_out.item()) == f_noalloc
     # beyond the fixed scratch: rejected with an error, nothing launched
     rc = L.tad_eval_symmetric_dirichlet_tri_noalloc(
         ctypes.c_void_p(x_d.data_ptr()), ctypes.c_void_p(faces.data_ptr()), ctypes.c_void_p(params.data_ptr()),

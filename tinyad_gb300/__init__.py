@@ -67,7 +67,7 @@ EXPORTS = [
     "tad_problem_set_settings", "tad_n_vars", "tad_add_elements", "tad_add_elements_custom", "tad_finalize",
     "tad_hessian_nnz", "tad_hessian_pattern", "tad_eval", "tad_eval_with_gradient", "tad_eval_with_derivatives",
     "tad_eval_with_hessian_proj", "tad_eval_d", "tad_eval_with_hessian_proj_d", "tad_newton_direction",
-    "tad_line_search", "tad_newton_solve", "tad_newton_solve_d", "tad_last_solve_stats", "tad_debug_scalar_op",
+    "tad_line_search", "tad_newton_decrement", "tad_newton_decrement_d", "tad_newton_solve", "tad_newton_solve_d", "tad_last_solve_stats", "tad_debug_scalar_op",
     "tad_get_stream", "tad_measure_fma_peak", "tad_profile_kernels",
     "tad_launch_count", "tad_adjoint_rest_gradient", "tad_eval_symmetric_dirichlet_tri_noalloc",
     "tad_batch_create", "tad_batch_add_elements", "tad_batch_newton_solve", "tad_batch_newton_solve_d",
@@ -120,6 +120,8 @@ def load(build_if_missing: bool = True):
     L.tad_gauss_newton_direction.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double, _dp, _dp, _dp]
     L.tad_newton_direction_reduced_basis.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int64, _ip, _ip, _dp, ctypes.c_double,
                                                      ctypes.c_double, _dp, _dp, _dp]
+    L.tad_newton_decrement.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
+    L.tad_newton_decrement_d.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _dp]
     L.tad_line_search.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double, _dp, ctypes.c_double, _dp, _dp]
     L.tad_newton_solve.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_double, ctypes.c_double, _dp,
                                    ctypes.POINTER(ctypes.c_int)]
@@ -315,6 +317,20 @@ class ScalarFunction:
         self._check(self.L.tad_newton_direction(self.h, _d(x), int(projected), projection_eps, 0.0, _d(d), _d(f), _d(g)),
                     allow=(TAD_ERR_PCG_NOCONV,))
         return d, float(f[0]), g
+
+    def newton_decrement(self, d, g) -> float:
+        """newton_decrement(d, g) = -d.g / 2 (NewtonDecrement.hh:20-26), reduced
+        on the device in a fixed order."""
+        d, g = self._x(d), self._x(g)
+        out = np.zeros(1)
+        self._check(self.L.tad_newton_decrement(self.h, _d(d), _d(g), _d(out)))
+        return float(out[0])
+
+    def newton_decrement_device(self, d_ptr: int, g_ptr: int) -> float:
+        """newton_decrement on device-resident d and g (pointers to n_vars doubles)."""
+        out = np.zeros(1)
+        self._check(self.L.tad_newton_decrement_d(self.h, ctypes.c_void_p(d_ptr), ctypes.c_void_p(g_ptr), _d(out)))
+        return float(out[0])
 
     def newton_direction_reduced_basis(self, x, B, projection_eps: float = default_hessian_projection_eps,
                                        w_identity: float = 0.0):

@@ -60,7 +60,7 @@ struct BatchScalars
     double* rr;
     int32_t* done;    // [m]
     int32_t* iters;   // [m]
-    int32_t* choice;  // [m] accepted trial, -1 none
+    int32_t* choice;  // [m] accepted trial, -1 none, -3 none and stalled in this iteration
     double* step;     // [m]
     int32_t* searching;   // meshes without an accepted trial after the last selection
     int32_t* pcg_active;  // [2] meshes still iterating after the last two PCG updates (ping-pong)
@@ -420,7 +420,7 @@ __global__ void k_b_ls_select(int n_meshes, int t0, int nt, const double* steps,
             return;
         }
     }
-    if (t0 + nt >= LS_TRIALS) S.stalled[m] = 1;
+    if (t0 + nt >= LS_TRIALS) { S.stalled[m] = 1; S.choice[m] = -3; }
     else atomicAdd(S.searching, 1);   // the later trial launches return at once when none search
 }
 
@@ -437,13 +437,16 @@ __global__ void k_b_axpy(const Chunk* ch, int n_chunks, double* x, const double*
 }
 
 /* energy of the next iteration's x: the full step's (trial 0, evaluated with
-   the derivatives at x + d) for the meshes that took it or are stalled
-   (their d is 0); the others are evaluated afresh (need_eval) */
+   the derivatives at x + d) for the meshes that took it, and for meshes
+   stalled before this iteration (their d is 0, so trial 0 is x itself); a
+   mesh that stalled in this iteration (choice -3) keeps f(x), since its
+   trial 0 was the rejected point; the others are evaluated afresh
+   (need_eval) */
 __global__ void k_b_adopt_f(int n_meshes, BatchScalars S)
 {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= n_meshes) return;
-    if (S.choice[m] == 0 || S.stalled[m]) S.f[m] = S.ftr[m * LS_TRIALS];
+    if (S.choice[m] == 0 || (S.stalled[m] && S.choice[m] != -3)) S.f[m] = S.ftr[m * LS_TRIALS];
 }
 
 template <int d>

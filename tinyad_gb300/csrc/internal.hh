@@ -263,9 +263,12 @@ int amg_levels(const Problem& P);
 tad_status pcg_solve(Problem& P, const double* b, double* xsol, double w_identity, int precision,
                      double rel_tol, int max_iters, int* iters_out);
 /* f_on_device: the energy at x is already in ds->f (f is then ignored);
-   t_start > 0 resumes the trial sequence there with ds->dg already set */
+   t_start > 0 resumes the trial sequence there with ds->dg already set;
+   stop_decrement > 0: if -d.g/2 < stop_decrement, x is left as it is and
+   *stopped is set (the Newton loop's stopping test, taken before the step) */
 tad_status line_search_device(Problem& P, double* x, const double* d, double f, double s_max,
-                              bool* found, double* f_out, int* trials, bool f_on_device = false, int t_start = 0);
+                              bool* found, double* f_out, int* trials, bool f_on_device = false, int t_start = 0,
+                              double stop_decrement = 0.0, bool* stopped = nullptr);
 /* x_in_h / x_out_h (host API): x is copied in from and out to these host
    buffers by the solve itself, overlapped with the compute where it can */
 tad_status newton_solve(Problem& P, double* x_d, int n_iters, double eps, double stop_decrement,

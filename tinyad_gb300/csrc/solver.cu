@@ -919,8 +919,10 @@ static tad_status ensure_step_sequence(Problem& P, double s_max, int n)
 }
 
 tad_status line_search_device(Problem& P, double* x, const double* d, double f, double s_max, bool* found,
-                              double* f_out, int* trials, bool f_on_device, int t_start)
+                              double* f_out, int* trials, bool f_on_device, int t_start, double stop_decrement,
+                              bool* stopped)
 {
+    if (stopped) *stopped = false;
     cudaStream_t s = P.stream;
     const int max_iters = P.settings.ls_max_iters > 0 ? P.settings.ls_max_iters : 64;
     tad_status st = ensure_step_sequence(P, s_max, max_iters);
@@ -951,6 +953,14 @@ tad_status line_search_device(Problem& P, double* x, const double* d, double f, 
         TAD_CUDA_TRY(cudaStreamSynchronize(s));
         // an element error of this step (or of the evaluation before it) first
         if (*P.err_h != 0) return check_device_error(P);
+        if (stop_decrement > 0.0 && P.hs->decrement < stop_decrement)
+        {
+            // converged by the Newton decrement: no step (the reference tests it before line_search)
+            if (stopped) *stopped = true;
+            if (f_out) *f_out = f_on_device ? P.hs->f : f;
+            if (trials) *trials = 0;
+            return TAD_OK;
+        }
         if (P.hs->ls_choice == -2) return fail(TAD_ERR_NONFINITE, "Assertion failed: f_new == f_new (NaN energy in line search)");
         if (P.hs->ls_choice >= 0)
         {
@@ -1108,8 +1118,15 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
         if (!input_issued)
         {
             // a predicted call that stopped before its first PCG (no iteration
-            // asked for, or an error): x takes the input before it is used below
-            if (issue_input() == cudaSuccess) cudaStreamWaitEvent(st, P.ev_in, 0);
+            // asked for, or an error): x takes the input before it is used
+            // below; a failed copy is the call's status (x may be stale)
+            const cudaError_t e = issue_input();
+            if (e == cudaSuccess) cudaStreamWaitEvent(st, P.ev_in, 0);
+            else if (rs == TAD_OK)
+            {
+                set_error(std::string("CUDA error: ") + cudaGetErrorString(e) + " (input copy)");
+                rs = TAD_ERR_CUDA;
+            }
         }
         if (cur != x) cudaMemcpyAsync(x, cur, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
         const bool ok = rs == TAD_OK;
@@ -1243,6 +1260,7 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
         if (s != TAD_OK && s != TAD_ERR_PCG_NOCONV) return finish(s);
         cudaEventRecord(ev(it, 3), st);
         bool found = false;
+        bool stopped = false;   // the Newton decrement fell below stop_decrement: no step
         double fn = 0.0;
         int trials = 0;
         have_derivs = false;
@@ -1289,9 +1307,19 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
         {
             if (s != TAD_OK && s != TAD_ERR_PCG_NOCONV) return finish(s);
             const int choice = P.hs->ls_choice;
-            if (choice == -2)
+            if (stop_decrement > 0.0 && P.hs->decrement < stop_decrement)
+            {
+                // converged by the Newton decrement (d.g was reduced before the
+                // selection): the reference stops before line_search, so x keeps
+                // this iteration's start; the trial's derivatives and any error
+                // it reported are dropped
+                stopped = true;
+                if (*P.err_h != 0) TAD_CUDA_TRY(cudaMemsetAsync(P.err, 0, sizeof(int32_t), st));
+                fn = choice == 0 ? P.hs->f_prev : P.hs->f;   // an accepted trial moved ds->f on
+            }
+            else if (choice == -2)
                 return finish(fail(TAD_ERR_NONFINITE, "Assertion failed: f_new == f_new (NaN energy in line search)"));
-            if (choice == 0)
+            else if (choice == 0)
             {
                 // accepted: x + d is the new state, its derivatives are assembled
                 std::swap(cur, spare);
@@ -1312,18 +1340,23 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
         }
         else
         {
-            s = line_search_device(P, cur, P.dx, 0.0, 1.0, &found, &fn, &trials, true);
+            s = line_search_device(P, cur, P.dx, 0.0, 1.0, &found, &fn, &trials, true, 0, stop_decrement, &stopped);
             if (s != TAD_OK) return finish(s);
             speculate = found && trials == 1;
+        }
+        cudaEventRecord(ev(it, 4), st);
+        if (stopped)
+        {
+            // iterations done = steps taken; f_hist[it] is the final energy
+            f = fn;
+            break;
         }
         // the energy at the start of this iteration (ds->f, or what an accepted
         // speculative step replaced there)
         f = have_derivs ? P.hs->f_prev : P.hs->f;
         if (f_hist) f_hist[it] = f;
-        cudaEventRecord(ev(it, 4), st);
         P.ls_trials_total += trials;
         f = fn;
-        if (stop_decrement > 0.0 && P.hs->decrement < stop_decrement) { ++it; break; }
         if (!found) { ++it; break; }
     }
     if (f_hist) f_hist[it] = f;
@@ -1373,6 +1406,42 @@ TAD_API tad_status tad_newton_direction(tad_problem* P, const double* x_h, int p
     P->pcg_iters_total = it;
     if (ps == TAD_ERR_PCG_NOCONV) set_error("Linear solve did not reach its tolerance.");
     return ps;
+}
+
+/* newton_decrement(d, g) = -d.g / 2 (include/TinyAD/Utils/NewtonDecrement.hh:20-26),
+   as a fixed-order device reduction (k_dot_dg) on the problem's stream */
+static tad_status newton_decrement_dev(Problem& P, const double* d_d, const double* g_d, double* out)
+{
+    cudaStream_t s = P.stream;
+    k_dot_dg<<<RED_BLOCKS, RED_THREADS, 0, s>>>(P.n_vars, d_d, g_d, P.partials, P.counters + 4, P.ds);
+    P.n_launches += 1;
+    TAD_CUDA_TRY(cudaGetLastError());
+    TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
+    TAD_CUDA_TRY(cudaStreamSynchronize(s));
+    *out = P.hs->decrement;
+    return TAD_OK;
+}
+
+TAD_API tad_status tad_newton_decrement(tad_problem* P, const double* d_h, const double* g_h, double* out)
+{
+    if (!P || !d_h || !g_h || !out) return fail(TAD_ERR_ARG, "NULL argument");
+    TAD_CUDA_TRY(cudaSetDevice(P->device));
+    tad_status s = ensure_finalized(*P);
+    if (s != TAD_OK) return s;
+    const int64_t n = P->n_vars;
+    // staged in the problem's own direction and right-hand-side buffers
+    TAD_CUDA_TRY(cudaMemcpyAsync(P->dx, d_h, n * 8, cudaMemcpyHostToDevice, P->stream));
+    TAD_CUDA_TRY(cudaMemcpyAsync(P->rhs, g_h, n * 8, cudaMemcpyHostToDevice, P->stream));
+    return newton_decrement_dev(*P, P->dx, P->rhs, out);
+}
+
+TAD_API tad_status tad_newton_decrement_d(tad_problem* P, const double* d_d, const double* g_d, double* out)
+{
+    if (!P || !d_d || !g_d || !out) return fail(TAD_ERR_ARG, "NULL argument");
+    TAD_CUDA_TRY(cudaSetDevice(P->device));
+    tad_status s = ensure_finalized(*P);
+    if (s != TAD_OK) return s;
+    return newton_decrement_dev(*P, d_d, g_d, out);
 }
 
 TAD_API tad_status tad_line_search(tad_problem* P, const double* x_h, const double* d_h, double f, const double* g_h,
