@@ -95,24 +95,32 @@ struct DevScalars
     int32_t spec_ok;     // Newton: the PCG is done and x is the state the carried derivatives belong to
 };
 
-/* one level of the AMG hierarchy (amg.cu); level 0 borrows the problem's
-   pattern and values */
+/* one level of the smoothed-aggregation AMG hierarchy (amg.cu); level 0
+   borrows the problem's pattern and values.  Values and vectors are sized for
+   FP64 and used in the PCG's precision. */
 struct AmgLevel
 {
     int64_t n = 0, nb = 0;
-    int32_t *bptr = nullptr, *bcol = nullptr, *diag = nullptr;
-    int32_t *agg = nullptr;                  // rows of the level above -> rows here
-    int32_t *aptr = nullptr, *aidx = nullptr;
-    int32_t *cptr = nullptr, *cidx = nullptr;
-    void *A = nullptr, *dinv = nullptr;      // values / inverted diagonal blocks (PCG precision)
-    void *r = nullptr, *z = nullptr, *w = nullptr, *t = nullptr;
+    int32_t *bptr = nullptr, *bcol = nullptr, *diag = nullptr;   // this level's matrix
+    void* A = nullptr;                       // its values (level 0: the problem's H)
+    int64_t max_row = 0;                     // longest block row
+    void* dl1 = nullptr;                     // inverted l1 blocks (the smoother)
+    void *r = nullptr, *x = nullptr, *res = nullptr, *w = nullptr;   // V-cycle vectors (w: coarsest-level scratch)
+    // transfer to the next level (all but the coarsest)
+    int64_t nc = 0, np = 0, nq = 0;
+    int32_t *pptr = nullptr, *pcol = nullptr, *pslot = nullptr, *pdiag = nullptr;   // P pattern
+    int32_t *qptr = nullptr, *qcol = nullptr;                                     // Q = A P pattern
+    int32_t *qlptr = nullptr, *qla = nullptr, *qlp = nullptr;                      // per Q block: (A, P) products
+    int32_t *tptr = nullptr, *tu = nullptr, *tp = nullptr;                        // transposed P lists
+    double* cscale = nullptr;                // per aggregate 1 / sqrt(size)
+    void *Pv = nullptr, *Qv = nullptr;       // P and Q values
 };
 
 struct Problem
 {
-    std::vector<AmgLevel> amg;       // aggregation-AMG hierarchy, built when first needed
+    std::vector<AmgLevel> amg;       // smoothed-aggregation AMG hierarchy (pattern built at finalisation)
     int64_t amg_solves = 0;          // solves that used it (statistics)
-    double* amg_omega = nullptr;     // device: per-level smoother damping (+ 2 scratch norms)
+    bool amg_values_ready = false;   // values computed for the current H
 
     int kind = 0;                    // 0: empty, 1: scalar terms, 2: vector terms (sum of squares)
     int64_t n_outputs_total = 0;     // vector problems: residuals
@@ -256,8 +264,12 @@ void launch_zero(double* p, int64_t n, cudaStream_t s);
 
 // ---- solver.cu
 void add_identity(Problem& P, double w, int precision);   // H += w I (assembled H)
-tad_status amg_prepare(Problem& P, int precision);        // hierarchy (lazily) + values for the current H
-void amg_vcycle(Problem& P, int precision, const void* r, void* z);   // z = V-cycle(r) on P.stream
+tad_status amg_build(Problem& P);                         // the hierarchy's patterns (once per problem)
+tad_status amg_prepare(Problem& P, int precision);        // hierarchy (if not built) + values for the current H
+/* CG under the V-cycle, on P.stream: mode 0 restarts from the current (xs, r)
+   (z = V(r), p = Ap = 0, beta = 0); mode 1 is the step after the fused SpMV
+   (x += alpha p, r -= alpha Ap with the stop test, z = V(r), beta) */
+void amg_apply(Problem& P, int precision, int mode, void* xs, void* r, void* z, void* p, void* Ap);
 void amg_free(Problem& P);
 int amg_levels(const Problem& P);
 tad_status pcg_solve(Problem& P, const double* b, double* xsol, double w_identity, int precision,

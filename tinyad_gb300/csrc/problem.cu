@@ -281,6 +281,13 @@ tad_status ensure_finalized(Problem& P)
     TAD_CUDA_TRY(dalloc(&P.r32, n)); TAD_CUDA_TRY(dalloc(&P.z32, n)); TAD_CUDA_TRY(dalloc(&P.p32, n));
     TAD_CUDA_TRY(dalloc(&P.Ap32, n)); TAD_CUDA_TRY(dalloc(&P.dx32, n)); TAD_CUDA_TRY(dalloc(&P.dinv32, nh * dd));
     P.finalized = true;
+    // the AMG hierarchy's patterns (host work, once per problem) here rather
+    // than inside the first solve that needs them
+    if (P.settings.preconditioner == 1)
+    {
+        s = amg_build(P);
+        if (s != TAD_OK) return s;
+    }
     return TAD_OK;
 }
 

@@ -528,30 +528,25 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_rz(int64_t n, const T* __re
     }
 }
 
-/* Conjugate gradients preconditioned by one AMG V-cycle, from x = 0. */
+/* Conjugate gradients preconditioned by one smoothed-aggregation V-cycle
+   (amg.cu), restarted from the current iterate (xs, r) of a block-Jacobi
+   solve: its tolerance, iteration count and cap carry over. */
 template <int d, typename T>
-static tad_status pcg_core_amg(Problem& P, const double* b, T* xs, double rel_tol, int max_iters, int* iters_out,
-                               T* r, T* z, T* p, T* Ap, int prec)
+static tad_status pcg_core_amg(Problem& P, T* xs, int* iters_out, T* r, T* z, T* p, T* Ap, int prec)
 {
     tad_status st = amg_prepare(P, prec);
     if (st != TAD_OK) return st;
     ++P.amg_solves;
     const T* H = (const T*)P.H;
-    const int64_t nh = P.n_handles, n = P.n_vars;
+    const int64_t nh = P.n_handles;
     cudaStream_t s = P.stream;
-    // x = 0, r = b, p = Ap = 0, tolerance and counters (its z = D^-1 r is replaced)
-    k_pcg_init<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, b, xs, r, z, p, Ap, (T*)P.amg[0].dinv, nullptr, nullptr, 0.0,
-                                                        P.partials, P.counters, P.ds, rel_tol, max_iters);
-    amg_vcycle(P, prec, r, z);
-    k_pcg_rz<T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, r, z, P.partials, P.counters + 9, P.ds, 1);
-    P.n_launches += 2;
+    amg_apply(P, prec, 0, xs, r, z, p, Ap);
     TAD_CUDA_TRY(cudaGetLastError());
     constexpr int CHUNK = 4;
     auto launch_iteration = [&]() {
         launch_pcg_spmv<d, T>(s, nh, P.bptr, P.bcol, H, z, p, Ap, P.partials, P.counters + 1, P.ds);
-        k_pcg_update_nopc<T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, xs, r, p, Ap, P.partials, P.counters + 2, P.ds);
-        amg_vcycle(P, prec, r, z);
-        k_pcg_rz<T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, r, z, P.partials, P.counters + 9, P.ds, 0);
+        P.n_launches += 1;
+        amg_apply(P, prec, 1, xs, r, z, p, Ap);
     };
     if (P.amg_graph == nullptr || P.amg_graph_prec != prec || P.amg_graph_x != (const void*)xs || P.amg_graph_H != (const void*)H)
     {
@@ -566,7 +561,7 @@ static tad_status pcg_core_amg(Problem& P, const double* b, T* xs, double rel_to
         P.amg_graph_prec = prec;
         P.amg_graph_x = (const void*)xs;
         P.amg_graph_H = (const void*)H;
-        P.amg_graph_launches = P.n_launches - l0 + 3 * CHUNK;
+        P.amg_graph_launches = P.n_launches - l0;
         P.n_launches = l0;
     }
     int replays = 1;
@@ -581,22 +576,21 @@ static tad_status pcg_core_amg(Problem& P, const double* b, T* xs, double rel_to
         if (P.hs->done) break;
         if (sizeof(T) == 4)
         {
-            // FP32 V-cycles on a system that is nearly singular at FP32
-            // rounding level can stop reducing the residual: give up after
-            // two host checks without a 10 % reduction (the caller falls back)
+            // FP32 V-cycles on a system nearly singular at FP32 rounding
+            // level may stop reducing the residual: give up after two host
+            // checks without a 10 % reduction (the caller falls back)
             if (rr_last > 0.0 && !(P.hs->rr < 0.9 * rr_last)) ++slow;
             rr_last = P.hs->rr;
             if (slow >= 2)
             {
-                if (iters_out) *iters_out += P.hs->iters;
+                if (iters_out) *iters_out = P.hs->iters;
                 return TAD_ERR_PCG_NOCONV;
             }
         }
         replays = std::min(4, 2 * replays);
     }
-    if (iters_out) *iters_out += P.hs->iters;
-    if (P.hs->breakdown) return TAD_ERR_PCG_NOCONV;
-    if (!(P.hs->rr <= P.hs->tol2)) return TAD_ERR_PCG_NOCONV;
+    if (iters_out) *iters_out = P.hs->iters;
+    if (P.hs->breakdown || !(P.hs->rr <= P.hs->tol2)) return TAD_ERR_PCG_NOCONV;
     return TAD_OK;
 }
 
@@ -622,23 +616,15 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
     // The first iteration is launched directly and checked at once (early
     // Newton iterations converge in one); after that, CHUNK iterations
     // captured once per (precision, solution buffer) are replayed, with the
-    // replays between host checks doubling up to 8.  With the AMG policy,
-    // a solve that after the first 1 + CHUNK iterations is still far from its
-    // tolerance, or whose block-Jacobi rate predicts more than
-    // AMG_SWITCH_ITERS further iterations, restarts with the
-    // AMG-preconditioned CG (w must be 0 there: the hierarchy is built from H
-    // itself).  An FP32 solve (mixed precision)
-    // whose V-cycles break down or stall -- FP32 V-cycles on systems nearly
-    // singular at FP32 rounding level (the eps-regularised rigid motions of
-    // an unconstrained mesh) do not converge reliably -- falls back to block
-    // Jacobi alone, from zero.
+    // replays between host checks doubling up to 8.  With the AMG policy
+    // (preconditioner 1, w = 0: the hierarchy is built from H itself), a
+    // solve that has not met its tolerance after the first 1 + CHUNK
+    // iterations continues from its iterate under the smoothed-aggregation
+    // V-cycle: block Jacobi has removed the high frequencies by then, and
+    // what is left takes it hundreds of iterations on large meshes (the
+    // V-cycle: 10-20).  An FP32 solve (mixed precision) whose V-cycles break
+    // down or stall falls back to block Jacobi alone, from zero.
     constexpr int CHUNK = 8;
-    constexpr double AMG_SWITCH_RATIO = 16.0;
-    // an AMG iteration costs ~4 block-Jacobi ones plus the hierarchy's values
-    // (measured on the 1.64M-face disk: 0.26 vs 0.06 ms); switching pays when
-    // block Jacobi still needs more than this many iterations
-    constexpr double AMG_SWITCH_ITERS = 64.0;
-    double rr_first = 0.0;
     auto launch_iteration = [&]() {
         launch_pcg_spmv<d, T>(s, nh, P.bptr, P.bcol, H, z, p, Ap, P.partials, P.counters + 1, P.ds);
         k_pcg_update<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, xs, r, z, p, Ap, dinv, P.partials, P.counters + 2, P.ds);
@@ -682,29 +668,14 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
             TAD_CUDA_TRY(cudaStreamSynchronize(s));
         }
         if (P.hs->done) break;
-        if (replays == 0) rr_first = P.hs->rr;
-        bool slow = false;
-        if (replays == 1)
-        {
-            // the residual rate over iterations 1 .. 1 + CHUNK predicts how many
-            // more block-Jacobi iterations the target needs
-            const double rr = P.hs->rr, tol2 = P.hs->tol2;
-            if (rr > AMG_SWITCH_RATIO * tol2) slow = true;
-            else if (rr > tol2 && rr_first > rr && tol2 > 0.0)
-                slow = CHUNK * std::log(rr / tol2) / std::log(rr_first / rr) > AMG_SWITCH_ITERS;
-            else if (rr > tol2) slow = true;   // no progress over the chunk
-        }
+        const bool slow = replays == 1;   // not done after 1 + CHUNK iterations
         if (allow_amg && slow && P.settings.preconditioner == 1 && w == 0.0)
         {
-            // block Jacobi's fast start (the high frequencies) is over, and what
-            // is left would take more than AMG_SWITCH_ITERS iterations at the
-            // observed rate (or the residual is still more than a factor
-            // sqrt(AMG_SWITCH_RATIO) above the target): restart with AMG
-            const int it = P.hs->iters;
-            if (iters_out) *iters_out = it;
-            const int left = std::max(1, max_iters - it);
-            const tad_status sa = pcg_core_amg<d, T>(P, b, xs, rel_tol, left, iters_out, r, z, p, Ap, prec);
+            // block Jacobi's fast start (the high frequencies) is over and the
+            // tolerance is not met: continue from this iterate under the V-cycle
+            const tad_status sa = pcg_core_amg<d, T>(P, xs, iters_out, r, z, p, Ap, prec);
             if (sizeof(T) == 8 || sa == TAD_OK) return sa;
+            if (P.hs->breakdown == 0 && P.hs->done) return sa;   // the iteration cap
             // FP32: the V-cycle broke down or stalled (a system nearly singular
             // at FP32 rounding level, e.g. the rigid motions of an
             // unconstrained mesh): block Jacobi alone, from zero
