@@ -272,6 +272,7 @@ tad_status amg_prepare(Problem& P, int precision);        // hierarchy (if not b
 void amg_apply(Problem& P, int precision, int mode, void* xs, void* r, void* z, void* p, void* Ap);
 void amg_free(Problem& P);
 int amg_levels(const Problem& P);
+tad_status prepare_solver_graphs(Problem& P);              // capture the Newton loop's PCG graphs (finalisation)
 tad_status pcg_solve(Problem& P, const double* b, double* xsol, double w_identity, int precision,
                      double rel_tol, int max_iters, int* iters_out);
 /* f_on_device: the energy at x is already in ds->f (f is then ignored);

@@ -288,7 +288,8 @@ tad_status ensure_finalized(Problem& P)
         s = amg_build(P);
         if (s != TAD_OK) return s;
     }
-    return TAD_OK;
+    // and the Newton loop's captured PCG iteration graphs
+    return prepare_solver_graphs(P);
 }
 
 /* ------------------------------------------------------------------------ */

@@ -528,6 +528,70 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_rz(int64_t n, const T* __re
     }
 }
 
+constexpr int PCG_CHUNK = 8;   // block-Jacobi iterations per captured graph
+constexpr int AMG_CHUNK = 4;   // V-cycle-preconditioned iterations per captured graph
+
+/* The chunk of PCG_CHUNK block-Jacobi iterations as a CUDA graph, captured
+   once per (precision, solution buffer, Hessian buffer) and replayed. */
+template <int d, typename T>
+static tad_status ensure_pcg_graph(Problem& P, T* xs, T* r, T* z, T* p, T* Ap, T* dinv, int prec)
+{
+    const T* H = (const T*)P.H;
+    if (P.pcg_graph && P.pcg_graph_prec == prec && P.pcg_graph_chunk == PCG_CHUNK && P.pcg_graph_x == (const void*)xs &&
+        P.pcg_graph_H == (const void*)H)
+        return TAD_OK;
+    if (P.pcg_graph) { cudaGraphExecDestroy(P.pcg_graph); P.pcg_graph = nullptr; }
+    cudaStream_t s = P.stream;
+    const int64_t nh = P.n_handles;
+    cudaGraph_t graph;
+    TAD_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    for (int it = 0; it < PCG_CHUNK; ++it)
+    {
+        launch_pcg_spmv<d, T>(s, nh, P.bptr, P.bcol, H, z, p, Ap, P.partials, P.counters + 1, P.ds);
+        k_pcg_update<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, xs, r, z, p, Ap, dinv, P.partials, P.counters + 2, P.ds);
+    }
+    TAD_CUDA_TRY(cudaStreamEndCapture(s, &graph));
+    TAD_CUDA_TRY(cudaGraphInstantiate(&P.pcg_graph, graph, 0));
+    cudaGraphDestroy(graph);
+    P.pcg_graph_prec = prec;
+    P.pcg_graph_chunk = PCG_CHUNK;
+    P.pcg_graph_x = (const void*)xs;
+    P.pcg_graph_H = (const void*)H;
+    return TAD_OK;
+}
+
+/* The chunk of AMG_CHUNK V-cycle-preconditioned CG iterations (fused SpMV,
+   then update + V-cycle) as a CUDA graph, captured like ensure_pcg_graph. */
+template <int d, typename T>
+static tad_status ensure_amg_graph(Problem& P, T* xs, T* r, T* z, T* p, T* Ap, int prec)
+{
+    const T* H = (const T*)P.H;
+    if (P.amg_graph && P.amg_graph_prec == prec && P.amg_graph_x == (const void*)xs && P.amg_graph_H == (const void*)H)
+        return TAD_OK;
+    tad_status st = amg_build(P);
+    if (st != TAD_OK) return st;
+    if (P.amg_graph) { cudaGraphExecDestroy(P.amg_graph); P.amg_graph = nullptr; }
+    cudaStream_t s = P.stream;
+    const int64_t l0 = P.n_launches;
+    cudaGraph_t graph;
+    TAD_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    for (int it = 0; it < AMG_CHUNK; ++it)
+    {
+        launch_pcg_spmv<d, T>(s, P.n_handles, P.bptr, P.bcol, H, z, p, Ap, P.partials, P.counters + 1, P.ds);
+        P.n_launches += 1;
+        amg_apply(P, prec, 1, xs, r, z, p, Ap);
+    }
+    TAD_CUDA_TRY(cudaStreamEndCapture(s, &graph));
+    TAD_CUDA_TRY(cudaGraphInstantiate(&P.amg_graph, graph, 0));
+    cudaGraphDestroy(graph);
+    P.amg_graph_prec = prec;
+    P.amg_graph_x = (const void*)xs;
+    P.amg_graph_H = (const void*)H;
+    P.amg_graph_launches = P.n_launches - l0;
+    P.n_launches = l0;
+    return TAD_OK;
+}
+
 /* Conjugate gradients preconditioned by one smoothed-aggregation V-cycle
    (amg.cu), restarted from the current iterate (xs, r) of a block-Jacobi
    solve: its tolerance, iteration count and cap carry over. */
@@ -542,28 +606,8 @@ static tad_status pcg_core_amg(Problem& P, T* xs, int* iters_out, T* r, T* z, T*
     cudaStream_t s = P.stream;
     amg_apply(P, prec, 0, xs, r, z, p, Ap);
     TAD_CUDA_TRY(cudaGetLastError());
-    constexpr int CHUNK = 4;
-    auto launch_iteration = [&]() {
-        launch_pcg_spmv<d, T>(s, nh, P.bptr, P.bcol, H, z, p, Ap, P.partials, P.counters + 1, P.ds);
-        P.n_launches += 1;
-        amg_apply(P, prec, 1, xs, r, z, p, Ap);
-    };
-    if (P.amg_graph == nullptr || P.amg_graph_prec != prec || P.amg_graph_x != (const void*)xs || P.amg_graph_H != (const void*)H)
-    {
-        if (P.amg_graph) { cudaGraphExecDestroy(P.amg_graph); P.amg_graph = nullptr; }
-        const int64_t l0 = P.n_launches;
-        cudaGraph_t graph;
-        TAD_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        for (int it = 0; it < CHUNK; ++it) launch_iteration();
-        TAD_CUDA_TRY(cudaStreamEndCapture(s, &graph));
-        TAD_CUDA_TRY(cudaGraphInstantiate(&P.amg_graph, graph, 0));
-        cudaGraphDestroy(graph);
-        P.amg_graph_prec = prec;
-        P.amg_graph_x = (const void*)xs;
-        P.amg_graph_H = (const void*)H;
-        P.amg_graph_launches = P.n_launches - l0;
-        P.n_launches = l0;
-    }
+    st = ensure_amg_graph<d, T>(P, xs, r, z, p, Ap, prec);
+    if (st != TAD_OK) return st;
     int replays = 1;
     double rr_last = 0.0;
     int slow = 0;
@@ -614,17 +658,16 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
         TAD_CUDA_TRY(cudaGetLastError());
     }
     // The first iteration is launched directly and checked at once (early
-    // Newton iterations converge in one); after that, CHUNK iterations
+    // Newton iterations converge in one); after that, PCG_CHUNK iterations
     // captured once per (precision, solution buffer) are replayed, with the
     // replays between host checks doubling up to 8.  With the AMG policy
     // (preconditioner 1, w = 0: the hierarchy is built from H itself), a
-    // solve that has not met its tolerance after the first 1 + CHUNK
+    // solve that has not met its tolerance after the first 1 + PCG_CHUNK
     // iterations continues from its iterate under the smoothed-aggregation
     // V-cycle: block Jacobi has removed the high frequencies by then, and
     // what is left takes it hundreds of iterations on large meshes (the
     // V-cycle: 10-20).  An FP32 solve (mixed precision) whose V-cycles break
     // down or stall falls back to block Jacobi alone, from zero.
-    constexpr int CHUNK = 8;
     auto launch_iteration = [&]() {
         launch_pcg_spmv<d, T>(s, nh, P.bptr, P.bcol, H, z, p, Ap, P.partials, P.counters + 1, P.ds);
         k_pcg_update<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, xs, r, z, p, Ap, dinv, P.partials, P.counters + 2, P.ds);
@@ -644,23 +687,10 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
         }
         else
         {
-            if (P.pcg_graph == nullptr || P.pcg_graph_prec != prec || P.pcg_graph_chunk != CHUNK || P.pcg_graph_x != (const void*)xs ||
-                P.pcg_graph_H != (const void*)H)
-            {
-                if (P.pcg_graph) { cudaGraphExecDestroy(P.pcg_graph); P.pcg_graph = nullptr; }
-                cudaGraph_t graph;
-                TAD_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-                for (int it = 0; it < CHUNK; ++it) launch_iteration();
-                TAD_CUDA_TRY(cudaStreamEndCapture(s, &graph));
-                TAD_CUDA_TRY(cudaGraphInstantiate(&P.pcg_graph, graph, 0));
-                cudaGraphDestroy(graph);
-                P.pcg_graph_prec = prec;
-                P.pcg_graph_chunk = CHUNK;
-                P.pcg_graph_x = (const void*)xs;
-                P.pcg_graph_H = (const void*)H;
-            }
+            const tad_status sg = ensure_pcg_graph<d, T>(P, xs, r, z, p, Ap, dinv, prec);
+            if (sg != TAD_OK) return sg;
             for (int k = 0; k < replays; ++k) TAD_CUDA_TRY(cudaGraphLaunch(P.pcg_graph, s));
-            P.n_launches += 2 * CHUNK * replays;
+            P.n_launches += 2 * PCG_CHUNK * replays;
         }
         if (!(resume && replays == 0))
         {
@@ -668,7 +698,7 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
             TAD_CUDA_TRY(cudaStreamSynchronize(s));
         }
         if (P.hs->done) break;
-        const bool slow = replays == 1;   // not done after 1 + CHUNK iterations
+        const bool slow = replays == 1;   // not done after 1 + PCG_CHUNK iterations
         if (allow_amg && slow && P.settings.preconditioner == 1 && w == 0.0)
         {
             // block Jacobi's fast start (the high frequencies) is over and the
@@ -812,6 +842,34 @@ static tad_status pcg_dispatch(Problem& P, const double* b, double* xsol, int pr
     if (iters) *iters = total;
     if (!(P.hs->rr <= rel_tol * rel_tol * bb * 1.0001) && !(P.hs->rr <= tol * tol * bb)) return TAD_ERR_PCG_NOCONV;
     return st == TAD_ERR_PCG_NOCONV ? TAD_OK : st;
+}
+
+/* The captured iteration graphs of the Newton loop's solves (its solution and
+   vector buffers, the problem's precision), at finalisation, so that the
+   first solve needing them does not capture them */
+template <int d>
+static tad_status prepare_graphs_d(Problem& P)
+{
+    const bool amg = P.settings.preconditioner == 1 && !P.amg.empty();
+    if (P.precision == TAD_PREC_MIXED)
+    {
+        tad_status st = ensure_pcg_graph<d, float>(P, P.dx32, P.r32, P.z32, P.p32, P.Ap32, P.dinv32, 1);
+        if (st == TAD_OK && amg) st = ensure_amg_graph<d, float>(P, P.dx32, P.r32, P.z32, P.p32, P.Ap32, 1);
+        return st;
+    }
+    tad_status st = ensure_pcg_graph<d, double>(P, P.dx, P.r, P.z, P.p, P.Ap, P.dinv, 0);
+    if (st == TAD_OK && amg) st = ensure_amg_graph<d, double>(P, P.dx, P.r, P.z, P.p, P.Ap, 0);
+    return st;
+}
+
+tad_status prepare_solver_graphs(Problem& P)
+{
+    switch (P.d)
+    {
+    case 1: return prepare_graphs_d<1>(P);
+    case 2: return prepare_graphs_d<2>(P);
+    default: return prepare_graphs_d<3>(P);
+    }
 }
 
 /* H += w I on the assembled diagonal blocks */
