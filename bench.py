@@ -609,6 +609,9 @@ def main():
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         clk.mark()
+        # the timed region is also the profiler range (a no-op unless a
+        # profiler started with --profile-from-start off is attached)
+        torch.cuda.profiler.start()
         e0.record(stream)
         # the K iterations as one solver call, as a Newton solve runs them
         fh = fn.newton_solve_device(x.data_ptr(), args.steps)
@@ -617,6 +620,7 @@ def main():
         for k in stage:
             stage[k] += st[k]
         torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
         clk.unmark()
         ms = e0.elapsed_time(e1)
         launches = fn.launch_count - launches0
