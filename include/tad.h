@@ -381,8 +381,9 @@ TAD_API tad_status tad_batch_newton_solve(tad_batch* b, double* x_h, int n_iters
                                           double* f_hist_h);
 TAD_API tad_status tad_batch_newton_solve_d(tad_batch* b, double* x_d, int n_iters, double proj_eps,
                                             double* f_hist_h);
-/* times candidate (block rows per chunk, threads per block) pairs on the
-   batch at x_d and keeps the fastest; best3 = [rows, threads, ms] */
+/* times candidate (block rows per chunk, threads per block, blocks per SM
+   of the persistent PCG) triples on the batch at x_d and keeps the fastest;
+   best3 = [rows, threads, ms] */
 TAD_API tad_status tad_batch_autotune(tad_batch* b, const double* x_d, double proj_eps, double* best3);
 /* sets the chunking directly: chunk_rows block rows per PCG chunk (4x as many
    elements per element chunk), threads per block; the next solve recaptures */

@@ -85,3 +85,45 @@ def test_batch_mesh_without_elements(tad, oracle):
         p = oracle.Problem.from_workload(w)
         _, fho, _ = p.newton(w.x0, 40)
         assert abs(p.eval(xs[m]) - fho[-1]) <= 1e-8 * abs(fho[-1]), (m, p.eval(xs[m]), fho[-1])
+
+
+def test_batch_history_is_each_iterates_energy(tad, oracle):
+    """The per-iteration energies the batch reports (the history: f_start
+    and the adopted trial energies) are the energies of the batch's own
+    iterates, iteration by iteration, including iterations where one mesh
+    rejects its full Newton step while the others take theirs: the middle
+    mesh starts stretched eight times along v, and its first full steps are
+    rejected (checked on the single-problem loop's trial counts).  Each
+    mesh's history also follows the single-problem loop with the same
+    algorithm (block-Jacobi PCG, 16 Armijo trials) to within the effect of
+    the inexact (1e-6) solves, which sum in different orders.  The meshes
+    have two pinned boundary vertices, so the solves are well posed (on an
+    unconstrained disk the rotation a tight solve leaves in the step depends
+    on the summation order)."""
+    base = [meshes.disk_param_pinned(g, seed=100 + i) for i, g in enumerate((8, 14, 20))]
+    w1 = base[1]
+    x_str = (w1.x0.reshape(-1, 2) * np.array([1.0, 8.0])).ravel()
+    ws = [base[0], meshes.Workload(name="stretched", var_dim=2, n_handles=w1.n_handles, x0=x_str, terms=w1.terms),
+          base[2]]
+    settings = dict(precision=0, pcg_rel_tol=1e-6, pcg_max_iters=2000)
+    b = tad.Batch(ws, **settings)
+    _, fh = b.newton_solve(b.x0(), 6)
+    ps = [oracle.Problem.from_workload(w) for w in ws]
+    for k in range(1, 7):
+        xk, fk = b.newton_solve(b.x0(), k)      # the same trajectory, stopped after k iterations
+        assert np.array_equal(fk, fh[:k + 1])
+        for m, xm in enumerate(b.split(xk)):
+            e = ps[m].eval(xm)
+            assert abs(fh[k, m] - e) <= 1e-12 * abs(e), (k, m, fh[k, m], e)
+    rejected = 0
+    for m, w in enumerate(ws):
+        fn = tad.ScalarFunction.from_workload(w, preconditioner=0, ls_max_iters=16, **settings)
+        x = w.x0.copy()
+        hist = [fn.eval(x)]
+        for _ in range(6):
+            x, f1 = fn.newton_solve(x, 1)
+            if m == 1 and fn.last_solve_stats()["ls_trials"] > 1:
+                rejected += 1
+            hist.append(float(f1[-1]))
+        assert np.allclose(fh[:, m], hist, rtol=1e-5, atol=0.0), (m, fh[:, m], hist)
+    assert rejected >= 1

@@ -13,21 +13,18 @@
  * of block rows (or elements) that each belong to one mesh.  A kernel walks
  * the chunk list with a fixed grid (grid-stride over chunks); the last
  * chunk of a mesh to finish sums that mesh's chunk partials in chunk order,
- * so every per-mesh reduction is deterministic.  The PCG kernels use a chunk
- * list rebuilt on the device from the meshes still iterating (at PCG
- * iterations 0-4, 6, 8, 12, 16, ...), cut so that the remaining rows spread
- * over the whole grid, one block per chunk.
+ * so every per-mesh reduction is deterministic.
  *
  * One Newton iteration (elements -> f -> assembly, only when some mesh did
- * not take the previous full step -> PCG with a fixed number of iterations,
- * each mesh stopping at its own tolerance -> the full step, evaluated by the
+ * not take the previous full step -> PCG, each mesh stopping at its own
+ * tolerance, all iterations in one persistent launch whose chunk list
+ * follows the meshes still iterating -> the full step, evaluated by the
  * element kernels and assembly at x + d, which are the next iteration's
  * derivatives -> batches of 8 and 7 energy-only trials while some mesh has
  * not accepted one -> per-mesh step) has a fixed launch sequence and is
  * captured once as a CUDA graph; the host replays one graph per iteration.
- * Kernels of the PCG iterations after every mesh has converged, and of the
- * trials after every mesh has accepted a step, return at once (device
- * counters).
+ * Trial kernels after every mesh has accepted a step return at once (a
+ * device counter).
  * A small autotuner times candidate chunk sizes / block sizes on the batch
  * itself and keeps the fastest.
  */
@@ -63,13 +60,13 @@ struct BatchScalars
     int32_t* choice;  // [m] accepted trial, -1 none, -3 none and stalled in this iteration
     double* step;     // [m]
     int32_t* searching;   // meshes without an accepted trial after the last selection
-    int32_t* pcg_active;  // [2] meshes still iterating after the last two PCG updates (ping-pong)
     int32_t* stalled;     // [m] no trial step passed the Armijo test: x stays, and so would every later
                           // iteration's result; the mesh is left out of the PCG and the line search
                           // until the next solve call
     int32_t* need_eval;   // meshes that rejected the full step in the last iteration (0: the
                           // derivatives assembled at x + d are those of every mesh's new x)
     double* f_start;      // [m] energy at the start of the last iteration (the history)
+    double* pap;          // [m] p.Ap of the persistent PCG's last SpMV phase
 };
 
 constexpr int LS_TRIALS = 16;
@@ -183,17 +180,7 @@ __global__ void k_b_dot(const Chunk* ch, int n_chunks, const int32_t* mcb, const
     }
 }
 
-/* The PCG kernels' chunk list, rebuilt on the device from the meshes still
-   iterating: their rows are cut into chunks of C = max(min_rows,
-   ceil(R / (2 G))) rows for R active rows and a grid of G blocks, so the
-   remaining work spreads over the whole grid however few meshes are left
-   (the last meshes to converge are the largest ones, whose rows would
-   otherwise sit in a few long chunks, one block each).  At most 2 G +
-   n_meshes chunks.  One block; thread t owns a contiguous run of meshes,
-   and the chunk offsets are an exclusive scan of the per-thread counts.
-   active: skip the rebuild when no mesh is iterating (0). */
-constexpr int CHUNK_BUILD_THREADS = 1024;
-
+/* exclusive prefix sum over the block (one value per thread); total: the sum */
 template <typename V>
 __device__ __forceinline__ V block_exclusive_scan(V v, V* warp_tot, V& total)
 {
@@ -223,38 +210,6 @@ __device__ __forceinline__ V block_exclusive_scan(V v, V* warp_tot, V& total)
     total = warp_tot[nw - 1];
     __syncthreads();
     return before + inc - v;
-}
-
-__global__ void __launch_bounds__(CHUNK_BUILD_THREADS) k_b_pcg_chunks(int n_meshes, const int64_t* __restrict__ row_off,
-                                                                      const int32_t* __restrict__ done, int grid,
-                                                                      int min_rows, const int32_t* active, Chunk* ch,
-                                                                      int32_t* mcb, int32_t* mce, int32_t* n_ch)
-{
-    if (active && *active == 0) return;
-    __shared__ long long tot_ll[32];
-    __shared__ int tot_i[32];
-    const int per = (n_meshes + CHUNK_BUILD_THREADS - 1) / CHUNK_BUILD_THREADS;
-    const int m0 = min(n_meshes, (int)threadIdx.x * per), m1 = min(n_meshes, m0 + per);
-    long long rows = 0;
-    for (int m = m0; m < m1; ++m)
-        if (!done[m]) rows += row_off[m + 1] - row_off[m];
-    long long R;
-    (void)block_exclusive_scan<long long>(rows, tot_ll, R);
-    const long long C = max((long long)min_rows, (R + 2LL * grid - 1) / (2LL * grid));
-    int cnt = 0;
-    for (int m = m0; m < m1; ++m)
-        if (!done[m]) cnt += (int)((row_off[m + 1] - row_off[m] + C - 1) / C);
-    int total;
-    int off = block_exclusive_scan<int>(cnt, tot_i, total);
-    for (int m = m0; m < m1; ++m)
-    {
-        mcb[m] = off;
-        if (!done[m])
-            for (long long b = row_off[m]; b < row_off[m + 1]; b += C)
-                ch[off++] = Chunk{m, (int32_t)b, (int32_t)min((long long)row_off[m + 1], b + C)};
-        mce[m] = off;
-    }
-    if (threadIdx.x == 0) *n_ch = total;
 }
 
 /* per mesh: x = 0, r = b, z = D^-1 r with the diagonal blocks inverted here
@@ -303,94 +258,271 @@ __global__ void k_b_pcg_init(const Chunk* ch, int n_chunks, const int32_t* mcb, 
     }
 }
 
-/* per mesh still iterating: Ap = H z + beta Ap, p = z + beta p (H p_new =
-   H z + beta H p_old, as in the single-problem PCG), alpha = rz / p.Ap.
-   active: meshes still iterating after the previous update (0: every block
-   returns at once -- the rest of the iteration budget is idle) */
-template <int d, typename T>
-__global__ void k_b_spmv(const Chunk* ch, const int32_t* n_ch, int stride, const int32_t* mcb, const int32_t* mce,
-                         const int32_t* bptr, const int32_t* bcol, const T* H, const T* z, T* p, T* Ap, double* partials,
-                         unsigned* counters, BatchScalars S, const int32_t* active)
+/* ---- the PCG stage as one persistent launch ------------------------------
+   All PCG iterations of a batched Newton iteration run in one launch of a
+   grid that fits on the GPU at once (cooperative launch where the capture
+   allows it).  Each iteration is two phases separated by grid barriers:
+     SpMV    Ap = H z + beta Ap, p = z + beta p, p.Ap -> alpha (per mesh)
+     update  x += alpha p, r -= alpha Ap, z = D^-1 r, r.z and r.r -> beta,
+             the stop test (per mesh)
+   Every block derives the same chunk list from the meshes still iterating
+   at the start of the iteration (their rows cut into chunks of
+   C = max(min_rows, ceil(R / 4G)) rows), so the work of the remaining
+   meshes spreads over the whole grid without a rebuild kernel; blocks take
+   chunks from a per-phase counter, so the blocks that drew short chunks
+   take more (a static assignment left the grid waiting at the barriers
+   for its slowest blocks).  Per-mesh
+   sums: the last chunk of a mesh to finish adds that mesh's chunk partials
+   in chunk order (deterministic).  Rows move between blocks as meshes
+   finish; a phase reads what other SMs wrote in the phase before with
+   ordinary loads, ordered by the barrier: its waiting thread's GPU-scope
+   fence after the generation changes, then __syncthreads, as in a
+   cooperative grid synchronisation.  The barriers wait a bounded time: a wait
+   that gives up sets bit 8 of the device error word (TAD_ERR_TIMEOUT) and
+   every block leaves the loop at its next barrier. */
+constexpr int PB_THREADS = 256;                 // block size of the launch bound (8 blocks per SM: full occupancy); the launch uses the batch's
+                                                // threads per block and its pb_per_sm blocks per SM (autotuned)
+constexpr long long PB_SPIN_LIMIT = 1LL << 23;   // ~2-4 s of polling with __nanosleep(256)
+
+struct GridBarrier
 {
-    if (*active == 0) return;
-    const int n_chunks = *n_ch;
-    for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x)
+    unsigned* count;   // arrivals of the current barrier
+    unsigned* gen;     // barrier generation (on another 128-byte line than count: the
+                       // waiting blocks poll it while the others still arrive)
+    int32_t* err;      // the problem's device error word
+};
+
+/* all blocks of the grid; false if this or another block's wait gave up */
+__device__ __forceinline__ bool grid_barrier(const GridBarrier& gb)
+{
+    __shared__ int ok_s;
+    __syncthreads();
+    if (threadIdx.x == 0)
     {
-        const Chunk c = ch[ci];
-        if (S.done[c.mesh]) continue;
-        const T beta = from_double<T>(S.beta[c.mesh]);
-        T part = T(0);
-        for (int64_t u = c.begin + threadIdx.x; u < c.end; u += blockDim.x)
+        volatile unsigned* vgen = gb.gen;
+        const unsigned g = *vgen;
+        __threadfence();
+        int ok = 0;
+        if (atomicAdd(gb.count, 1u) == gridDim.x - 1)
         {
-            T y[d];
-            bsr_row_product<d, T>(bptr, bcol, H, z, u, y);
-#pragma unroll
-            for (int i = 0; i < d; ++i)
+            *gb.count = 0u;
+            __threadfence();
+            atomicAdd(gb.gen, 1u);
+            ok = 1;
+        }
+        else
+        {
+            for (long long k = 0; k < PB_SPIN_LIMIT; ++k)
             {
-                const T apn = y[i] + beta * Ap[u * d + i];
-                const T pn = z[u * d + i] + beta * p[u * d + i];
-                Ap[u * d + i] = apn;
-                p[u * d + i] = pn;
-                part += pn * apn;
+                if (*vgen != g) { ok = 1; break; }
+                if (*(volatile int32_t*)gb.err & 8) break;
+                __nanosleep(256);
             }
+            if (!ok) atomicOr(gb.err, 8);
         }
-        double v[1] = {as_double(part)}, tot[1];
-        if (seg_finish<1>(ci, c.mesh, v, partials, stride, counters, mcb, mce, tot) && threadIdx.x == 0)
-        {
-            const int m = c.mesh;
-            if (!(tot[0] > 0.0) || !isfinite(tot[0])) { S.done[m] = 1; S.alpha[m] = 0.0; }
-            else S.alpha[m] = S.rz[m] / tot[0];
-        }
+        __threadfence();
+        ok_s = ok && !(*(volatile int32_t*)gb.err & 8);
     }
+    __syncthreads();
+    return ok_s != 0;
 }
 
-/* x += alpha p, r -= alpha Ap, z = D^-1 r; rz, rr and beta per mesh.  A mesh
-   that converged, reached max_iters or went non-finite is done; the others
-   are counted into active_out (zeroed before), which the next SpMV and
-   update read as their active_in */
-template <int d, typename T>
-__global__ void k_b_update(const Chunk* ch, const int32_t* n_ch, int stride, const int32_t* mcb, const int32_t* mce,
-                           T* x, T* r, T* z, const T* p, const T* Ap, const T* dinv, double* partials, unsigned* counters,
-                           BatchScalars S, int max_iters, const int32_t* active_in, int32_t* active_out)
+/* the chunk list of the meshes still iterating, in shared memory: start[m]
+   = first chunk of mesh m (start[n_meshes] = total), chunk size C */
+__device__ __forceinline__ void pb_chunk_list(int n_meshes, const int64_t* __restrict__ row_off, const int32_t* done,
+                                              int min_rows, int32_t* start, long long& C_out)
 {
-    if (*active_in == 0) return;
-    const int n_chunks = *n_ch;
-    for (int ci = blockIdx.x; ci < n_chunks; ci += gridDim.x)
+    __shared__ long long red_ll[32];
+    __shared__ int red_i[32];
+    __shared__ long long C_s;
+    const int per = (n_meshes + blockDim.x - 1) / blockDim.x;
+    const int m0 = min(n_meshes, (int)threadIdx.x * per), m1 = min(n_meshes, m0 + per);
+    long long rows = 0;
+    for (int m = m0; m < m1; ++m)
+        if (!*(volatile const int32_t*)&done[m]) rows += row_off[m + 1] - row_off[m];
+    long long R;
+    (void)block_exclusive_scan<long long>(rows, red_ll, R);
+    if (threadIdx.x == 0) C_s = max((long long)min_rows, (R + 4LL * gridDim.x - 1) / (4LL * gridDim.x));
+    __syncthreads();
+    const long long C = C_s;
+    int cnt = 0;
+    for (int m = m0; m < m1; ++m)
+        if (!*(volatile const int32_t*)&done[m]) cnt += (int)((row_off[m + 1] - row_off[m] + C - 1) / C);
+    int total;
+    int off = block_exclusive_scan<int>(cnt, red_i, total);
+    for (int m = m0; m < m1; ++m)
     {
-        const Chunk c = ch[ci];
-        if (S.done[c.mesh]) continue;
-        const T alpha = from_double<T>(S.alpha[c.mesh]);
-        T acc_rz = T(0), acc_rr = T(0);
-        for (int64_t u = c.begin + threadIdx.x; u < c.end; u += blockDim.x)
+        start[m] = off;
+        if (!*(volatile const int32_t*)&done[m]) off += (int)((row_off[m + 1] - row_off[m] + C - 1) / C);
+    }
+    if (threadIdx.x == 0) start[n_meshes] = total;
+    __syncthreads();
+    C_out = C;
+}
+
+/* mesh of chunk c: the last m with start[m] <= c (meshes without chunks have start[m] == start[m+1]) */
+__device__ __forceinline__ int pb_mesh_of(const int32_t* start, int n_meshes, int c)
+{
+    int lo = 0, hi = n_meshes;   // start[lo] <= c < start[hi]
+    while (hi - lo > 1)
+    {
+        const int mid = (lo + hi) >> 1;
+        if (start[mid] <= c) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+/* the block's share of one per-mesh sum: NV block partials into partials[i * stride + c]; the last
+   chunk of mesh m to arrive (cnt chunks) sums them in chunk order into tot (all threads) */
+template <int NV>
+__device__ __forceinline__ bool pb_finish(int c, int c0, int cnt, int m, double (&v)[NV], double* partials, int stride,
+                                          unsigned* counters, double (&tot)[NV])
+{
+    __shared__ double sh[NV][32];
+    __shared__ bool last;
+    __shared__ double res[NV];
+    bblock_sum<NV>(v, sh);
+    if (threadIdx.x == 0)
+    {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) partials[(int64_t)i * stride + c] = v[i];
+        __threadfence();
+        last = atomicAdd(&counters[m], 1u) == (unsigned)cnt - 1;
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double s2[NV];
+#pragma unroll
+    for (int i = 0; i < NV; ++i)
+    {
+        s2[i] = 0.0;
+        for (int k = c0 + threadIdx.x; k < c0 + cnt; k += blockDim.x) s2[i] += __ldcg(&partials[(int64_t)i * stride + k]);
+    }
+    bblock_sum<NV>(s2, sh);
+    if (threadIdx.x == 0)
+    {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) res[i] = s2[i];
+        counters[m] = 0u;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NV; ++i) tot[i] = res[i];
+    return true;
+}
+
+/* the block's next chunk of the phase whose counter is ctr (all threads) */
+__device__ __forceinline__ int pb_next_chunk(unsigned* ctr)
+{
+    __shared__ int c_s;
+    __syncthreads();   // the previous chunk's readers of c_s are done
+    if (threadIdx.x == 0) c_s = (int)atomicAdd(ctr, 1u);
+    __syncthreads();
+    return c_s;
+}
+
+template <int d, typename T>
+__global__ void __launch_bounds__(PB_THREADS, sizeof(T) == 4 ? 8 : 4) k_b_pcg_persistent(int n_meshes, const int64_t* __restrict__ row_off,
+                                                                 int min_rows, const int32_t* __restrict__ bptr,
+                                                                 const int32_t* __restrict__ bcol, const T* __restrict__ H,
+                                                                 T* x, T* r, T* z, T* p, T* Ap, const T* __restrict__ dinv,
+                                                                 double* partials, int stride, unsigned* counters,
+                                                                 BatchScalars S, int max_iters, GridBarrier gb,
+                                                                 unsigned* work)
+{
+    // work[4]: chunk counters of the two phases of even and odd iterations;
+    // zero at launch; those of the next iteration are cleared during the
+    // update phase (their last users finished before the previous barrier)
+    extern __shared__ int32_t start[];   // n_meshes + 1
+    for (int it = 0; it < max_iters; ++it)
+    {
+        long long C;
+        pb_chunk_list(n_meshes, row_off, S.done, min_rows, start, C);
+        const int n_chunks = start[n_meshes];
+        if (n_chunks == 0) break;   // every mesh is done (the same decision in every block)
+        unsigned* ctr = work + 2 * (it & 1);
+        // SpMV phase
+        for (int c = pb_next_chunk(ctr); c < n_chunks; c = pb_next_chunk(ctr))
         {
-            T rv[d], zv[d];
-#pragma unroll
-            for (int i = 0; i < d; ++i)
+            const int m = pb_mesh_of(start, n_meshes, c);
+            const int c0 = start[m], cnt = start[m + 1] - c0;
+            const int64_t b0 = row_off[m] + (int64_t)(c - c0) * C;
+            const int64_t b1 = min((long long)row_off[m + 1], (long long)(b0 + C));
+            const T beta = from_double<T>(S.beta[m]);
+            T part = T(0);
+            for (int64_t u = b0 + threadIdx.x; u < b1; u += blockDim.x)
             {
-                x[u * d + i] += alpha * p[u * d + i];
-                rv[i] = r[u * d + i] - alpha * Ap[u * d + i];
-                r[u * d + i] = rv[i];
+                T y[d];
+                bsr_row_product<d, T>(bptr, bcol, H, z, u, y);
+#pragma unroll
+                for (int i = 0; i < d; ++i)
+                {
+                    const T apn = y[i] + beta * Ap[u * d + i];
+                    const T pn = z[u * d + i] + beta * p[u * d + i];
+                    Ap[u * d + i] = apn;
+                    p[u * d + i] = pn;
+                    part += pn * apn;
+                }
             }
-            apply_dinv<d, T>(dinv, u, rv, zv);
-#pragma unroll
-            for (int i = 0; i < d; ++i)
+            // done flags change only in the update phase: blocks still building this
+            // iteration's chunk list read them, so a breakdown is recorded in pap and
+            // acted on by the update's finisher (alpha = 0 leaves x and r as they are)
+            double v[1] = {as_double(part)}, tot[1];
+            if (pb_finish<1>(c, c0, cnt, m, v, partials, stride, counters, tot) && threadIdx.x == 0)
             {
-                z[u * d + i] = zv[i];
-                acc_rz += rv[i] * zv[i];
-                acc_rr += rv[i] * rv[i];
+                S.pap[m] = tot[0];
+                S.alpha[m] = (tot[0] > 0.0 && isfinite(tot[0])) ? S.rz[m] / tot[0] : 0.0;
             }
         }
-        double v[2] = {as_double(acc_rz), as_double(acc_rr)}, tot[2];
-        if (seg_finish<2>(ci, c.mesh, v, partials, stride, counters, mcb, mce, tot) && threadIdx.x == 0)
+        if (!grid_barrier(gb)) return;
+        if (blockIdx.x == 0 && threadIdx.x == 0)
         {
-            const int m = c.mesh;
-            S.beta[m] = tot[0] / S.rz[m];
-            S.rz[m] = tot[0];
-            S.rr[m] = tot[1];
-            S.iters[m] += 1;
-            if (tot[1] <= S.tol2[m] || S.iters[m] >= max_iters || !isfinite(tot[1])) S.done[m] = 1;
-            else atomicAdd(active_out, 1);
+            work[2 * ((it + 1) & 1)] = 0u;
+            work[2 * ((it + 1) & 1) + 1] = 0u;
         }
+        // update phase
+        for (int c = pb_next_chunk(ctr + 1); c < n_chunks; c = pb_next_chunk(ctr + 1))
+        {
+            const int m = pb_mesh_of(start, n_meshes, c);
+            const int c0 = start[m], cnt = start[m + 1] - c0;
+            const int64_t b0 = row_off[m] + (int64_t)(c - c0) * C;
+            const int64_t b1 = min((long long)row_off[m + 1], (long long)(b0 + C));
+            const T alpha = from_double<T>(S.alpha[m]);
+            T acc_rz = T(0), acc_rr = T(0);
+            for (int64_t u = b0 + threadIdx.x; u < b1; u += blockDim.x)
+            {
+                T rv[d], zv[d];
+#pragma unroll
+                for (int i = 0; i < d; ++i)
+                {
+                    x[u * d + i] += alpha * p[u * d + i];
+                    rv[i] = r[u * d + i] - alpha * Ap[u * d + i];
+                    r[u * d + i] = rv[i];
+                }
+                apply_dinv<d, T>(dinv, u, rv, zv);
+#pragma unroll
+                for (int i = 0; i < d; ++i)
+                {
+                    z[u * d + i] = zv[i];
+                    acc_rz += rv[i] * zv[i];
+                    acc_rr += rv[i] * rv[i];
+                }
+            }
+            double v[2] = {as_double(acc_rz), as_double(acc_rr)}, tot[2];
+            if (pb_finish<2>(c, c0, cnt, m, v, partials, stride, counters, tot) && threadIdx.x == 0)
+            {
+                const double pap = S.pap[m];
+                if (!(pap > 0.0) || !isfinite(pap)) { S.done[m] = 1; continue; }   // non-positive curvature
+                S.beta[m] = tot[0] / S.rz[m];
+                S.rz[m] = tot[0];
+                S.rr[m] = tot[1];
+                S.iters[m] += 1;
+                if (tot[1] <= S.tol2[m] || S.iters[m] >= max_iters || !isfinite(tot[1])) S.done[m] = 1;
+            }
+        }
+        if (!grid_barrier(gb)) return;
     }
 }
 
@@ -470,12 +602,10 @@ struct Batch
     Chunk *vch = nullptr, *ech = nullptr;
     int n_vch = 0, n_ech = 0;
     int32_t *vmcb = nullptr, *vmce = nullptr, *emcb = nullptr, *emce = nullptr;
-    // PCG chunk list built on the device (k_b_pcg_chunks): capacity, list,
-    // per-mesh ranges, count; per-mesh row offsets
-    int pch_cap = 0;
-    Chunk* pch = nullptr;
-    int32_t *pmcb = nullptr, *pmce = nullptr, *n_pch = nullptr;
+    // per-mesh row offsets (the persistent PCG's chunk lists); chunk capacity
+    // of the persistent PCG (2 x its grid + n_meshes)
     int64_t* row_off = nullptr;
+    int pch_cap = 0;
     double* partials = nullptr;
     unsigned* counters = nullptr;   // [LS_TRIALS * 4096]
     double* scal = nullptr;
@@ -489,6 +619,10 @@ struct Batch
     double* xt = nullptr;           // x + d, where the full step's derivatives are evaluated
     int pcg_iters = 64;
     double pcg_tol = 1e-2;
+    int sms = 0;                    // the device's SM count
+    int pb_per_sm = 8;              // blocks per SM of the persistent PCG (at most what fits)
+    bool cooperative = false;       // cooperative launches can be captured (the persistent PCG's co-residency guarantee)
+    unsigned* bar = nullptr;        // [64]: grid-barrier arrival count [0], generation [32], chunk counters [48..51]
 };
 
 static std::vector<Chunk> make_chunks(const std::vector<int64_t>& off, int rows, std::vector<int32_t>& mcb, std::vector<int32_t>& mce)
@@ -549,30 +683,12 @@ static tad_status batch_setup_chunks(Batch& B)
     TAD_CUDA_TRY(upload(&B.vmce, vmce));
     TAD_CUDA_TRY(upload(&B.emcb, emcb));
     TAD_CUDA_TRY(upload(&B.emce, emce));
-    B.pch_cap = 2 * B.grid + B.n_meshes;
-    if (B.pch) { cudaFree(B.pch); B.pch = nullptr; }
-    TAD_CUDA_TRY(cudaMalloc(&B.pch, (size_t)B.pch_cap * sizeof(Chunk)));
-    if (!B.pmcb)
-    {
-        TAD_CUDA_TRY(cudaMalloc(&B.pmcb, (size_t)B.n_meshes * sizeof(int32_t)));
-        TAD_CUDA_TRY(cudaMalloc(&B.pmce, (size_t)B.n_meshes * sizeof(int32_t)));
-        TAD_CUDA_TRY(cudaMalloc(&B.n_pch, sizeof(int32_t)));
-        TAD_CUDA_TRY(upload(&B.row_off, B.vert_off));
-    }
+    B.pch_cap = 4 * B.sms * 16 + B.n_meshes;   // the persistent PCG's chunks: at most 4 per block + n_meshes
+    if (!B.row_off) TAD_CUDA_TRY(upload(&B.row_off, B.vert_off));
     if (B.partials) cudaFree(B.partials);
     const size_t n_part = std::max<size_t>((size_t)std::max(B.n_vch, B.n_ech) * LS_TRIALS, (size_t)B.pch_cap) * 2;
     TAD_CUDA_TRY(cudaMalloc(&B.partials, n_part * sizeof(double)));
     return TAD_OK;
-}
-
-/* PCG iterations before which the chunk list is rebuilt (0, 1, 2, 3, 4, 6,
-   8, 12, 16, 24, 32, 48, ...): between rebuilds the list is a superset of
-   the meshes still iterating, whose finished chunks are skipped */
-static bool rebuild_chunks_before(int it)
-{
-    if (it <= 4) return true;
-    const int q = it % 3 == 0 ? it / 3 : it;
-    return (q & (q - 1)) == 0;
 }
 
 /* record one batched Newton iteration on the problem's stream (captured) */
@@ -603,26 +719,36 @@ static tad_status record_iteration(Batch& B, int prec, double eps)
     P.launch_guard = nullptr;
     if (st != TAD_OK) return st;
     TAD_CUDA_TRY(cudaMemcpyAsync(B.S.f_start, B.S.f, (size_t)B.n_meshes * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    // 2. PCG, per-mesh tolerance.  Iteration it reads the active count the
-    // previous update left in pcg_active[it & 1] and counts into the other
-    // slot; the first count is set nonzero so the first iteration runs.
+    // 2. PCG, per-mesh tolerance: the init (per-mesh scalars, the inverted
+    // diagonal blocks), then every iteration in one persistent launch
     k_b_pcg_init<d, T><<<G, TH, 0, s>>>(B.vch, B.n_vch, B.vmcb, B.vmce, P.rhs, P.diag, H, xs, r, z, p, Ap, dinv,
                                         B.partials, B.counters, B.S, B.pcg_tol);
-    TAD_CUDA_TRY(cudaMemsetAsync(B.S.pcg_active, 1, sizeof(int32_t), s));
-    for (int it = 0; it < B.pcg_iters; ++it)
     {
-        const int32_t* in = B.S.pcg_active + (it & 1);
-        int32_t* out = B.S.pcg_active + ((it + 1) & 1);
-        if (rebuild_chunks_before(it))
-            k_b_pcg_chunks<<<1, CHUNK_BUILD_THREADS, 0, s>>>(B.n_meshes, B.row_off, B.S.done, G, TH, in, B.pch, B.pmcb,
-                                                             B.pmce, B.n_pch);
-        // one block per chunk slot (blocks past the list's length return at
-        // once): the block scheduler balances chunks of uneven length
-        k_b_spmv<d, T><<<B.pch_cap, TH, 0, s>>>(B.pch, B.n_pch, B.pch_cap, B.pmcb, B.pmce, P.bptr, P.bcol, H, z, p,
-                                                Ap, B.partials, B.counters, B.S, in);
-        TAD_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(int32_t), s));
-        k_b_update<d, T><<<B.pch_cap, TH, 0, s>>>(B.pch, B.n_pch, B.pch_cap, B.pmcb, B.pmce, xs, r, z, p, Ap, dinv,
-                                                  B.partials, B.counters, B.S, B.pcg_iters, in, out);
+        int per_sm = 0;
+        const size_t smem = (size_t)(B.n_meshes + 1) * sizeof(int32_t);
+        const int pth = std::min(TH, PB_THREADS);
+        TAD_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_b_pcg_persistent<d, T>, pth, smem));
+        const int Gp = std::max(1, B.sms * std::min(std::max(per_sm, 1), B.pb_per_sm));
+        GridBarrier gb{B.bar, B.bar + 32, P.err};
+        // a barrier count left over by a launch that gave up starts from zero
+        // again; the chunk counters (bar[48..51]) start at zero
+        TAD_CUDA_TRY(cudaMemsetAsync(B.bar, 0, sizeof(unsigned), s));
+        TAD_CUDA_TRY(cudaMemsetAsync(B.bar + 48, 0, 4 * sizeof(unsigned), s));
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)Gp);
+        cfg.blockDim = dim3(pth);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = s;
+        cudaLaunchAttribute attr;
+        attr.id = cudaLaunchAttributeCooperative;
+        attr.val.cooperative = 1;
+        cfg.attrs = &attr;
+        cfg.numAttrs = B.cooperative ? 1 : 0;
+        // chunk partials: at most 4 Gp + n_meshes chunks (two values each)
+        TAD_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_b_pcg_persistent<d, T>, B.n_meshes, (const int64_t*)B.row_off, pth,
+                                        (const int32_t*)P.bptr, (const int32_t*)P.bcol, (const T*)H, xs, r, z, p, Ap,
+                                        (const T*)dinv, B.partials, 4 * Gp + B.n_meshes, B.counters, B.S, B.pcg_iters, gb,
+                                        B.bar + 48));
     }
     k_b_to_double<T><<<G, TH, 0, s>>>(n, xs, P.dx);
     // 3. line search: d.g per mesh (with the g at x, before the full step's
@@ -718,7 +844,13 @@ TAD_API tad_status tad_batch_create(int var_dim, int n_meshes, const int64_t* n_
         if (n_handles[m] <= 0) { delete B; return batch_fail(TAD_ERR_ARG, "every mesh needs at least one handle"); }
         B->vert_off[m + 1] = B->vert_off[m] + n_handles[m];
     }
-    tad_status s = tad_problem_create(var_dim, B->vert_off[n_meshes], settings, &B->P);
+    // each mesh solves with block Jacobi (the batched PCG has no V-cycle), so the
+    // concatenated problem builds no AMG hierarchy
+    tad_settings st;
+    if (settings) st = *settings;
+    else tad_settings_default(&st);
+    st.preconditioner = 0;
+    tad_status s = tad_problem_create(var_dim, B->vert_off[n_meshes], &st, &B->P);
     if (s != TAD_OK) { delete B; return s; }
     *out = B;
     return TAD_OK;
@@ -746,6 +878,42 @@ TAD_API tad_status tad_batch_add_elements(tad_batch* B, int energy, int valence,
     return TAD_OK;
 }
 
+__global__ void k_b_noop() {}
+
+/* whether a cooperative launch can be recorded in a stream capture here (a
+   one-block no-op, captured on a private stream and instantiated) */
+static bool cooperative_capture_works()
+{
+    cudaStream_t st;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) { cudaGetLastError(); return false; }
+    bool ok = false;
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess)
+    {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(1);
+        cfg.blockDim = dim3(32);
+        cfg.stream = st;
+        cudaLaunchAttribute attr;
+        attr.id = cudaLaunchAttributeCooperative;
+        attr.val.cooperative = 1;
+        cfg.attrs = &attr;
+        cfg.numAttrs = 1;
+        const cudaError_t e1 = cudaLaunchKernelEx(&cfg, k_b_noop);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e2 = cudaStreamEndCapture(st, &g);
+        if (e1 == cudaSuccess && e2 == cudaSuccess && g)
+        {
+            cudaGraphExec_t ge = nullptr;
+            ok = cudaGraphInstantiate(&ge, g, 0) == cudaSuccess;
+            if (ge) cudaGraphExecDestroy(ge);
+        }
+        if (g) cudaGraphDestroy(g);
+    }
+    cudaGetLastError();
+    cudaStreamDestroy(st);
+    return ok;
+}
+
 static tad_status batch_prepare(tad_batch* B)
 {
     tad_status s = ensure_finalized(*B->P);
@@ -754,7 +922,11 @@ static tad_status batch_prepare(tad_batch* B)
     {
         int sms = 0;
         TAD_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, B->P->device));
-        B->grid = 4 * std::max(sms, 1);
+        B->sms = std::max(sms, 1);
+        B->grid = 4 * B->sms;
+        B->cooperative = cooperative_capture_works();
+        TAD_CUDA_TRY(cudaMalloc(&B->bar, 64 * sizeof(unsigned)));
+        TAD_CUDA_TRY(cudaMemset(B->bar, 0, 64 * sizeof(unsigned)));
         TAD_CUDA_TRY(cudaMalloc(&B->counters, (size_t)LS_TRIALS * 4096 * sizeof(unsigned)));
         TAD_CUDA_TRY(cudaMemset(B->counters, 0, (size_t)LS_TRIALS * 4096 * sizeof(unsigned)));
         const int nm = B->n_meshes;
@@ -775,11 +947,11 @@ static tad_status batch_prepare(tad_batch* B)
         B->S.rr = q; q += nm;
         B->S.step = q; q += nm;
         B->S.f_start = q; q += nm;
+        B->S.pap = q; q += nm;
         B->S.done = B->iscal;
         B->S.iters = B->iscal + nm;
         B->S.choice = B->iscal + 2 * nm;
         B->S.searching = B->iscal + 3 * nm;
-        B->S.pcg_active = B->iscal + 4 * nm;
         B->S.stalled = B->iscal + 4 * nm + 2;
         B->S.need_eval = B->iscal + 5 * nm + 2;
         TAD_CUDA_TRY(cudaMalloc(&B->steps, LS_TRIALS * sizeof(double)));
@@ -878,15 +1050,20 @@ TAD_API tad_status tad_batch_autotune(tad_batch* B, const double* x_d, double ep
     // the linear solves get harder as the meshes converge, and the first
     // iteration alone favours the launch shape of the easy solves
     constexpr int TUNE_ITERS = 3;
-    const int rows_c[] = {256, 512, 1024, 2048, 4096};
+    // element / vector chunk rows x threads per block x blocks per SM of the
+    // persistent PCG (the PCG's chunks follow the meshes still iterating)
+    const int rows_c[] = {512, 2048};
     const int thr_c[] = {128, 256};
+    const int pb_c[] = {4, 8, 16};
     double best = 1e30;
-    int br = B->chunk_rows, bt = B->threads;
+    int br = B->chunk_rows, bt = B->threads, bp = B->pb_per_sm;
     for (int rows : rows_c)
         for (int thr : thr_c)
+            for (int pb : pb_c)
         {
             B->chunk_rows = rows;
             B->threads = thr;
+            B->pb_per_sm = pb;
             s = batch_setup_chunks(*B);
             if (s != TAD_OK) return s;
             s = batch_capture(*B, eps);
@@ -905,10 +1082,11 @@ TAD_API tad_status tad_batch_autotune(tad_batch* B, const double* x_d, double ep
             TAD_CUDA_TRY(cudaEventSynchronize(P.ev[6]));
             cudaEventElapsedTime(&ms, P.ev[5], P.ev[6]);
             ms /= TUNE_ITERS;
-            if (ms < best) { best = ms; br = rows; bt = thr; }
+            if (ms < best) { best = ms; br = rows; bt = thr; bp = pb; }
         }
     B->chunk_rows = br;
     B->threads = bt;
+    B->pb_per_sm = bp;
     s = batch_setup_chunks(*B);
     if (s != TAD_OK) return s;
     s = batch_capture(*B, eps);
@@ -945,7 +1123,7 @@ TAD_API tad_status tad_batch_destroy(tad_batch* B)
     if (B->P) cudaStreamSynchronize(B->P->stream);
     if (B->graph) cudaGraphExecDestroy(B->graph);
     void* bufs[] = {B->vch, B->ech, B->vmcb, B->vmce, B->emcb, B->emce, B->partials, B->counters, B->scal, B->iscal,
-                    B->steps, B->x, B->xt, B->pch, B->pmcb, B->pmce, B->n_pch, B->row_off};
+                    B->steps, B->x, B->xt, B->row_off, B->bar};
     for (void* b : bufs) if (b) cudaFree(b);
     if (B->fh) cudaFreeHost(B->fh);
     tad_problem_destroy(B->P);
