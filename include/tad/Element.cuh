@@ -80,6 +80,60 @@ struct ActiveElement
 #endif
 };
 
+/* An ActiveElement whose scalar S carries only m = S::k of the element's
+   derivatives: variable j of the derivative numbering above (FirstPassive:
+   j = (slot - 1) * d + i) becomes local derivative p of S when idx[p] == j,
+   and enters as a constant otherwise.  S's Hessian is then the m x m
+   principal block of the element Hessian on the indices idx, and its
+   gradient those m gradient entries; lanes evaluating one element with
+   index sets that cover every index pair together obtain the whole Hessian
+   (k_elem_hess_lanes, ElementKernels.cuh).  Staged: the positions come from
+   xs (slot-major, d per recorded vertex, already in the passive type), which
+   the lanes of one element fill together -- the lane-split kernel stages
+   them relative to the first vertex (translation-invariant energies), so an
+   FP32 evaluation sees exact-rounded edge vectors. */
+template <int d, int N, typename S, bool FirstPassive = false, bool Staged = false>
+struct SubsetElement
+{
+    using scalar_type = S;
+    using passive_type = typename S::passive_type;
+    static constexpr bool active_mode = true;
+    int64_t handle;
+    int32_t vh[N];
+    int idx[S::k];
+    const double* x;
+    int32_t* err;
+    const passive_type* xs;
+
+#if defined(__CUDACC__)
+    __device__ Vec<S, d> variables(int v) const
+    {
+        int slot = -1;
+#pragma unroll
+        for (int i = N - 1; i >= 0; --i)
+            if (vh[i] == v) slot = i;
+        if (slot < 0) { report_error(err, DEVERR_UNRECORDED_ACCESS); slot = 0; }
+        Vec<S, d> r;
+#pragma unroll
+        for (int i = 0; i < d; ++i)
+        {
+            S s(Staged ? xs[slot * d + i] : (passive_type)x[(int64_t)d * v + i]);
+            const int j = (FirstPassive ? slot - 1 : slot) * d + i;
+#pragma unroll
+            for (int p = 0; p < S::k; ++p)
+                if (idx[p] == j) s.grad[p] = typename S::grad_type(1);
+            r[i] = s;
+        }
+        return r;
+    }
+    __device__ S variable(int v) const
+    {
+        static_assert(d == 1, "element.variable(vh) needs variable dimension 1; use element.variables(vh)");
+        return variables(v)[0];
+    }
+#endif
+};
+
 template <int d, int N, typename T>
 struct PassiveElement
 {

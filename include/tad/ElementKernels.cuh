@@ -378,6 +378,212 @@ __global__ void __launch_bounds__(128) k_project_general(const uint32_t* __restr
     }
 }
 
+/* ---------------------------------------------------------------------------
+ * Lane-split second-order evaluation, mixed precision, for translation-
+ * invariant energies with 9 reduced derivatives (d (N - 1) = 9: the
+ * tetrahedron, d = 3, N = 4).  The dense kernel above holds a Scalar<9> of
+ * 65 registers per live intermediate (FP64 value and gradient, 45-entry FP32
+ * Hessian); the symmetric Dirichlet tetrahedron keeps about twenty alive and
+ * spilled 5.7 KB a thread.  Here several lanes evaluate each element, each
+ * with a 3-derivative scalar (SubsetElement seeds its index triple):
+ *   k_elem_grad_lanes  3 lanes per element; lane s: Scalar<3> without
+ *                      Hessian, double-float value and gradient, on the
+ *                      reduced indices 3s .. 3s+2 -- the energy and the
+ *                      accurate gradient;
+ *   k_elem_hess_lanes  12 lanes per element; lane l: FP32 Scalar<3> on the
+ *                      l-th line of the affine plane of order 3 (points
+ *                      (u, c) <-> reduced index 3u + c; every pair of the 9
+ *                      indices lies on exactly one of its 12 lines, and the
+ *                      3 lines of direction 0 partition them), so the 12
+ *                      principal 3 x 3 blocks hold every Hessian entry once.
+ * The Hessian lanes evaluate in FP32 (the Hessian's precision), on vertex
+ * positions taken relative to the element's first vertex (exact-rounded
+ * edge vectors; the energy is translation invariant); the energy and
+ * gradient the Newton loop and the line search use come from the
+ * double-float lanes.  The blocks are assembled in shared memory, lifted to
+ * the first vertex (lift_translation_invariant's sums) and written as one
+ * coalesced range; the PSD projection is k_project_blocks (KnownInvariant).
+ * Measured on the 48^3 tetrahedral cube (663,552 tets), one projected
+ * evaluation: the dense kernel with its fused projection 6.65 ms; here the
+ * Hessian lanes 1.2 ms, the gradient lanes 1.1 ms and k_project_blocks
+ * 1.0 ms, 3.4 ms in all.  Staging the FP32 relative positions once per
+ * element (instead of an FP64 difference and conversion per coordinate and
+ * lane) took the Hessian lanes from 1.32 to 1.2 ms.
+ * ------------------------------------------------------------------------ */
+template <int d, int N, typename T, typename Energy> struct LaneHessian
+{
+    static constexpr bool value = std::is_same<T, float>::value && ReducedDerivatives<Energy, N>::value && d * (N - 1) == 9;
+};
+
+constexpr int GL_ELEMS = 32;   // elements per block of k_elem_grad_lanes (3 lanes each)
+constexpr int HL_ELEMS = 8;    // elements per block of k_elem_hess_lanes (12 lanes each)
+/* minimum resident blocks per SM of the two kernels */
+#ifndef TAD_GL_MINB
+#define TAD_GL_MINB 5
+#endif
+#ifndef TAD_HL_MINB
+#define TAD_HL_MINB 5
+#endif
+constexpr int GL_MIN_BLOCKS = TAD_GL_MINB;
+constexpr int HL_MIN_BLOCKS = TAD_HL_MINB;
+
+/* reduced index triple of line l (0..11) of the affine plane of order 3 */
+__device__ __forceinline__ void plane_line(int l, int (&t)[3])
+{
+    const int dir = l / 3, c = l % 3;
+    if (dir == 0) { t[0] = 3 * c; t[1] = 3 * c + 1; t[2] = 3 * c + 2; }
+    else
+    {
+        const int a = dir - 1;   // slope
+        t[0] = c;
+        t[1] = 3 + (c + a) % 3;
+        t[2] = 6 + (c + 2 * a) % 3;
+    }
+}
+
+template <int d, int N, typename Energy>
+__global__ void __launch_bounds__(3 * GL_ELEMS, GL_MIN_BLOCKS) k_elem_grad_lanes(ElemLaunch L, Energy energy)
+{
+    constexpr int k = d * N;
+    static_assert(d * (N - 1) == 9, "9 reduced derivatives");
+    using S = Scalar<3, float, false, DoubleFloatValue, DoubleFloat>;
+    __shared__ float gs[GL_ELEMS][2 * k];   // the element gradient as double-float pairs (hi, lo)
+    if (L.active && *L.active == 0) return;
+    const int le = threadIdx.x / 3, s = threadIdx.x % 3;
+    const int64_t e0 = (int64_t)blockIdx.x * GL_ELEMS, e = e0 + le;
+    if (e < L.n_elem)
+    {
+        SubsetElement<d, N, S, true> el;
+        el.handle = e;
+        el.x = L.x;
+        el.err = L.err;
+#pragma unroll
+        for (int i = 0; i < N; ++i) el.vh[i] = L.rec[e * N + i];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) el.idx[c] = 3 * s + c;
+        const S r = energy(el);
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+        {
+            gs[le][2 * (d + 3 * s + c)] = r.grad[c].hi;
+            gs[le][2 * (d + 3 * s + c) + 1] = r.grad[c].lo;
+        }
+        if (s == 0) L.out_f[e] = (double)r.val;
+    }
+    __syncthreads();
+    if (e < L.n_elem)
+        for (int i = s; i < d; i += 3)
+        {
+            // first vertex: g_0 = -sum_{slots >= 1} g_slot (lift_translation_invariant)
+            DoubleFloat acc(gs[le][2 * (d + i)], gs[le][2 * (d + i) + 1]);
+#pragma unroll
+            for (int sl = 2; sl < N; ++sl) acc = acc + DoubleFloat(gs[le][2 * (sl * d + i)], gs[le][2 * (sl * d + i) + 1]);
+            gs[le][2 * i] = -acc.hi;
+            gs[le][2 * i + 1] = -acc.lo;
+        }
+    __syncthreads();
+    const int64_t ne = L.n_elem - e0 < GL_ELEMS ? L.n_elem - e0 : GL_ELEMS;
+    float* dst = (float*)L.out_g + e0 * (2 * k);
+    bool fin = true;
+    for (int q = threadIdx.x; q < ne * 2 * k; q += blockDim.x)
+    {
+        const float v = gs[q / (2 * k)][q % (2 * k)];
+        dst[q] = v;
+        fin = fin && finite_val(v);
+    }
+    if (!fin) report_error(L.err, DEVERR_NONFINITE);
+}
+
+/* runs after k_elem_grad_lanes: an element whose energy is not finite (an
+   inverted element's +inf) gets a zero Hessian, as the functor's constant
+   return gives in the other kernels */
+template <int d, int N, typename Energy>
+__global__ void __launch_bounds__(12 * HL_ELEMS, HL_MIN_BLOCKS) k_elem_hess_lanes(ElemLaunch L, Energy energy)
+{
+    constexpr int k = d * N, R = d * (N - 1), NR = R * (R + 1) / 2;
+    constexpr int BS = N * (N + 1) / 2 * d * d;
+    static_assert(R == 9, "9 reduced derivatives");
+    using S = Scalar<3, float, true, float, float>;
+    __shared__ float xsh[HL_ELEMS][k];      // positions relative to the first vertex, FP32
+    __shared__ float hr[HL_ELEMS][NR];      // packed reduced Hessian per element
+    __shared__ float cs[HL_ELEMS][d][R];    // its slot-0 row sums C[p][J] = sum_s Hr(s d + p, J)
+    __shared__ bool inf_e[HL_ELEMS];        // the element's energy is not finite
+    if (L.active && *L.active == 0) return;
+    const int le = threadIdx.x / 12, l = threadIdx.x % 12;
+    const int64_t e0 = (int64_t)blockIdx.x * HL_ELEMS, e = e0 + le;
+    auto Hr = [&](int ei, int i, int j) { return i <= j ? hr[ei][packed_index(i, j, R)] : hr[ei][packed_index(j, i, R)]; };
+    SubsetElement<d, N, S, true, true> el;
+    if (e < L.n_elem)
+    {
+#pragma unroll
+        for (int i = 0; i < N; ++i) el.vh[i] = L.rec[e * N + i];
+        // the element's positions relative to its first vertex, one coordinate
+        // per lane (the lanes of an element share them)
+        for (int q = l; q < k; q += 12)
+        {
+            const int sl = q / d, c = q % d;
+            const int32_t v0 = el.vh[0], v = el.vh[sl] >= 0 ? el.vh[sl] : v0;   // -1: slot not recorded
+            xsh[le][q] = v0 < 0 ? 0.f : (float)(L.x[(int64_t)d * v + c] - L.x[(int64_t)d * v0 + c]);
+        }
+    }
+    __syncthreads();
+    if (e < L.n_elem)
+    {
+        el.handle = e;
+        el.x = L.x;
+        el.err = L.err;
+        el.xs = xsh[le];
+        plane_line(l, el.idx);
+        const S r = energy(el);
+#pragma unroll
+        for (int p = 0; p < 3; ++p)
+#pragma unroll
+            for (int q = p; q < 3; ++q)
+                if (q > p || l < 3)   // diagonal entries from the direction-0 lines only
+                {
+                    const int I = el.idx[p], J = el.idx[q];
+                    hr[le][I <= J ? packed_index(I, J, R) : packed_index(J, I, R)] = r.H(p, q);
+                }
+        if (l == 0) inf_e[le] = !finite_val(L.out_f[e]);
+    }
+    __syncthreads();
+    const int64_t ne = L.n_elem - e0 < HL_ELEMS ? L.n_elem - e0 : HL_ELEMS;
+    for (int q = threadIdx.x; q < ne * d * R; q += blockDim.x)
+    {
+        // lift_translation_invariant's sums: H_0t = -C, H_00 = sum over the C blocks
+        const int ei = q / (d * R), p = (q / R) % d, J = q % R;
+        float acc = 0.f;
+#pragma unroll
+        for (int sl = 0; sl < N - 1; ++sl) acc += Hr(ei, sl * d + p, J);
+        cs[ei][p][J] = acc;
+    }
+    __syncthreads();
+    float* dst = (float*)L.out_H + e0 * BS;
+    bool fin = true;
+    for (int q = threadIdx.x; q < ne * BS; q += blockDim.x)
+    {
+        const int ei = q / BS, w = q % BS;
+        int P = w / (d * d);   // vertex pair (a, b), a <= b, in packed order
+        const int pp = (w % (d * d)) / d, qq = w % d;
+        int a = 0;
+        while (P >= N - a) { P -= N - a; ++a; }
+        const int b = a + P;
+        float v;
+        if (a >= 1) v = Hr(ei, (a - 1) * d + pp, (b - 1) * d + qq);
+        else if (b >= 1) v = -cs[ei][pp][(b - 1) * d + qq];
+        else
+        {
+            v = 0.f;
+#pragma unroll
+            for (int t = 0; t < N - 1; ++t) v += cs[ei][pp][t * d + qq];
+        }
+        if (inf_e[ei]) v = 0.f;
+        dst[q] = v;
+        fin = fin && finite_val(v);
+    }
+    if (!fin) report_error(L.err, DEVERR_NONFINITE);
+}
+
 inline unsigned elem_grid(int64_t n) { return (unsigned)((n + 127) / 128); }
 
 /* ElemLaunch from the C-ABI callback arguments */
@@ -414,6 +620,13 @@ inline void launch_elements_hessian(const ElemLaunch& L, const Energy& energy, c
     if (L.n_elem <= 0) return;
     constexpr bool deflated = DeflatedProjection<N>::value;
     if (deflated && L.project && L.proj_list) cudaMemsetAsync(L.proj_list, 0, sizeof(uint32_t), s);
+    if constexpr (LaneHessian<d, N, T, Energy>::value)
+    {
+        k_elem_grad_lanes<d, N, Energy><<<(unsigned)((L.n_elem + GL_ELEMS - 1) / GL_ELEMS), 3 * GL_ELEMS, 0, s>>>(L, energy);
+        k_elem_hess_lanes<d, N, Energy><<<(unsigned)((L.n_elem + HL_ELEMS - 1) / HL_ELEMS), 12 * HL_ELEMS, 0, s>>>(L, energy);
+        if (L.project) k_project_blocks<d, N, T, true><<<elem_grid(L.n_elem), 128, 0, s>>>(L, (T)L.eps);
+        return;
+    }
     k_elem_hessian<d, N, T, Energy><<<elem_grid(L.n_elem), 128, 0, s>>>(L, energy);
     if constexpr (!FusedProjection<d * N>::value)
         if (L.project)
@@ -433,7 +646,9 @@ inline void launch_elements_first_order(int mode, const ElemLaunch& L, const Ene
 {
     if (L.n_elem <= 0) return;
     const unsigned g = elem_grid(L.n_elem);
-    using PMixed = typename ValOf<float, d * N>::type;
+    // the value type of the mixed second-order kernels (double-float for the lane-split ones)
+    using PMixed = std::conditional_t<LaneHessian<d, N, float, Energy>::value, DoubleFloatValue,
+                                      typename ValOf<float, d * N>::type>;
     switch (mode)
     {
     case 0: k_elem_value<d, N, Energy><<<g, 128, 0, s>>>(L, energy); break;

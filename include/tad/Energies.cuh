@@ -39,7 +39,8 @@ struct SymmetricDirichletTri
         const int64_t e = element.handle;
         const double* p = prm + e * n_params;
         Mat<P, 2, 2> Mr;
-        Mr.m[0] = P(p[0]); Mr.m[1] = P(p[1]); Mr.m[2] = P(p[2]); Mr.m[3] = P(p[3]);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) Mr.m[i] = P(p[i]);
         const Vec<T, 2> a = element.variables(vtx[e * 3 + 0]);
         const Vec<T, 2> b = element.variables(vtx[e * 3 + 1]);
         const Vec<T, 2> c = element.variables(vtx[e * 3 + 2]);
@@ -207,7 +208,8 @@ struct SymmetricDirichletTriResiduals
         const int64_t e = element.handle;
         const double* p = prm + e * n_params;
         Mat<P, 2, 2> Mr;
-        Mr.m[0] = P(p[0]); Mr.m[1] = P(p[1]); Mr.m[2] = P(p[2]); Mr.m[3] = P(p[3]);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) Mr.m[i] = P(p[i]);
         const Vec<T, 2> a = element.variables(vtx[e * 3 + 0]);
         const Vec<T, 2> b = element.variables(vtx[e * 3 + 1]);
         const Vec<T, 2> c = element.variables(vtx[e * 3 + 2]);

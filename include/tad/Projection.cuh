@@ -87,11 +87,49 @@ __device__ __forceinline__ void jacobi_angle<float>(float app, float aqq, float 
 }
 #endif
 
+/* One Jacobi rotation in the (p, q) plane with precomputed (t, c): A <- J^T A J
+   on the packed matrix, V <- V J */
+template <int k, typename T>
+TAD_HD void jacobi_rotate(T* A, T* V, int p, int q, T t, T c)
+{
+    const T s = t * c;
+    const T apq = A[packed_index(p, q, k)];
+#pragma unroll
+    for (int r = 0; r < k; ++r)
+    {
+        if (r == p || r == q) continue;
+        const int ip = r < p ? packed_index(r, p, k) : packed_index(p, r, k);
+        const int iq = r < q ? packed_index(r, q, k) : packed_index(q, r, k);
+        const T arp = A[ip], arq = A[iq];
+        A[ip] = c * arp - s * arq;
+        A[iq] = s * arp + c * arq;
+    }
+    A[packed_index(p, p, k)] -= t * apq;
+    A[packed_index(q, q, k)] += t * apq;
+    A[packed_index(p, q, k)] = T(0);
+#pragma unroll
+    for (int r = 0; r < k; ++r)
+    {
+        const T vp = V[r * k + p], vq = V[r * k + q];
+        V[r * k + p] = c * vp - s * vq;
+        V[r * k + q] = s * vp + c * vq;
+    }
+}
+
 /* In place: A packed (k(k+1)/2) -> eigenvalues on the diagonal, V (k*k,
-   column l = eigenvector l, row-major V[r*k + l]) */
+   column l = eigenvector l, row-major V[r*k + l]).  Cyclic Jacobi in the
+   round-robin (parallel) ordering: with n = k rounded up to even, a sweep is
+   n - 1 rounds of n/2 disjoint pairs (the circle method: index n - 1 meets
+   r, and (r + j, r - j) mod (n - 1) for j = 1 .. n/2 - 1; a pair with the
+   padding index k of an odd k is skipped), so every pair is visited once per
+   sweep.  The rotations of a round act on disjoint index pairs and commute:
+   their angles are all taken from the matrix at the start of the round and
+   are independent of one another, which a sweep in row order would chain
+   (Golub & Van Loan 8.5.5 on the parallel orderings and their convergence). */
 template <int k, typename T>
 TAD_HD void jacobi_eigen_packed(T* A, T* V)
 {
+    constexpr int n = k + (k & 1), m = n - 1, np = n / 2;
 #pragma unroll
     for (int r = 0; r < k; ++r)
 #pragma unroll
@@ -110,38 +148,33 @@ TAD_HD void jacobi_eigen_packed(T* A, T* V)
             for (int q = p + 1; q < k; ++q) off += A[packed_index(p, q, k)] * A[packed_index(p, q, k)];
         if (!(off > tol)) break;
 #pragma unroll
-        for (int p = 0; p < k - 1; ++p)
+        for (int r = 0; r < m; ++r)
+        {
+            int P[np], Q[np];
+            T tt[np], cc[np];
 #pragma unroll
-            for (int q = p + 1; q < k; ++q)
+            for (int j = 0; j < np; ++j)
             {
-                const T apq = A[packed_index(p, q, k)];
+                const int a = j == 0 ? n - 1 : (r + j) % m, b = j == 0 ? r : (r + m - j) % m;
+                P[j] = a < b ? a : b;
+                Q[j] = a < b ? b : a;
+            }
+#pragma unroll
+            for (int j = 0; j < np; ++j)
+            {
+                tt[j] = T(0);
+                cc[j] = T(1);
+                if (Q[j] >= k) continue;   // the padding index
+                const T apq = A[packed_index(P[j], Q[j], k)];
                 // FP32: no branch -- the fast angle maps a_pq = 0 to the identity rotation
                 if (sizeof(T) == 8 && apq == T(0)) continue;
-                const T app = A[packed_index(p, p, k)], aqq = A[packed_index(q, q, k)];
-                T t, c;
-                jacobi_angle(app, aqq, apq, t, c);
-                const T s = t * c;
-#pragma unroll
-                for (int r = 0; r < k; ++r)
-                {
-                    if (r == p || r == q) continue;
-                    const int ip = r < p ? packed_index(r, p, k) : packed_index(p, r, k);
-                    const int iq = r < q ? packed_index(r, q, k) : packed_index(q, r, k);
-                    const T arp = A[ip], arq = A[iq];
-                    A[ip] = c * arp - s * arq;
-                    A[iq] = s * arp + c * arq;
-                }
-                A[packed_index(p, p, k)] = app - t * apq;
-                A[packed_index(q, q, k)] = aqq + t * apq;
-                A[packed_index(p, q, k)] = T(0);
-#pragma unroll
-                for (int r = 0; r < k; ++r)
-                {
-                    const T vp = V[r * k + p], vq = V[r * k + q];
-                    V[r * k + p] = c * vp - s * vq;
-                    V[r * k + q] = s * vp + c * vq;
-                }
+                jacobi_angle(A[packed_index(P[j], P[j], k)], A[packed_index(Q[j], Q[j], k)], apq, tt[j], cc[j]);
             }
+#pragma unroll
+            for (int j = 0; j < np; ++j)
+                if (Q[j] < k && !(sizeof(T) == 8 && A[packed_index(P[j], Q[j], k)] == T(0)))
+                    jacobi_rotate<k, T>(A, V, P[j], Q[j], tt[j], cc[j]);
+        }
     }
 }
 

@@ -214,6 +214,34 @@ def test_tet_eval_parity(tad, oracle):
         assert rel_err(f, fo) <= TOL and rel_err(g, go) <= TOL and sparse_rel_err(H, Ho) <= TOL
 
 
+def test_tet_mixed_lane_kernels(tad, oracle):
+    """Mixed precision on tets runs the lane-split evaluation (three
+    double-float gradient lanes and twelve FP32 Hessian lanes per element,
+    each on an index triple of the affine plane of order 3): f and g match
+    the FP64 oracle, the exact and the projected H match it at FP32
+    accuracy, and inverted elements give +inf, zero derivatives and the
+    eps*I projected block, as the reference does (HessianProjection.hh:66-98)."""
+    w = meshes.tet_twist(4, seed=1)
+    fm = tad.ScalarFunction.from_workload(w, precision=tad.PREC_MIXED)
+    p = oracle.Problem.from_workload(w)
+    for x in (w.x0, valid_perturbation(w, p, 0.01, 3)):
+        f, g, H = fm.eval_with_derivatives(x)
+        fo, go, Ho = p.eval_with_derivatives(x)
+        assert rel_err(f, fo) <= 1e-12 and rel_err(g, go) <= 1e-10, (rel_err(f, fo), rel_err(g, go))
+        assert H.nnz == Ho.nnz and sparse_rel_err(H, Ho) <= 5e-5, sparse_rel_err(H, Ho)
+        f, g, H = fm.eval_with_hessian_proj(x)
+        fo, go, Ho = p.eval_with_hessian_proj(x)
+        assert rel_err(f, fo) <= 1e-12 and rel_err(g, go) <= 1e-10
+        assert sparse_rel_err(H, Ho) <= 5e-5, sparse_rel_err(H, Ho)
+    x = w.x0.copy()
+    x[2::3] *= -1.0   # mirrored: every tetrahedron inverted
+    assert p.eval(x) == np.inf
+    f, g, H = fm.eval_with_hessian_proj(x)
+    fo, go, Ho = p.eval_with_hessian_proj(x)
+    assert f == np.inf and fo == np.inf
+    assert rel_err(g, go) <= 1e-10 and sparse_rel_err(H, Ho) <= 5e-5, (rel_err(g, go), sparse_rel_err(H, Ho))
+
+
 def test_tet_newton_parity(tad, oracle):
     w = meshes.tet_twist(4, seed=1)
     fn, p = _pair(tad, oracle, w, pcg_rel_tol=1e-10, pcg_max_iters=3000)

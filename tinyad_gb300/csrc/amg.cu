@@ -53,7 +53,7 @@ namespace tadlib {
 constexpr int64_t AMG_COARSE_ROWS = 256;
 constexpr int AMG_MAX_LEVELS = 12;
 constexpr int AMG_COARSE_SWEEPS = 12;
-constexpr int AMG_COARSE_THREADS = 512;
+constexpr int AMG_COARSE_THREADS = 1024;
 /* damping of the prolongator smoother I - omega S A, S the l1 block-Jacobi
    inverse: rho(S A) <= 1 for symmetric positive definite A, so omega < 2
    keeps it stable without a spectral-radius estimate (the usual 4 / (3 rho)
@@ -722,7 +722,13 @@ __global__ void __launch_bounds__(RED_THREADS) k_amg_post(int64_t n, const int32
 }
 
 /* coarsest level: x (already S r) plus AMG_COARSE_SWEEPS - 1 further l1
-   block-Jacobi sweeps x += S (r - A x), in one thread block (w: scratch) */
+   block-Jacobi sweeps x += S (r - A x), in one thread block (w: scratch).
+   CoarseLanes<d> lanes share a block row (lane l takes its blocks l, l + L,
+   ...; a fixed xor-shuffle tree sums them): a coarse row of a tetrahedral
+   mesh has 30-40 3 x 3 blocks, whose dependent loads one thread per row
+   walked in sequence (95 us per call on the 48^3 cube, 12 sweeps). */
+template <int d> struct CoarseLanes { static constexpr int value = d == 3 ? 8 : 4; };
+
 template <int d, typename T>
 __global__ void __launch_bounds__(AMG_COARSE_THREADS) k_amg_coarse(int64_t n, const int32_t* __restrict__ bptr,
                                                                    const int32_t* __restrict__ bcol, const T* __restrict__ A,
@@ -730,20 +736,43 @@ __global__ void __launch_bounds__(AMG_COARSE_THREADS) k_amg_coarse(int64_t n, co
                                                                    T* __restrict__ x, T* __restrict__ w, const DevScalars* ds)
 {
     AMG_STOP;
+    constexpr int L = CoarseLanes<d>::value, RPP = AMG_COARSE_THREADS / L;   // rows per pass
+    const int lane = threadIdx.x % L, sub = threadIdx.x / L;
     T* a = x;
     T* b = w;
     for (int k = 1; k < AMG_COARSE_SWEEPS; ++k)
     {
-        for (int64_t u = threadIdx.x; u < n; u += blockDim.x)
+        for (int64_t base = 0; base < n; base += RPP)
         {
+            const int64_t u = base + sub;
             T y[d];
-            bsr_row_product<d, T>(bptr, bcol, A, a, u, y);
-            T e[d], s[d];
 #pragma unroll
-            for (int i = 0; i < d; ++i) e[i] = r[u * d + i] - y[i];
-            apply_dinv<d, T>(dl1, u, e, s);
+            for (int i = 0; i < d; ++i) y[i] = T(0);
+            if (u < n)
+                for (int32_t q = bptr[u] + lane; q < bptr[u + 1]; q += L)
+                {
+                    const int64_t v = bcol[q];
+                    T B[d * d], av[d];
+                    load_block<d, T>(A + (int64_t)q * d * d, B);
+                    load_vec<d, T>(a + v * d, av);
 #pragma unroll
-            for (int i = 0; i < d; ++i) b[u * d + i] = a[u * d + i] + s[i];
+                    for (int i = 0; i < d; ++i)
+#pragma unroll
+                        for (int j = 0; j < d; ++j) y[i] += B[i * d + j] * av[j];
+                }
+#pragma unroll
+            for (int off = L / 2; off > 0; off >>= 1)
+#pragma unroll
+                for (int i = 0; i < d; ++i) y[i] += __shfl_xor_sync(0xffffffffu, y[i], off, L);
+            if (u < n && lane == 0)
+            {
+                T e[d], sv[d];
+#pragma unroll
+                for (int i = 0; i < d; ++i) e[i] = r[u * d + i] - y[i];
+                apply_dinv<d, T>(dl1, u, e, sv);
+#pragma unroll
+                for (int i = 0; i < d; ++i) b[u * d + i] = a[u * d + i] + sv[i];
+            }
         }
         __syncthreads();
         T* t = a; a = b; b = t;
@@ -803,24 +832,6 @@ __global__ void __launch_bounds__(RED_THREADS) k_amg_update(int64_t n, T* __rest
         ds->rr = tot[0];
         ds->iters += 1;
         if (tot[0] <= ds->tol2 || ds->iters >= ds->max_iters || !isfinite(tot[0])) ds->done = 1;
-    }
-}
-
-/* r.z, beta = r.z / rz_old (first: 0) and the breakdown test (single-level hierarchies) */
-template <typename T>
-__global__ void __launch_bounds__(RED_THREADS) k_amg_rz(int64_t m, const T* __restrict__ r, const T* __restrict__ z,
-                                                        double* partials, unsigned* counter, DevScalars* ds, int first)
-{
-    AMG_STOP;
-    T part = T(0);
-    GRID_STRIDE(i, m) part += r[i] * z[i];
-    double v[1] = {as_double(part)}, tot[1];
-    if (!grid_sum<1>(v, partials, counter, tot)) return;
-    if (threadIdx.x == 0)
-    {
-        if (!(tot[0] > 0.0) || !isfinite(tot[0])) { ds->breakdown = 1; ds->done = 1; return; }
-        ds->beta = first ? 0.0 : tot[0] / ds->rz;
-        ds->rz = tot[0];
     }
 }
 
@@ -884,13 +895,7 @@ static void apply(Problem& P, int mode, T* xs, T* r, T* z, T* p, T* Ap)
         k_amg_update<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(L.n, xs, r, p, Ap, (const T*)L.dl1, z, P.partials,
                                                               P.counters + 2, P.ds);
     P.n_launches += 1;
-    vcycle_from<d, T>(P, 0, r, z, mode == 0);
-    if (P.amg.size() == 1)
-    {
-        // a single level: the coarse sweeps are the whole preconditioner, and r.z is reduced here
-        k_amg_rz<T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(L.n * d, r, z, P.partials, P.counters + 9, P.ds, mode == 0);
-        P.n_launches += 1;
-    }
+    vcycle_from<d, T>(P, 0, r, z, mode == 0);   // the solver uses hierarchies of two or more levels
 }
 
 template <int d, typename T>

@@ -699,7 +699,9 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
         }
         if (P.hs->done) break;
         const bool slow = replays == 1;   // not done after 1 + PCG_CHUNK iterations
-        if (allow_amg && slow && P.settings.preconditioner == 1 && w == 0.0)
+        // (a problem at or below the coarsest AMG size is one level: its
+        // "V-cycle" would be the coarse smoother alone, so block Jacobi goes on)
+        if (allow_amg && slow && P.settings.preconditioner == 1 && w == 0.0 && P.amg.size() > 1)
         {
             // block Jacobi's fast start (the high frequencies) is over and the
             // tolerance is not met: continue from this iterate under the V-cycle
@@ -850,7 +852,7 @@ static tad_status pcg_dispatch(Problem& P, const double* b, double* xsol, int pr
 template <int d>
 static tad_status prepare_graphs_d(Problem& P)
 {
-    const bool amg = P.settings.preconditioner == 1 && !P.amg.empty();
+    const bool amg = P.settings.preconditioner == 1 && P.amg.size() > 1;
     if (P.precision == TAD_PREC_MIXED)
     {
         tad_status st = ensure_pcg_graph<d, float>(P, P.dx32, P.r32, P.z32, P.p32, P.Ap32, P.dinv32, 1);
