@@ -325,6 +325,30 @@ def test_newton_direction_api(tad, oracle):
     assert abs(d @ go - do @ go) <= 1e-8 * abs(do @ go)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_newton_direction_tet_w_identity(tad, oracle, precision):
+    """newton_direction with w I added (NewtonDirection.hh:32) on tets, whose
+    PCG runs on the sliced-ELL copy of H: in FP64 the direction solves the
+    oracle's (H + w I) d = -g; in mixed precision the system of its own FP32
+    Hessian (FP64 refinement to 1e-11), whose shifted diagonal H_ii + w is
+    itself rounded to FP32 (hence 1e-6 there)."""
+    import scipy.sparse as sp
+    w = meshes.tet_twist(4, seed=2)
+    prec = tad.PREC_MIXED if precision == "mixed" else tad.PREC_FP64
+    fn, p = _pair(tad, oracle, w, precision=prec, pcg_rel_tol=1e-11, pcg_max_iters=5000, refine_max_iters=8,
+                  refine_rel_tol=1e-11)
+    x = valid_perturbation(w, p, 0.01, 4)
+    if precision == "fp64":
+        _, g_ref, H_ref = p.eval_with_hessian_proj(x)
+    else:
+        _, g_ref, H_ref = fn.eval_with_hessian_proj(x)
+    for wid in (0.0, 0.5):
+        d, f, g = fn.newton_direction(x, w_identity=wid)
+        A = H_ref + wid * sp.identity(H_ref.shape[0], format="csr")
+        tol = 1e-6 if (precision == "mixed" and wid != 0.0) else 1e-8
+        assert rel_err(A @ d, -g_ref) <= tol, (wid, rel_err(A @ d, -g_ref))
+
+
 def test_newton_decrement(tad, oracle):
     """newton_decrement (NewtonDecrement.hh:20-26) through the C ABI, host and
     device forms, against the oracle's -d.g/2; and the reference's loop

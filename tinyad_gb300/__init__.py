@@ -307,14 +307,16 @@ class ScalarFunction:
         return float(f[0]), g, self._csr(vals)
 
     # ---- solver utilities ----------------------------------------------------
-    def newton_direction(self, x, projection_eps: float = default_hessian_projection_eps, projected: bool = True):
-        """d = -H(x)^-1 g(x) (device PCG), H projected (default) or exact.
-        Returns (d, f, g)."""
+    def newton_direction(self, x, projection_eps: float = default_hessian_projection_eps, projected: bool = True,
+                         w_identity: float = 0.0):
+        """d = -(H(x) + w I)^-1 g(x) (device PCG; NewtonDirection.hh:25-48), H
+        projected (default) or exact.  Returns (d, f, g)."""
         x = self._x(x)
         d = np.zeros(self.n_vars)
         g = np.zeros(self.n_vars)
         f = np.zeros(1)
-        self._check(self.L.tad_newton_direction(self.h, _d(x), int(projected), projection_eps, 0.0, _d(d), _d(f), _d(g)),
+        self._check(self.L.tad_newton_direction(self.h, _d(x), int(projected), projection_eps, float(w_identity), _d(d),
+                                                _d(f), _d(g)),
                     allow=(TAD_ERR_PCG_NOCONV,))
         return d, float(f[0]), g
 

@@ -638,6 +638,23 @@ __global__ void k_amg_residual(int64_t n, const int32_t* __restrict__ bptr, cons
     }
 }
 
+/* k_amg_residual on the sliced-ELL copy of the finest level's matrix (the
+   problem's H) */
+template <int d, typename T>
+__global__ void k_amg_residual_sell(int64_t n, const int32_t* __restrict__ sptr, const int32_t* __restrict__ scol,
+                                    const T* __restrict__ As, const T* __restrict__ r, const T* __restrict__ x,
+                                    T* __restrict__ res, const DevScalars* ds)
+{
+    AMG_STOP;
+    GRID_STRIDE(u, n)
+    {
+        T y[d];
+        sell_row_product<d, T>(sptr, scol, As, x, u, y);
+#pragma unroll
+        for (int i = 0; i < d; ++i) res[u * d + i] = r[u * d + i] - y[i];
+    }
+}
+
 /* r_c(I) = sum_u P(u, I)^T res(u), x_c(I) = S_c(I) r_c(I): one warp per
    coarse row, lane k taking the k-th, (k+32)-th, ... (u, P(u, I)) pair, then
    a fixed xor-shuffle tree (deterministic) */
@@ -812,18 +829,22 @@ __global__ void __launch_bounds__(RED_THREADS) k_amg_update(int64_t n, T* __rest
     T part = T(0);
     GRID_STRIDE(u, n)
     {
-        T rv[d], zv[d];
+        T xv[d], pv[d], rv[d], av[d], zv[d];
+        load_vec<d, T>(x + u * d, xv);
+        load_vec<d, T>(p + u * d, pv);
+        load_vec<d, T>(r + u * d, rv);
+        load_vec<d, T>(Ap + u * d, av);
 #pragma unroll
         for (int i = 0; i < d; ++i)
         {
-            x[u * d + i] += alpha * p[u * d + i];
-            rv[i] = r[u * d + i] - alpha * Ap[u * d + i];
-            r[u * d + i] = rv[i];
+            xv[i] += alpha * pv[i];
+            rv[i] -= alpha * av[i];
             part += rv[i] * rv[i];
         }
+        store_vec<d, T>(x + u * d, xv);
+        store_vec<d, T>(r + u * d, rv);
         apply_dinv<d, T>(dl1, u, rv, zv);
-#pragma unroll
-        for (int i = 0; i < d; ++i) z[u * d + i] = zv[i];
+        store_vec<d, T>(z + u * d, zv);
     }
     double v[1] = {as_double(part)}, tot[1];
     if (!grid_sum<1>(v, partials, counter, tot)) return;
@@ -868,7 +889,11 @@ static void vcycle_from(Problem& P, size_t l, const T* r, T* x, int first)
     }
     AmgLevel& C = P.amg[l + 1];
     const unsigned g = grid_for(L.n);
-    k_amg_residual<d, T><<<g, RED_THREADS, 0, s>>>(L.n, L.bptr, L.bcol, A, r, x, (T*)L.res, ds);
+    const SellView sv = l == 0 ? sell_view(P, A) : SellView{nullptr, nullptr, nullptr};
+    if (sv.Hs)
+        k_amg_residual_sell<d, T><<<g, RED_THREADS, 0, s>>>(L.n, sv.sptr, sv.scol, (const T*)sv.Hs, r, x, (T*)L.res, ds);
+    else
+        k_amg_residual<d, T><<<g, RED_THREADS, 0, s>>>(L.n, L.bptr, L.bcol, A, r, x, (T*)L.res, ds);
     k_amg_restrict<d, T><<<warp_grid(C.n), RED_THREADS, 0, s>>>(C.n, L.tptr, L.tu, L.tp, (const T*)L.Pv, (const T*)L.res,
                                                                 (const T*)C.dl1, (T*)C.r, (T*)C.x, ds);
     P.n_launches += 2;

@@ -7,6 +7,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include "internal.hh"
 #include "grid_reduce.cuh"
 #include "../../include/tad/Scalar.cuh"
 
@@ -35,6 +36,19 @@ __device__ __forceinline__ void load_vec(const T* __restrict__ src, T (&v)[d])
     {
 #pragma unroll
         for (int j = 0; j < d; ++j) v[j] = src[j];
+    }
+}
+
+/* store the d entries of one block row of a vector (one 8-byte store for 2D FP32) */
+template <int d, typename T>
+__device__ __forceinline__ void store_vec(T* __restrict__ dst, const T (&v)[d])
+{
+    if constexpr (d == 2 && sizeof(T) == 4)
+        *reinterpret_cast<float2*>(dst) = make_float2(v[0], v[1]);
+    else
+    {
+#pragma unroll
+        for (int j = 0; j < d; ++j) dst[j] = v[j];
     }
 }
 
@@ -103,6 +117,72 @@ __device__ __forceinline__ void bsr_row_product(const int32_t* __restrict__ bptr
     }
 }
 
+/* y = (row u of the matrix) z from its sliced-ELL copy (Problem::sptr/scol/
+   Hs): u's blocks sit at sptr[u/32] + j*32 + u%32, j < the slice's longest
+   row (zero blocks beyond u's own).  With rows mapped to consecutive lanes
+   (GRID_STRIDE), a warp is one slice: its j-th column ids and blocks are
+   contiguous 128- and 32*d*d*sizeof(T)-byte ranges, the block and id loads
+   of all j are independent, and no row pointer is loaded.  Blocks are summed
+   in the row's order, as bsr_row_product does. */
+template <int d, typename T>
+__device__ __forceinline__ void sell_row_product(const int32_t* __restrict__ sptr, const int32_t* __restrict__ scol,
+                                                 const T* __restrict__ Hs, const T* __restrict__ z, int64_t u, T (&y)[d])
+{
+#pragma unroll
+    for (int i = 0; i < d; ++i) y[i] = T(0);
+    const int64_t sl = u >> 5;
+    int64_t q = sptr[sl] + (u & 31);
+    const int64_t q1 = sptr[sl + 1];
+    for (; q + 96 < q1; q += 128)
+    {
+        int64_t v[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) v[k] = __ldg(scol + q + 32 * k);
+        T B[4][d * d], zv[4][d];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+        {
+            load_block<d, T>(Hs + (q + 32 * k) * d * d, B[k]);
+            load_vec<d, T>(z + v[k] * d, zv[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+#pragma unroll
+            for (int i = 0; i < d; ++i)
+#pragma unroll
+                for (int j = 0; j < d; ++j) y[i] += B[k][i * d + j] * zv[k][j];
+    }
+    for (; q < q1; q += 32)
+    {
+        const int64_t v = __ldg(scol + q);
+        T B[d * d], zv[d];
+        load_block<d, T>(Hs + q * d * d, B);
+        load_vec<d, T>(z + v * d, zv);
+#pragma unroll
+        for (int i = 0; i < d; ++i)
+#pragma unroll
+            for (int j = 0; j < d; ++j) y[i] += B[i * d + j] * zv[j];
+    }
+}
+
+/* the sliced-ELL arrays of a problem's H (all null: none, use the BSR form) */
+struct SellView
+{
+    const int32_t* sptr;
+    const int32_t* scol;
+    const void* Hs;
+};
+
+/* The sliced-ELL view of the problem's H when the matrix H handed to a solve
+   is that H and the copy exists (other matrices, such as the FP64 copy of a
+   mixed solve's completion, have none) */
+template <typename T>
+inline SellView sell_view(const Problem& P, const T* H)
+{
+    if (P.Hs && (const void*)H == P.Hs_of) return SellView{P.sptr, P.scol, P.Hs};
+    return SellView{nullptr, nullptr, nullptr};
+}
+
 
 /* ---- block-Jacobi preconditioner: invert (H_uu + w I) ------------------- */
 /* inverse of block row u's diagonal block (+ w I) into I; a block that is not
@@ -163,12 +243,14 @@ __global__ void k_diag_inv(int64_t nh, const int32_t* __restrict__ diag, const T
 template <int d, typename T>
 __device__ __forceinline__ void apply_dinv(const T* __restrict__ dinv, int64_t u, const T (&r)[d], T (&z)[d])
 {
+    T D[d * d];
+    load_block<d, T>(dinv + u * d * d, D);
 #pragma unroll
     for (int i = 0; i < d; ++i)
     {
         T acc = T(0);
 #pragma unroll
-        for (int j = 0; j < d; ++j) acc += dinv[u * d * d + i * d + j] * r[j];
+        for (int j = 0; j < d; ++j) acc += D[i * d + j] * r[j];
         z[i] = acc;
     }
 }

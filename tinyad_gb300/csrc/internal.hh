@@ -159,6 +159,15 @@ struct Problem
     double* x = nullptr;
     double* g = nullptr;
     void* H = nullptr;         // nb*d*d, double or float
+    // sliced-ELL copy of H for the SpMVs: block rows in slices of 32; slot
+    // sptr[s] + j * 32 + (u mod 32) holds the j-th block of row u of slice s
+    // (zero blocks pad rows shorter than their slice's longest), so a warp's
+    // 32 rows read their j-th blocks and column ids as contiguous ranges
+    int64_t n_slots = 0;
+    int32_t *sptr = nullptr, *scol = nullptr;   // slices + 1 / slots
+    int32_t *spos = nullptr, *sdiag = nullptr;  // per BSR block / per block row: its slot
+    void* Hs = nullptr;                          // n_slots*d*d, as H (null: no copy, CSR SpMVs)
+    const void* Hs_of = nullptr;                 // the buffer Hs copies (H as allocated; solves may swap H)
     double* H64 = nullptr;     // FP64 copy for mixed-mode refinement residuals (optional)
     double* csr_tmp = nullptr; // CSR-ordered values for export
 

@@ -236,7 +236,8 @@ void launch_assemble_grad_newton(Problem& P, int precision, bool pairs)
 
 template <int d, typename T>
 __global__ void k_assemble_hess(int64_t nb, const int32_t* __restrict__ cptr, const int32_t* __restrict__ cidx,
-                                const T* __restrict__ eH, T* __restrict__ H, const int32_t* guard)
+                                const T* __restrict__ eH, T* __restrict__ H, const int32_t* guard,
+                                T* __restrict__ Hs, const int32_t* __restrict__ spos)
 {
     const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (b >= nb || (guard && *guard == 0)) return;
@@ -275,6 +276,7 @@ __global__ void k_assemble_hess(int64_t nb, const int32_t* __restrict__ cptr, co
         }
     }
     tad::store_row<T, d * d>(H, b, acc);
+    if (Hs) tad::store_row<T, d * d>(Hs, spos[b], acc);   // and its sliced-ELL slot
 }
 
 void launch_assemble_hess(Problem& P, int precision)
@@ -283,9 +285,11 @@ void launch_assemble_hess(Problem& P, int precision)
     if (P.nb == 0) return;
 #define TAD_ASM(D)                                                                                         \
     if (precision == TAD_PREC_MIXED)                                                                       \
-        k_assemble_hess<D, float><<<grid, 256, 0, P.stream>>>(P.nb, P.cptr, P.cidx, (const float*)P.eH, (float*)P.H, P.launch_guard); \
+        k_assemble_hess<D, float><<<grid, 256, 0, P.stream>>>(P.nb, P.cptr, P.cidx, (const float*)P.eH, (float*)P.H,    \
+                                                              P.launch_guard, (float*)P.Hs, P.spos);              \
     else                                                                                                   \
-        k_assemble_hess<D, double><<<grid, 256, 0, P.stream>>>(P.nb, P.cptr, P.cidx, (const double*)P.eH, (double*)P.H, P.launch_guard);
+        k_assemble_hess<D, double><<<grid, 256, 0, P.stream>>>(P.nb, P.cptr, P.cidx, (const double*)P.eH, (double*)P.H, \
+                                                               P.launch_guard, (double*)P.Hs, P.spos);
     switch (P.d)
     {
     case 1: TAD_ASM(1); break;

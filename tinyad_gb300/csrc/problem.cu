@@ -222,6 +222,62 @@ static tad_status build_pattern(Problem& P)
     return TAD_OK;
 }
 
+/* The sliced-ELL layout of H's pattern (Problem::sptr/scol/spos/sdiag) and
+   the zeroed copy Hs, for 3 x 3 blocks.  Measured per PCG SpMV (ncu, cold
+   cache): 663,552 tets (3 x 3 blocks, ~15 per row) 30.9 us for the BSR form
+   with 8 lanes per row, 22.0 us on the copy; the 1.64M-face disk (2 x 2
+   blocks, ~7 per row, each warp's rows already one contiguous 3.6 KB range)
+   31.2 us against 31.8 us, while the second write made its assembly 18 us
+   slower -- so 2 x 2 problems keep the BSR form only.  Left out too when the
+   padding would add more than half the blocks of the pattern. */
+static tad_status build_sell(Problem& P)
+{
+    if (P.d != 3) return TAD_OK;
+    const int64_t nh = P.n_handles, ns = (nh + 31) / 32;
+    std::vector<int32_t> sptr(ns + 1, 0);
+    for (int64_t sl = 0; sl < ns; ++sl)
+    {
+        int32_t mx = 0;
+        for (int64_t u = sl * 32; u < std::min<int64_t>(nh, sl * 32 + 32); ++u) mx = std::max(mx, P.bptr_h[u + 1] - P.bptr_h[u]);
+        if ((int64_t)sptr[sl] + 32 * (int64_t)mx >= INT32_MAX) return TAD_OK;
+        sptr[sl + 1] = sptr[sl] + 32 * mx;
+    }
+    const int64_t slots = sptr[ns];
+    if (slots > P.nb + P.nb / 2) return TAD_OK;
+    std::vector<int32_t> scol(slots), spos(P.nb), sdiag(nh, -1);
+    for (int64_t sl = 0; sl < ns; ++sl)
+        for (int lane = 0; lane < 32; ++lane)
+        {
+            const int64_t u = sl * 32 + lane;
+            const int32_t len = u < nh ? P.bptr_h[u + 1] - P.bptr_h[u] : 0;
+            for (int32_t j = 0; (int64_t)sptr[sl] + 32 * j < sptr[sl + 1]; ++j)
+            {
+                const int64_t q = sptr[sl] + 32 * (int64_t)j + lane;
+                if (j < len)
+                {
+                    const int32_t b = P.bptr_h[u] + j;
+                    scol[q] = P.bcol_h[b];
+                    spos[b] = (int32_t)q;
+                    if (P.bcol_h[b] == u) sdiag[u] = (int32_t)q;
+                }
+                else scol[q] = (int32_t)std::min<int64_t>(u, nh - 1);   // a zero block; any valid column
+            }
+        }
+    P.n_slots = slots;
+    TAD_CUDA_TRY(dalloc(&P.sptr, ns + 1));
+    TAD_CUDA_TRY(dalloc(&P.scol, slots));
+    TAD_CUDA_TRY(dalloc(&P.spos, P.nb));
+    TAD_CUDA_TRY(dalloc(&P.sdiag, nh));
+    TAD_CUDA_TRY(dalloc((double**)&P.Hs, slots * P.d * P.d));
+    TAD_CUDA_TRY(cudaMemcpy(P.sptr, sptr.data(), (ns + 1) * 4, cudaMemcpyHostToDevice));
+    TAD_CUDA_TRY(cudaMemcpy(P.scol, scol.data(), slots * 4, cudaMemcpyHostToDevice));
+    TAD_CUDA_TRY(cudaMemcpy(P.spos, spos.data(), P.nb * 4, cudaMemcpyHostToDevice));
+    TAD_CUDA_TRY(cudaMemcpy(P.sdiag, sdiag.data(), nh * 4, cudaMemcpyHostToDevice));
+    TAD_CUDA_TRY(cudaMemset(P.Hs, 0, slots * P.d * P.d * sizeof(double)));
+    P.Hs_of = P.H;
+    return TAD_OK;
+}
+
 tad_status ensure_finalized(Problem& P)
 {
     if (P.finalized) return TAD_OK;
@@ -274,6 +330,8 @@ tad_status ensure_finalized(Problem& P)
     if (s != TAD_OK) return s;
     const int64_t n = P.n_vars, nh = P.n_handles, dd = P.d * P.d;
     TAD_CUDA_TRY(dalloc((double**)&P.H, P.nb * dd));
+    s = build_sell(P);
+    if (s != TAD_OK) return s;
     TAD_CUDA_TRY(dalloc(&P.csr_tmp, P.nb * dd));
     TAD_CUDA_TRY(dalloc(&P.r, n)); TAD_CUDA_TRY(dalloc(&P.z, n)); TAD_CUDA_TRY(dalloc(&P.p, n));
     TAD_CUDA_TRY(dalloc(&P.Ap, n)); TAD_CUDA_TRY(dalloc(&P.dx, n)); TAD_CUDA_TRY(dalloc(&P.dinv, nh * dd));
@@ -429,7 +487,7 @@ TAD_API tad_status tad_problem_destroy(tad_problem* P)
                     P->x, P->g, P->H, P->H64, P->csr_tmp, P->r, P->z, P->p, P->Ap, P->dx, P->dinv,
                     P->r32, P->z32, P->p32, P->Ap32, P->dx32, P->dinv32, P->rhs, P->res, P->steps,
                     P->partials, P->counters, P->ds, P->err, P->proj_list, P->steps_seq, P->x_trial,
-                    P->last_x, P->diff_flag};
+                    P->last_x, P->diff_flag, P->sptr, P->scol, P->spos, P->sdiag, P->Hs};
     for (void* b : bufs) dfree(b);
     if (P->hs) cudaFreeHost(P->hs);
     if (P->err_h) cudaFreeHost(P->err_h);

@@ -263,18 +263,61 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_spmv_vec(int64_t nh, const 
     }
 }
 
+/* k_pcg_spmv_fused on the sliced-ELL copy of H (sell_row_product) */
+template <int d, typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_pcg_spmv_sell(int64_t nh, const int32_t* __restrict__ sptr,
+                                                               const int32_t* __restrict__ scol, const T* __restrict__ Hs,
+                                                               const T* __restrict__ z, T* __restrict__ p, T* __restrict__ Ap,
+                                                               double* partials, unsigned* counter, DevScalars* ds)
+{
+    if (*(volatile int32_t*)&ds->done) return;
+    const T beta = from_double<T>(ds->beta);
+    T part = T(0);
+    GRID_STRIDE(u, nh)
+    {
+        T y[d];
+        sell_row_product<d, T>(sptr, scol, Hs, z, u, y);
+#pragma unroll
+        for (int i = 0; i < d; ++i)
+        {
+            const T apn = y[i] + beta * Ap[u * d + i];
+            const T pn = z[u * d + i] + beta * p[u * d + i];
+            Ap[u * d + i] = apn;
+            p[u * d + i] = pn;
+            part += pn * apn;
+        }
+    }
+    double v[1] = {as_double(part)}, tot[1];
+    if (!grid_sum<1>(v, partials, counter, tot)) return;
+    if (threadIdx.x == 0)
+    {
+        ds->pAp = tot[0];
+        if (!(tot[0] > 0.0) || !isfinite(tot[0]))
+        {
+            ds->breakdown = 1;
+            ds->done = 1;
+            ds->alpha = 0.0;
+        }
+        else ds->alpha = ds->rz / tot[0];
+    }
+}
+
 template <int d> struct SpmvGroup { static constexpr int value = d == 3 ? 16 : 8; };
 
-/* The PCG SpMV for d x d blocks: thread per block row for d <= 2 (rows of
-   ~7 2x2 blocks on triangle meshes: 41.1 us; the 4- and 8-lane vector form
-   45.5 / 76.3 us on the 1.64M-face disk), 8 lanes per row for d = 3 (rows
-   of ~15 3x3 blocks on tet meshes: 27.1 instead of 37.4 us on 663,552
-   tets). */
+/* The PCG SpMV for d x d blocks: on the sliced-ELL copy of H where there is
+   one (thread per block row, coalesced block and column-id loads); else on
+   the BSR arrays, a thread per block row for d <= 2 (rows of ~7 2x2 blocks
+   on triangle meshes: 41.1 us; the 4- and 8-lane vector form 45.5 / 76.3 us
+   on the 1.64M-face disk) and 8 lanes per row for d = 3 (rows of ~15 3x3
+   blocks on tet meshes: 27.1 instead of 37.4 us on 663,552 tets). */
 template <int d, typename T>
-inline void launch_pcg_spmv(cudaStream_t s, int64_t nh, const int32_t* bptr, const int32_t* bcol, const T* H, const T* z,
-                            T* p, T* Ap, double* partials, unsigned* counter, DevScalars* ds)
+inline void launch_pcg_spmv(cudaStream_t s, const SellView& sv, int64_t nh, const int32_t* bptr, const int32_t* bcol,
+                            const T* H, const T* z, T* p, T* Ap, double* partials, unsigned* counter, DevScalars* ds)
 {
-    if constexpr (d == 3)
+    if (sv.Hs)
+        k_pcg_spmv_sell<d, T><<<PCG_BLOCKS, RED_THREADS, 0, s>>>(nh, sv.sptr, sv.scol, (const T*)sv.Hs, z, p, Ap, partials,
+                                                                counter, ds);
+    else if constexpr (d == 3)
         k_pcg_spmv_vec<d, T, 8><<<PCG_BLOCKS, RED_THREADS, 0, s>>>(nh, bptr, bcol, H, z, p, Ap, partials, counter, ds);
     else
         k_pcg_spmv_fused<d, T, SpmvGroup<d>::value><<<PCG_BLOCKS, RED_THREADS, 0, s>>>(nh, bptr, bcol, H, z, p, Ap, partials,
@@ -282,7 +325,8 @@ inline void launch_pcg_spmv(cudaStream_t s, int64_t nh, const int32_t* bptr, con
 }
 
 template <int d, typename T>
-__global__ void __launch_bounds__(RED_THREADS) k_pcg_update(int64_t nh, T* x, T* r, T* z, const T* __restrict__ p, const T* __restrict__ Ap,
+__global__ void __launch_bounds__(RED_THREADS) k_pcg_update(int64_t nh, T* __restrict__ x, T* __restrict__ r, T* __restrict__ z,
+                                                            const T* __restrict__ p, const T* __restrict__ Ap,
                                                             const T* __restrict__ dinv, double* partials, unsigned* counter, DevScalars* ds)
 {
     if (*(volatile int32_t*)&ds->done) return;
@@ -290,19 +334,25 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_update(int64_t nh, T* x, T*
     T part0 = T(0), part1 = T(0);
     GRID_STRIDE(u, nh)
     {
-        T rv[d], zv[d];
+        // whole block rows per access (8-byte vectors for 2D FP32); x, r, z, p, Ap are distinct buffers
+        T xv[d], pv[d], rv[d], av[d], zv[d];
+        load_vec<d, T>(x + u * d, xv);
+        load_vec<d, T>(p + u * d, pv);
+        load_vec<d, T>(r + u * d, rv);
+        load_vec<d, T>(Ap + u * d, av);
 #pragma unroll
         for (int i = 0; i < d; ++i)
         {
-            x[u * d + i] += alpha * p[u * d + i];
-            rv[i] = r[u * d + i] - alpha * Ap[u * d + i];
-            r[u * d + i] = rv[i];
+            xv[i] += alpha * pv[i];
+            rv[i] -= alpha * av[i];
         }
+        store_vec<d, T>(x + u * d, xv);
+        store_vec<d, T>(r + u * d, rv);
         apply_dinv<d, T>(dinv, u, rv, zv);
+        store_vec<d, T>(z + u * d, zv);
 #pragma unroll
         for (int i = 0; i < d; ++i)
         {
-            z[u * d + i] = zv[i];
             part0 += rv[i] * zv[i];
             part1 += rv[i] * rv[i];
         }
@@ -547,7 +597,7 @@ static tad_status ensure_pcg_graph(Problem& P, T* xs, T* r, T* z, T* p, T* Ap, T
     TAD_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     for (int it = 0; it < PCG_CHUNK; ++it)
     {
-        launch_pcg_spmv<d, T>(s, nh, P.bptr, P.bcol, H, z, p, Ap, P.partials, P.counters + 1, P.ds);
+        launch_pcg_spmv<d, T>(s, sell_view(P, H), nh, P.bptr, P.bcol, H, z, p, Ap, P.partials, P.counters + 1, P.ds);
         k_pcg_update<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, xs, r, z, p, Ap, dinv, P.partials, P.counters + 2, P.ds);
     }
     TAD_CUDA_TRY(cudaStreamEndCapture(s, &graph));
@@ -577,7 +627,7 @@ static tad_status ensure_amg_graph(Problem& P, T* xs, T* r, T* z, T* p, T* Ap, i
     TAD_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     for (int it = 0; it < AMG_CHUNK; ++it)
     {
-        launch_pcg_spmv<d, T>(s, P.n_handles, P.bptr, P.bcol, H, z, p, Ap, P.partials, P.counters + 1, P.ds);
+        launch_pcg_spmv<d, T>(s, sell_view(P, H), P.n_handles, P.bptr, P.bcol, H, z, p, Ap, P.partials, P.counters + 1, P.ds);
         P.n_launches += 1;
         amg_apply(P, prec, 1, xs, r, z, p, Ap);
     }
@@ -669,7 +719,7 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
     // V-cycle: 10-20).  An FP32 solve (mixed precision) whose V-cycles break
     // down or stall falls back to block Jacobi alone, from zero.
     auto launch_iteration = [&]() {
-        launch_pcg_spmv<d, T>(s, nh, P.bptr, P.bcol, H, z, p, Ap, P.partials, P.counters + 1, P.ds);
+        launch_pcg_spmv<d, T>(s, sell_view(P, H), nh, P.bptr, P.bcol, H, z, p, Ap, P.partials, P.counters + 1, P.ds);
         k_pcg_update<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(nh, xs, r, z, p, Ap, dinv, P.partials, P.counters + 2, P.ds);
     };
     int replays = 0;
@@ -876,7 +926,8 @@ tad_status prepare_solver_graphs(Problem& P)
 
 /* H += w I on the assembled diagonal blocks */
 template <int d, typename T>
-__global__ void k_add_diag(int64_t nh, const int32_t* __restrict__ diag, T* __restrict__ H, double w)
+__global__ void k_add_diag(int64_t nh, const int32_t* __restrict__ diag, T* __restrict__ H, double w,
+                           const int32_t* __restrict__ sdiag, T* __restrict__ Hs)
 {
     GRID_STRIDE(u, nh)
     {
@@ -884,6 +935,9 @@ __global__ void k_add_diag(int64_t nh, const int32_t* __restrict__ diag, T* __re
         if (b < 0) continue;
 #pragma unroll
         for (int i = 0; i < d; ++i) H[(int64_t)b * d * d + i * d + i] += (T)w;
+        if (Hs)
+#pragma unroll
+            for (int i = 0; i < d; ++i) Hs[(int64_t)sdiag[u] * d * d + i * d + i] += (T)w;   // the sliced-ELL copy too
     }
 }
 
@@ -892,12 +946,12 @@ void add_identity(Problem& P, double w, int precision)
     const bool fp32 = precision == TAD_PREC_MIXED;
     switch (P.d)
     {
-    case 1: fp32 ? k_add_diag<1, float><<<RED_BLOCKS, RED_THREADS, 0, P.stream>>>(P.n_handles, P.diag, (float*)P.H, w)
-                 : k_add_diag<1, double><<<RED_BLOCKS, RED_THREADS, 0, P.stream>>>(P.n_handles, P.diag, (double*)P.H, w); break;
-    case 2: fp32 ? k_add_diag<2, float><<<RED_BLOCKS, RED_THREADS, 0, P.stream>>>(P.n_handles, P.diag, (float*)P.H, w)
-                 : k_add_diag<2, double><<<RED_BLOCKS, RED_THREADS, 0, P.stream>>>(P.n_handles, P.diag, (double*)P.H, w); break;
-    default: fp32 ? k_add_diag<3, float><<<RED_BLOCKS, RED_THREADS, 0, P.stream>>>(P.n_handles, P.diag, (float*)P.H, w)
-                  : k_add_diag<3, double><<<RED_BLOCKS, RED_THREADS, 0, P.stream>>>(P.n_handles, P.diag, (double*)P.H, w); break;
+    case 1: fp32 ? k_add_diag<1, float><<<RED_BLOCKS, RED_THREADS, 0, P.stream>>>(P.n_handles, P.diag, (float*)P.H, w, P.sdiag, (float*)P.Hs)
+                 : k_add_diag<1, double><<<RED_BLOCKS, RED_THREADS, 0, P.stream>>>(P.n_handles, P.diag, (double*)P.H, w, P.sdiag, (double*)P.Hs); break;
+    case 2: fp32 ? k_add_diag<2, float><<<RED_BLOCKS, RED_THREADS, 0, P.stream>>>(P.n_handles, P.diag, (float*)P.H, w, P.sdiag, (float*)P.Hs)
+                 : k_add_diag<2, double><<<RED_BLOCKS, RED_THREADS, 0, P.stream>>>(P.n_handles, P.diag, (double*)P.H, w, P.sdiag, (double*)P.Hs); break;
+    default: fp32 ? k_add_diag<3, float><<<RED_BLOCKS, RED_THREADS, 0, P.stream>>>(P.n_handles, P.diag, (float*)P.H, w, P.sdiag, (float*)P.Hs)
+                  : k_add_diag<3, double><<<RED_BLOCKS, RED_THREADS, 0, P.stream>>>(P.n_handles, P.diag, (double*)P.H, w, P.sdiag, (double*)P.Hs); break;
     }
     P.n_launches += 1;
 }
@@ -1537,7 +1591,7 @@ TAD_API tad_status tad_profile_kernels(tad_problem* P, const double* x_d, int re
         k_pcg_init<D, float><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.rhs, Q.dx32, Q.r32, Q.z32, Q.p32, Q.Ap32,    \
                                                                  Q.dinv32, Q.diag, (const float*)Q.H, 0.0,         \
                                                                  Q.partials, Q.counters, Q.ds, 1e-30, 1 << 30);    \
-        ms5[2] = timed([&] { launch_pcg_spmv<D, float>(st, nh, Q.bptr, Q.bcol, (const float*)Q.H, Q.z32, Q.p32,     \
+        ms5[2] = timed([&] { launch_pcg_spmv<D, float>(st, sell_view(Q, (const float*)Q.H), nh, Q.bptr, Q.bcol, (const float*)Q.H, Q.z32, Q.p32,     \
                                                        Q.Ap32, Q.partials, Q.counters + 1, Q.ds); });                 \
         ms5[3] = timed([&] { k_pcg_update<D, float><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.dx32, Q.r32, Q.z32,  \
                                Q.p32, Q.Ap32, Q.dinv32, Q.partials, Q.counters + 2, Q.ds); });                       \
@@ -1547,7 +1601,7 @@ TAD_API tad_status tad_profile_kernels(tad_problem* P, const double* x_d, int re
         k_pcg_init<D, double><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.rhs, Q.dx, Q.r, Q.z, Q.p, Q.Ap, Q.dinv,     \
                                                                   Q.diag, (const double*)Q.H, 0.0,                  \
                                                                   Q.partials, Q.counters, Q.ds, 1e-30, 1 << 30);    \
-        ms5[2] = timed([&] { launch_pcg_spmv<D, double>(st, nh, Q.bptr, Q.bcol, (const double*)Q.H, Q.z, Q.p, Q.Ap, \
+        ms5[2] = timed([&] { launch_pcg_spmv<D, double>(st, sell_view(Q, (const double*)Q.H), nh, Q.bptr, Q.bcol, (const double*)Q.H, Q.z, Q.p, Q.Ap, \
                                                         Q.partials, Q.counters + 1, Q.ds); });                        \
         ms5[3] = timed([&] { k_pcg_update<D, double><<<RED_BLOCKS, RED_THREADS, 0, st>>>(nh, Q.dx, Q.r, Q.z,       \
                                Q.p, Q.Ap, Q.dinv, Q.partials, Q.counters + 2, Q.ds); });                             \
