@@ -687,7 +687,10 @@ def main():
     share = {"spmv": stage["pcg_iters"] * prof["spmv"] / ms, "pcg_update": stage["pcg_iters"] * prof["pcg_update"] / ms,
              "elem_hessian": args.steps * prof["elem_hessian"] / ms, "assemble": args.steps * prof["assemble"] / ms}
     traffic = TRAFFIC_FROM_CAPTURE.get((args.workload, args.precision), {})
-    roof_spmv = {"bound": "hbm", "kernel": "k_pcg_spmv_fused (BSR SpMV + p update + p.Ap)", "achieved": spmv_gbs,
+    timing_note = "CUDA events around a captured CUDA graph of the kernel's launches, as the solver runs them"
+    spmv_name = ("k_pcg_spmv_sell (sliced-ELL SpMV + p update + p.Ap)" if w.var_dim == 3
+                 else "k_pcg_spmv_fused (BSR SpMV + p update + p.Ap)")
+    roof_spmv = {"bound": "hbm", "kernel": spmv_name, "achieved": spmv_gbs, "timing": timing_note,
                  "peak": hbm, "unit": "GB/s", "frac": spmv_gbs / hbm, "traffic": traffic.get("spmv"),
                  "traffic_source": TRAFFIC_SOURCE if traffic.get("spmv") else None,
                  "peak_source": f"{hbm_src} copy bandwidth (MEASURED_PEAKS.json hbm_gbs)",
@@ -696,8 +699,11 @@ def main():
     k_elem = w.var_dim * w.terms[0].valence
     elem_flops = ELEM_FLOPS.get(k_elem, 0) * w.terms[0].handles.shape[0]
     elem_tf = elem_flops / (prof["elem_hessian"] * 1e-3) / 1e12
+    elem_name = ("k_elem_grad_lanes + k_elem_hess_lanes + k_project_blocks (lane-split Double<k> evaluation + "
+                 "PSD projection)" if (k_elem == 12 and prec == tad.PREC_MIXED)
+                 else "k_elem_hessian + k_project_blocks (Double<k> evaluation + PSD projection)")
     roof_elem = {"bound": "fp32 CUDA-core pipe" if prec == tad.PREC_MIXED else "fp64 CUDA-core pipe",
-                 "kernel": "k_elem_hessian + k_project_blocks (Double<k> evaluation + PSD projection)", "achieved": elem_tf,
+                 "kernel": elem_name, "achieved": elem_tf, "timing": timing_note,
                  "peak": fp_peak, "unit": "TFLOP/s", "frac": elem_tf / fp_peak, "traffic": traffic.get("elem"),
                  "traffic_unit": "bytes per launch", "traffic_source": TRAFFIC_SOURCE if traffic.get("elem") else None,
                  "flops_source": "op counting of the library's arithmetic (oracle/flop_count.sh), not a counter",

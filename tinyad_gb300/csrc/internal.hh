@@ -120,6 +120,8 @@ struct Problem
 {
     std::vector<AmgLevel> amg;       // smoothed-aggregation AMG hierarchy (pattern built at finalisation)
     int64_t amg_solves = 0;          // solves that used it (statistics)
+    bool amg_sticky = false;         // the last solve needed the V-cycle: the next one switches after its first iteration
+    bool in_newton = false;          // solves of the Newton loop (the only ones that use amg_sticky)
     bool amg_values_ready = false;   // values computed for the current H
 
     int kind = 0;                    // 0: empty, 1: scalar terms, 2: vector terms (sum of squares)

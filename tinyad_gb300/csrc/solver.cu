@@ -747,12 +747,17 @@ static tad_status pcg_core(Problem& P, const double* b, T* xs, double w, double 
             TAD_CUDA_TRY(cudaMemcpyAsync(P.hs, P.ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
             TAD_CUDA_TRY(cudaStreamSynchronize(s));
         }
-        if (P.hs->done) break;
-        const bool slow = replays == 1;   // not done after 1 + PCG_CHUNK iterations
+        if (P.hs->done) { if (allow_amg) P.amg_sticky = false; break; }
+        // not done after 1 + PCG_CHUNK iterations -- or after the first, when
+        // the previous solve needed the V-cycle: the hard Newton steps of a
+        // solve come in a run (the late ones), and each spent PCG_CHUNK
+        // block-Jacobi iterations before switching
+        const bool slow = replays == 1 || (replays == 0 && P.amg_sticky && P.in_newton);
         // (a problem at or below the coarsest AMG size is one level: its
         // "V-cycle" would be the coarse smoother alone, so block Jacobi goes on)
         if (allow_amg && slow && P.settings.preconditioner == 1 && w == 0.0 && P.amg.size() > 1)
         {
+            P.amg_sticky = true;
             // block Jacobi's fast start (the high frequencies) is over and the
             // tolerance is not met: continue from this iterate under the V-cycle
             const tad_status sa = pcg_core_amg<d, T>(P, xs, iters_out, r, z, p, Ap, prec);
@@ -1193,12 +1198,19 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
             continues = *P.diff_flag_h == 0;
         }
         P.streak = continues ? P.streak + 1 : 0;
+        if (!continues) P.amg_sticky = false;   // a new solve: its PCG history starts here
     }
     double* cur = x;
     double* spare = P.x_trial;
     bool have_derivs = predicted;   // derivatives at cur already assembled (accepted speculative step)
     bool early_out = false;         // a copy of spare to x_out_h was issued on the side stream
     double* early_buf = nullptr;
+    struct NewtonScope
+    {
+        Problem& P;
+        ~NewtonScope() { P.in_newton = false; }
+    } newton_scope{P};
+    P.in_newton = true;
     auto finish = [&](tad_status rs) {
         if (!input_issued)
         {
@@ -1381,6 +1393,7 @@ tad_status newton_solve(Problem& P, double* x, int n_iters, double eps, double s
             {
                 // x changed: everything above used derivatives of another state
                 P.streak = 0;
+                P.amg_sticky = false;   // a new solve: its PCG history starts here
                 have_derivs = false;
                 speculate = true;
                 --it;
@@ -1573,13 +1586,31 @@ TAD_API tad_status tad_profile_kernels(tad_problem* P, const double* x_d, int re
     k_neg<<<RED_BLOCKS, RED_THREADS, 0, st>>>(Q.n_vars, Q.g, Q.rhs);
     cudaEvent_t e0 = Q.ev[5], e1 = Q.ev[6];
     float ms = 0.f;
+    // each kernel is timed as the solver runs it: reps launches captured in one
+    // CUDA graph and replayed (the PCG's iterations run from captured graphs),
+    // so the figure is the kernels' own time plus the graph's launch spacing;
+    // launched from the host one by one they would add the launch latency
     auto timed = [&](auto&& launch) -> double {
         launch();   // warm
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t ge = nullptr;
+        bool graph_ok = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+        if (graph_ok)
+        {
+            for (int r = 0; r < reps; ++r) launch();
+            graph_ok = cudaStreamEndCapture(st, &g) == cudaSuccess && cudaGraphInstantiate(&ge, g, 0) == cudaSuccess;
+            if (graph_ok) graph_ok = cudaGraphLaunch(ge, st) == cudaSuccess;   // warm the graph
+        }
+        cudaGetLastError();
         cudaEventRecord(e0, st);
-        for (int r = 0; r < reps; ++r) launch();
+        if (graph_ok) cudaGraphLaunch(ge, st);
+        else
+            for (int r = 0; r < reps; ++r) launch();
         cudaEventRecord(e1, st);
         cudaEventSynchronize(e1);
         cudaEventElapsedTime(&ms, e0, e1);
+        if (ge) cudaGraphExecDestroy(ge);
+        if (g) cudaGraphDestroy(g);
         return (double)ms / reps;
     };
     ms5[0] = timed([&] { eval_elements(Q, TAD_MODE_HESSIAN_PROJ, x_d, 1e-9, prec); });
