@@ -526,12 +526,22 @@ __device__ __forceinline__ int32_t find_slot(const int32_t* col, int32_t m, int3
     return (m > 0 && col[b] == key) ? b : -1;
 }
 
+/* groups per warp of k_amg_galerkin (each with its own accumulators in
+   shared memory): 4 for blocks of up to 16 bytes, 2 up to 36, else 1 */
+template <int d, typename T> struct GalerkinGroups
+{
+    static constexpr int value = (d * d * (int)sizeof(T) <= 16) ? 4 : (d * d * (int)sizeof(T) <= 36) ? 2 : 1;
+};
+
 /* A_c = P^T Q, one warp per coarse row I (rows of at most AMG_ROW_CAP
-   blocks): the row's accumulators live in shared memory; for each
-   (u, P(u, I)) in fine row order the lanes take the blocks Q(u, J) of row u,
-   whose columns are distinct, so each accumulator receives at most one
-   product per u and the sums run in the same fixed order as one thread
-   would run them (no atomics) */
+   blocks).  The warp is split into G groups; group g takes the pairs
+   (u, P(u, I)) number g, g + G, ... of the row's list, and its lanes take the
+   blocks Q(u, J) of row u, whose columns are distinct, into the group's own
+   accumulators in shared memory -- so no two lanes add into one accumulator
+   at once, and each accumulator sums its pairs in list order.  The G partial
+   rows are added in group order at the end: a fixed order, no atomics.  (One
+   group of 32 lanes left most lanes idle on rows of 7-12 Q blocks and walked
+   the list's dependent loads one pair at a time.) */
 template <int d, typename T>
 __global__ void __launch_bounds__(AMG_SETUP_WARPS * 32) k_amg_galerkin(int64_t nc, const int32_t* __restrict__ tptr,
                                                                        const int32_t* __restrict__ tu,
@@ -541,47 +551,57 @@ __global__ void __launch_bounds__(AMG_SETUP_WARPS * 32) k_amg_galerkin(int64_t n
                                                                        const T* __restrict__ Qv, const int32_t* __restrict__ cptr,
                                                                        const int32_t* __restrict__ ccol, T* __restrict__ Ac)
 {
-    __shared__ T acc_s[AMG_SETUP_WARPS][AMG_ROW_CAP * d * d];
+    constexpr int G = GalerkinGroups<d, T>::value, LG = 32 / G;
+    __shared__ T acc_s[AMG_SETUP_WARPS][G][AMG_ROW_CAP * d * d];
     __shared__ int32_t col_s[AMG_SETUP_WARPS][AMG_ROW_CAP];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    T* acc = acc_s[w];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane / LG, gl = lane % LG;
     int32_t* col = col_s[w];
+    T* acc = acc_s[w][g];
     for (int64_t I = blockIdx.x * (int64_t)AMG_SETUP_WARPS + w; I < nc; I += (int64_t)gridDim.x * AMG_SETUP_WARPS)
     {
         const int32_t c0 = cptr[I], m = cptr[I + 1] - c0;
-        for (int32_t k = lane; k < m; k += 32)
-        {
-            col[k] = ccol[c0 + k];
+        for (int32_t k = lane; k < m; k += 32) col[k] = ccol[c0 + k];
+        for (int32_t k = gl; k < m; k += LG)
 #pragma unroll
             for (int i = 0; i < d * d; ++i) acc[k * d * d + i] = T(0);
-        }
         __syncwarp();
-        for (int32_t t = tptr[I]; t < tptr[I + 1]; ++t)
+        const int32_t t_end = tptr[I + 1];
+        for (int32_t tb = tptr[I]; tb < t_end; tb += G)
         {
-            const int32_t u = tu[t];
-            T Pt[d * d];
+            const int32_t t = tb + g;
+            if (t < t_end)
             {
-                T Pb[d * d];
-                load_block<d, T>(Pv + (int64_t)tp[t] * d * d, Pb);
+                const int32_t u = tu[t];
+                T Pt[d * d];
+                {
+                    T Pb[d * d];
+                    load_block<d, T>(Pv + (int64_t)tp[t] * d * d, Pb);
 #pragma unroll
-                for (int i = 0; i < d; ++i)
+                    for (int i = 0; i < d; ++i)
 #pragma unroll
-                    for (int j = 0; j < d; ++j) Pt[i * d + j] = Pb[j * d + i];
-            }
-            const int32_t q0 = qptr[u], q1 = qptr[u + 1];
-            for (int32_t q = q0 + lane; q < q1; q += 32)
-            {
-                T Qb[d * d];
-                load_block<d, T>(Qv + (int64_t)q * d * d, Qb);
-                const int32_t sl = find_slot(col, m, qcol[q]);
-                if (sl >= 0) mat_mul_acc<d, T>(Pt, Qb, acc + sl * d * d);
+                        for (int j = 0; j < d; ++j) Pt[i * d + j] = Pb[j * d + i];
+                }
+                const int32_t q1 = qptr[u + 1];
+                for (int32_t q = qptr[u] + gl; q < q1; q += LG)
+                {
+                    T Qb[d * d];
+                    load_block<d, T>(Qv + (int64_t)q * d * d, Qb);
+                    const int32_t sl = find_slot(col, m, qcol[q]);
+                    if (sl >= 0) mat_mul_acc<d, T>(Pt, Qb, acc + sl * d * d);
+                }
             }
             __syncwarp();
         }
         for (int32_t k = lane; k < m; k += 32)
         {
 #pragma unroll
-            for (int i = 0; i < d * d; ++i) Ac[(int64_t)(c0 + k) * d * d + i] = acc[k * d * d + i];
+            for (int i = 0; i < d * d; ++i)
+            {
+                T v = acc_s[w][0][k * d * d + i];
+#pragma unroll
+                for (int h = 1; h < G; ++h) v += acc_s[w][h][k * d * d + i];
+                Ac[(int64_t)(c0 + k) * d * d + i] = v;
+            }
         }
         __syncwarp();
     }
