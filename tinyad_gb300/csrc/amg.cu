@@ -64,6 +64,9 @@ constexpr double AMG_PROLONG_OMEGA = 1.8;
    shared memory: rows up to this many blocks (longer: a thread per row) */
 constexpr int AMG_ROW_CAP = 96;
 constexpr int AMG_SETUP_WARPS = 4;   // warps per block of the setup kernels
+/* prolongator rows of at most this many blocks are summed in registers (2D
+   rows have up to ~9; 3D rows 10-30, which keep the memory path) */
+template <int d> struct ProlongRegs { static constexpr int value = d <= 2 ? 8 : 1; };
 
 /* ---- host: aggregation and the patterns of P, Q, A_c ----------------------- */
 namespace {
@@ -438,9 +441,52 @@ __global__ void k_amg_prolongator(int64_t n, const int32_t* __restrict__ bptr, c
                                   const T* __restrict__ A, const T* __restrict__ dl1, T* __restrict__ Pv)
 {
     const T omega = (T)AMG_PROLONG_OMEGA;
+    constexpr int R = ProlongRegs<d>::value;
     GRID_STRIDE(u, n)
     {
         const int32_t p0 = pptr[u], p1 = pptr[u + 1];
+        if (p1 - p0 <= R)
+        {
+            // the row's (A S-weighted) sums in registers: S[k] = sum of the A blocks
+            // feeding P block p0 + k, in row order (the slot picked by a compare
+            // chain, not a register index)
+            T S[R][d * d];
+#pragma unroll
+            for (int k = 0; k < R; ++k)
+#pragma unroll
+                for (int i = 0; i < d * d; ++i) S[k][i] = T(0);
+            for (int32_t q = bptr[u]; q < bptr[u + 1]; ++q)
+            {
+                T B[d * d];
+                load_block<d, T>(A + (int64_t)q * d * d, B);
+                const int32_t k = pslot[q] - p0;
+#pragma unroll
+                for (int kk = 0; kk < R; ++kk)
+                    if (kk == k)
+#pragma unroll
+                        for (int i = 0; i < d * d; ++i) S[kk][i] += B[i];
+            }
+            T Di[d * d];
+            load_block<d, T>(dl1 + u * d * d, Di);
+            const int32_t pd = pdiag[u];
+#pragma unroll
+            for (int kk = 0; kk < R; ++kk)
+            {
+                const int32_t p = p0 + kk;
+                if (p >= p1) break;
+                const T c = (T)cscale[pcol[p]];
+                T O[d * d];
+#pragma unroll
+                for (int i = 0; i < d * d; ++i) O[i] = T(0);
+                mat_mul_acc<d, T>(Di, S[kk], O);
+#pragma unroll
+                for (int i = 0; i < d; ++i)
+#pragma unroll
+                    for (int j = 0; j < d; ++j)
+                        Pv[(int64_t)p * d * d + i * d + j] = ((p == pd && i == j) ? c : T(0)) - omega * c * O[i * d + j];
+            }
+            continue;
+        }
         for (int64_t i = (int64_t)p0 * d * d; i < (int64_t)p1 * d * d; ++i) Pv[i] = T(0);
         for (int32_t q = bptr[u]; q < bptr[u + 1]; ++q)
         {
@@ -652,7 +698,7 @@ __global__ void k_amg_residual(int64_t n, const int32_t* __restrict__ bptr, cons
     GRID_STRIDE(u, n)
     {
         T y[d];
-        bsr_row_product<d, T>(bptr, bcol, A, x, u, y);
+        bsr_row_product4<d, T>(bptr, bcol, A, x, u, y);
 #pragma unroll
         for (int i = 0; i < d; ++i) res[u * d + i] = r[u * d + i] - y[i];
     }

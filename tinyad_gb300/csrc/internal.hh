@@ -37,6 +37,18 @@ constexpr int RED_BLOCKS = 608;    // 4 x 152 SMs: fixed grid of the reductions
    reduction grid: measured faster there) */
 constexpr int PCG_BLOCKS = 1216;
 constexpr int RED_THREADS = 256;
+/* blocks of a kernel resident on the device at once (threads per block,
+   static shared memory), for grid-stride kernels that should run as one
+   wave; the caller computes it once per kernel */
+template <typename K>
+inline unsigned resident_grid(K kernel, int threads)
+{
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, 0);
+    return (unsigned)(per > 0 ? per : 1) * (unsigned)(sms > 0 ? sms : 1);
+}
 /* mixed-precision solves at least this loose are one FP32 PCG pass, with no
    FP64 refinement */
 constexpr double MIXED_LOOSE_TOL = 1e-4;

@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_spmv_fused(int64_t nh, cons
     GRID_STRIDE(u, nh)
     {
         T y[d];
-        bsr_row_product<d, T>(bptr, bcol, H, z, u, y);
+        bsr_row_product4<d, T>(bptr, bcol, H, z, u, y);
 #pragma unroll
         for (int i = 0; i < d; ++i)
         {
@@ -320,8 +320,13 @@ inline void launch_pcg_spmv(cudaStream_t s, const SellView& sv, int64_t nh, cons
     else if constexpr (d == 3)
         k_pcg_spmv_vec<d, T, 8><<<PCG_BLOCKS, RED_THREADS, 0, s>>>(nh, bptr, bcol, H, z, p, Ap, partials, counter, ds);
     else
-        k_pcg_spmv_fused<d, T, SpmvGroup<d>::value><<<PCG_BLOCKS, RED_THREADS, 0, s>>>(nh, bptr, bcol, H, z, p, Ap, partials,
-                                                                                  counter, ds);
+    {
+        // one wave of resident blocks (the grid-stride loop takes the rest)
+        static const unsigned grid = std::min<unsigned>(PCG_BLOCKS, resident_grid(k_pcg_spmv_fused<d, T, SpmvGroup<d>::value>,
+                                                                                   RED_THREADS));
+        k_pcg_spmv_fused<d, T, SpmvGroup<d>::value><<<grid, RED_THREADS, 0, s>>>(nh, bptr, bcol, H, z, p, Ap, partials,
+                                                                            counter, ds);
+    }
 }
 
 template <int d, typename T>
