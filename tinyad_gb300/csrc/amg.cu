@@ -32,7 +32,8 @@
  *   res = r - A x                   (k_amg_residual)
  *   r_c = P^T res, x_c = S_c r_c    (k_amg_restrict, one thread per coarse row)
  *   x_c <- V-cycle of the next level
- *   x += P x_c + S (res - Q x_c)    (k_amg_post: prolongation and
+ *   x += P x_c + S (res - Q x_c)    (k_amg_post, as x += R x_c + S res with
+ *                                    R = P - S Q formed with Q: prolongation and
  *                                    post-smoothing in one pass, since
  *                                    r - A (x + P x_c) = res - Q x_c)
  * and on the coarsest level (<= AMG_COARSE_ROWS block rows) AMG_COARSE_SWEEPS
@@ -84,6 +85,7 @@ struct HostLevel
     std::vector<int32_t> pdiag;              // per fine row: its P block in column agg(u)
     std::vector<int32_t> qptr, qcol;         // Q = A_l P
     std::vector<int32_t> qlptr, qla, qlp;    // per Q block: its (A block, P block) products
+    std::vector<int32_t> qrow, qpb;          // per Q block: its row, and the P block at its position (-1: none)
     std::vector<int32_t> tptr, tu, tp;       // per aggregate: (fine row, P block) with P(u, I) != 0, by u
 };
 
@@ -182,6 +184,16 @@ void transfer(HostLevel& F, HostLevel& C)
             out.insert(out.end(), F.pcol.begin() + F.pptr[v], F.pcol.begin() + F.pptr[v + 1]);
         }
     });
+    // per Q block: its row and the P block at the same (row, column), for R = P - S Q
+    F.qrow.resize(F.qcol.size());
+    F.qpb.resize(F.qcol.size());
+#pragma omp parallel for schedule(static)
+    for (int64_t u = 0; u < n; ++u)
+        for (int32_t b = F.qptr[u]; b < F.qptr[u + 1]; ++b)
+        {
+            F.qrow[b] = (int32_t)u;
+            F.qpb[b] = find_in(F.pcol, F.pptr[u], F.pptr[u + 1], F.qcol[b]);
+        }
     // the products of each Q block: (A block, P block) pairs in row order of A, then of P
     {
         std::vector<int32_t> cnt(F.qcol.size() + 1, 0);
@@ -265,7 +277,7 @@ void amg_free(Problem& P)
                 if (q) cudaFree(q);
         for (void* q : {(void*)L.pptr, (void*)L.pcol, (void*)L.pslot, (void*)L.pdiag, (void*)L.qptr, (void*)L.qcol,
                         (void*)L.tptr, (void*)L.tu, (void*)L.tp, (void*)L.cscale, (void*)L.qlptr, (void*)L.qla,
-                        (void*)L.qlp, L.Pv, L.Qv, L.dl1, L.r, L.x, L.res, L.w})
+                        (void*)L.qlp, (void*)L.qrow, (void*)L.qpb, L.Pv, L.Qv, L.Rv, L.dl1, L.r, L.x, L.res, L.w})
             if (q) cudaFree(q);
     }
     P.amg.clear();
@@ -331,9 +343,11 @@ tad_status amg_build(Problem& P)
                 upload(&L.tptr, h.tptr) != cudaSuccess || upload(&L.tu, h.tu) != cudaSuccess ||
                 upload(&L.tp, h.tp) != cudaSuccess || upload(&L.cscale, h.cscale) != cudaSuccess ||
                 upload(&L.qlptr, h.qlptr) != cudaSuccess || upload(&L.qla, h.qla) != cudaSuccess ||
-                upload(&L.qlp, h.qlp) != cudaSuccess ||
+                upload(&L.qlp, h.qlp) != cudaSuccess || upload(&L.qrow, h.qrow) != cudaSuccess ||
+                upload(&L.qpb, h.qpb) != cudaSuccess ||
                 cudaMalloc(&L.Pv, std::max<int64_t>(L.np, 1) * bs) != cudaSuccess ||
-                cudaMalloc(&L.Qv, std::max<int64_t>(L.nq, 1) * bs) != cudaSuccess)
+                cudaMalloc(&L.Qv, std::max<int64_t>(L.nq, 1) * bs) != cudaSuccess ||
+                cudaMalloc(&L.Rv, std::max<int64_t>(L.nq, 1) * bs) != cudaSuccess)
                 return fail();
         }
     }
@@ -531,10 +545,17 @@ __device__ __forceinline__ int32_t find_col(const int32_t* __restrict__ col, int
 }
 
 /* Q = A P, one thread per Q block: the sum of its (A block, P block)
-   products in the list's fixed order */
+   products in the list's fixed order; and R = P - S Q on the same block
+   (S the l1 inverse of the block's row; P's block at that position where P
+   has one -- its row pattern lies in Q's for every row with a diagonal block,
+   and a row without one is a variable no element uses, whose residual stays
+   zero), the post-smoothing's operator: x += P x_c + S (res - Q x_c) is
+   x += R x_c + S res, one row product instead of two in every V-cycle */
 template <int d, typename T>
 __global__ void k_amg_q(int64_t nq, const int32_t* __restrict__ qlptr, const int32_t* __restrict__ qla,
-                        const int32_t* __restrict__ qlp, const T* __restrict__ A, const T* __restrict__ Pv, T* __restrict__ Qv)
+                        const int32_t* __restrict__ qlp, const int32_t* __restrict__ qrow, const int32_t* __restrict__ qpb,
+                        const T* __restrict__ A, const T* __restrict__ Pv, const T* __restrict__ dl1, T* __restrict__ Qv,
+                        T* __restrict__ Rv)
 {
     GRID_STRIDE(b, nq)
     {
@@ -549,12 +570,28 @@ __global__ void k_amg_q(int64_t nq, const int32_t* __restrict__ qlptr, const int
             load_block<d, T>(Pv + (int64_t)__ldg(qlp + k) * d * d, Pb);
             mat_mul_acc<d, T>(B, Pb, acc);
         }
+        T S[d * d], R[d * d];
+        load_block<d, T>(dl1 + (int64_t)qrow[b] * d * d, S);
+        const int32_t pb = qpb[b];
+        if (pb >= 0) load_block<d, T>(Pv + (int64_t)pb * d * d, R);
+        else
+#pragma unroll
+            for (int i = 0; i < d * d; ++i) R[i] = T(0);
+        T O[d * d];
+#pragma unroll
+        for (int i = 0; i < d * d; ++i) O[i] = T(0);
+        mat_mul_acc<d, T>(S, acc, O);
+#pragma unroll
+        for (int i = 0; i < d * d; ++i) R[i] -= O[i];
         if constexpr (d == 2 && sizeof(T) == 4)
+        {
             reinterpret_cast<float4*>(Qv)[b] = make_float4(acc[0], acc[1], acc[2], acc[3]);
+            reinterpret_cast<float4*>(Rv)[b] = make_float4(R[0], R[1], R[2], R[3]);
+        }
         else
         {
 #pragma unroll
-            for (int i = 0; i < d * d; ++i) Qv[b * d * d + i] = acc[i];
+            for (int i = 0; i < d * d; ++i) { Qv[b * d * d + i] = acc[i]; Rv[b * d * d + i] = R[i]; }
         }
     }
 }
@@ -763,35 +800,33 @@ __global__ void k_amg_restrict(int64_t nc, const int32_t* __restrict__ tptr, con
     }
 }
 
-/* x += P x_c + S (res - Q x_c); top level (rz != NULL): also the PCG's r.z
-   reduction, beta = r.z / rz_old (first: 0) and the breakdown test */
+/* x += P x_c + S (res - Q x_c) = R x_c + S res (R = P - S Q, k_amg_q); top
+   level (rz != NULL): also the PCG's r.z reduction, beta = r.z / rz_old
+   (first: 0) and the breakdown test */
 template <int d, typename T>
-__global__ void __launch_bounds__(RED_THREADS) k_amg_post(int64_t n, const int32_t* __restrict__ pptr,
-                                                          const int32_t* __restrict__ pcol, const T* __restrict__ Pv,
-                                                          const int32_t* __restrict__ qptr, const int32_t* __restrict__ qcol,
-                                                          const T* __restrict__ Qv, const T* __restrict__ dl1,
-                                                          const T* __restrict__ xc, const T* __restrict__ res,
-                                                          T* __restrict__ x, const T* __restrict__ r, double* partials,
-                                                          unsigned* counter, DevScalars* ds, int first)
+__global__ void __launch_bounds__(RED_THREADS) k_amg_post(int64_t n, const int32_t* __restrict__ qptr,
+                                                          const int32_t* __restrict__ qcol, const T* __restrict__ Rv,
+                                                          const T* __restrict__ dl1, const T* __restrict__ xc,
+                                                          const T* __restrict__ res, T* __restrict__ x, const T* __restrict__ r,
+                                                          double* partials, unsigned* counter, DevScalars* ds, int first)
 {
     AMG_STOP;
     T part = T(0);
     GRID_STRIDE(u, n)
     {
-        T px[d], qx[d];
-        bsr_row_product<d, T>(pptr, pcol, Pv, xc, u, px);
-        bsr_row_product<d, T>(qptr, qcol, Qv, xc, u, qx);
-        T e[d], s[d];
-#pragma unroll
-        for (int i = 0; i < d; ++i) e[i] = res[u * d + i] - qx[i];
-        apply_dinv<d, T>(dl1, u, e, s);
+        T rx[d], rv[d], s[d], xv[d];
+        bsr_row_product4<d, T>(qptr, qcol, Rv, xc, u, rx);
+        load_vec<d, T>(res + u * d, rv);
+        apply_dinv<d, T>(dl1, u, rv, s);
+        load_vec<d, T>(x + u * d, xv);
 #pragma unroll
         for (int i = 0; i < d; ++i)
         {
-            const T xn = x[u * d + i] + px[i] + s[i];
-            x[u * d + i] = xn;
+            const T xn = xv[i] + rx[i] + s[i];
+            xv[i] = xn;
             if (r) part += r[u * d + i] * xn;
         }
+        store_vec<d, T>(x + u * d, xv);
     }
     if (!r) return;
     double v[1] = {as_double(part)}, tot[1];
@@ -965,13 +1000,12 @@ static void vcycle_from(Problem& P, size_t l, const T* r, T* x, int first)
     P.n_launches += 2;
     vcycle_from<d, T>(P, l + 1, (const T*)C.r, (T*)C.x, first);
     if (l == 0)
-        k_amg_post<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(L.n, L.pptr, L.pcol, (const T*)L.Pv, L.qptr, L.qcol,
-                                                            (const T*)L.Qv, (const T*)L.dl1, (const T*)C.x,
-                                                            (const T*)L.res, x, r, P.partials, P.counters + 9, P.ds, first);
+        k_amg_post<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(L.n, L.qptr, L.qcol, (const T*)L.Rv, (const T*)L.dl1,
+                                                            (const T*)C.x, (const T*)L.res, x, r, P.partials,
+                                                            P.counters + 9, P.ds, first);
     else
-        k_amg_post<d, T><<<g, RED_THREADS, 0, s>>>(L.n, L.pptr, L.pcol, (const T*)L.Pv, L.qptr, L.qcol, (const T*)L.Qv,
-                                                   (const T*)L.dl1, (const T*)C.x, (const T*)L.res, x, nullptr, nullptr,
-                                                   nullptr, P.ds, first);
+        k_amg_post<d, T><<<g, RED_THREADS, 0, s>>>(L.n, L.qptr, L.qcol, (const T*)L.Rv, (const T*)L.dl1, (const T*)C.x,
+                                                   (const T*)L.res, x, nullptr, nullptr, nullptr, P.ds, first);
     P.n_launches += 1;
 }
 
@@ -1017,7 +1051,8 @@ static void values(Problem& P)
         k_amg_prolongator<d, T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(L.n, L.bptr, L.pslot, L.pptr, L.pcol, L.pdiag,
                                                                    L.cscale, A, (const T*)L.dl1, (T*)L.Pv);
         k_amg_q<d, T><<<(unsigned)std::min<int64_t>(8 * RED_BLOCKS, (L.nq + RED_THREADS - 1) / RED_THREADS + 1), RED_THREADS,
-                        0, s>>>(L.nq, L.qlptr, L.qla, L.qlp, A, (const T*)L.Pv, (T*)L.Qv);
+                        0, s>>>(L.nq, L.qlptr, L.qla, L.qlp, L.qrow, L.qpb, A, (const T*)L.Pv, (const T*)L.dl1, (T*)L.Qv,
+                                (T*)L.Rv);
         P.n_launches += 2;
     }
 }

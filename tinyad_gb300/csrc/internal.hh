@@ -123,9 +123,11 @@ struct AmgLevel
     int32_t *pptr = nullptr, *pcol = nullptr, *pslot = nullptr, *pdiag = nullptr;   // P pattern
     int32_t *qptr = nullptr, *qcol = nullptr;                                     // Q = A P pattern
     int32_t *qlptr = nullptr, *qla = nullptr, *qlp = nullptr;                      // per Q block: (A, P) products
+    int32_t *qrow = nullptr, *qpb = nullptr;                                      // per Q block: its row, its P block (-1)
     int32_t *tptr = nullptr, *tu = nullptr, *tp = nullptr;                        // transposed P lists
     double* cscale = nullptr;                // per aggregate 1 / sqrt(size)
     void *Pv = nullptr, *Qv = nullptr;       // P and Q values
+    void* Rv = nullptr;                      // R = P - S Q on Q's pattern (the post-smoothing's operator)
 };
 
 struct Problem
