@@ -758,39 +758,46 @@ __global__ void k_amg_residual_sell(int64_t n, const int32_t* __restrict__ sptr,
     }
 }
 
-/* r_c(I) = sum_u P(u, I)^T res(u), x_c(I) = S_c(I) r_c(I): one warp per
-   coarse row, lane k taking the k-th, (k+32)-th, ... (u, P(u, I)) pair, then
-   a fixed xor-shuffle tree (deterministic) */
+/* r_c(I) = sum_u P(u, I)^T res(u), x_c(I) = S_c(I) r_c(I): RestrictLanes<d>
+   lanes per coarse row (32 / L rows per warp at once), lane k of a row taking
+   its k-th, (k+L)-th, ... (u, P(u, I)) pair, then a fixed xor-shuffle tree
+   within the row's lanes (deterministic).  Coarse rows have 20-40 pairs on
+   the 2D levels: a warp per row left its dependent gathers one row deep. */
+template <int d> struct RestrictLanes { static constexpr int value = d == 3 ? 16 : 8; };
+
 template <int d, typename T>
 __global__ void k_amg_restrict(int64_t nc, const int32_t* __restrict__ tptr, const int32_t* __restrict__ tu,
                                const int32_t* __restrict__ tp, const T* __restrict__ Pv, const T* __restrict__ res,
                                const T* __restrict__ dl1c, T* __restrict__ rc, T* __restrict__ xc, const DevScalars* ds)
 {
     AMG_STOP;
-    const int lane = threadIdx.x & 31;
+    constexpr int L = RestrictLanes<d>::value, RPW = 32 / L;
+    const int lane = threadIdx.x % L, sub = (threadIdx.x & 31) / L;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t I = warp; I < nc; I += n_warps)
+    for (int64_t base = warp * RPW; base < nc; base += n_warps * RPW)
     {
+        const int64_t I = base + sub;
         T acc[d];
 #pragma unroll
         for (int i = 0; i < d; ++i) acc[i] = T(0);
-        for (int32_t t = tptr[I] + lane; t < tptr[I + 1]; t += 32)
-        {
-            const int64_t u = tu[t];
-            T Pb[d * d], rv[d];
-            load_block<d, T>(Pv + (int64_t)tp[t] * d * d, Pb);
-            load_vec<d, T>(res + u * d, rv);
+        if (I < nc)
+            for (int32_t t = tptr[I] + lane; t < tptr[I + 1]; t += L)
+            {
+                const int64_t u = tu[t];
+                T Pb[d * d], rv[d];
+                load_block<d, T>(Pv + (int64_t)tp[t] * d * d, Pb);
+                load_vec<d, T>(res + u * d, rv);
 #pragma unroll
-            for (int j = 0; j < d; ++j)
+                for (int j = 0; j < d; ++j)
 #pragma unroll
-                for (int i = 0; i < d; ++i) acc[j] += Pb[i * d + j] * rv[i];
-        }
+                    for (int i = 0; i < d; ++i) acc[j] += Pb[i * d + j] * rv[i];
+            }
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1)
+        for (int off = L / 2; off > 0; off >>= 1)
 #pragma unroll
-            for (int i = 0; i < d; ++i) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], off);
-        if (lane == 0)
+            for (int i = 0; i < d; ++i) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], off, L);
+        if (I < nc && lane == 0)
         {
             T z[d];
             apply_dinv<d, T>(dl1c, I, acc, z);
@@ -995,7 +1002,7 @@ static void vcycle_from(Problem& P, size_t l, const T* r, T* x, int first)
         k_amg_residual_sell<d, T><<<g, RED_THREADS, 0, s>>>(L.n, sv.sptr, sv.scol, (const T*)sv.Hs, r, x, (T*)L.res, ds);
     else
         k_amg_residual<d, T><<<g, RED_THREADS, 0, s>>>(L.n, L.bptr, L.bcol, A, r, x, (T*)L.res, ds);
-    k_amg_restrict<d, T><<<warp_grid(C.n), RED_THREADS, 0, s>>>(C.n, L.tptr, L.tu, L.tp, (const T*)L.Pv, (const T*)L.res,
+    k_amg_restrict<d, T><<<warp_grid(C.n, 32 / RestrictLanes<d>::value), RED_THREADS, 0, s>>>(C.n, L.tptr, L.tu, L.tp, (const T*)L.Pv, (const T*)L.res,
                                                                 (const T*)C.dl1, (T*)C.r, (T*)C.x, ds);
     P.n_launches += 2;
     vcycle_from<d, T>(P, l + 1, (const T*)C.r, (T*)C.x, first);
