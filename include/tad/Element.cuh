@@ -105,14 +105,19 @@ struct SubsetElement
     int32_t* err;
     const passive_type* xs;
 
-#if defined(__CUDACC__)
-    __device__ Vec<S, d> variables(int v) const
+    TAD_HD Vec<S, d> variables(int v) const
     {
         int slot = -1;
 #pragma unroll
         for (int i = N - 1; i >= 0; --i)
             if (vh[i] == v) slot = i;
-        if (slot < 0) { report_error(err, DEVERR_UNRECORDED_ACCESS); slot = 0; }
+        if (slot < 0)
+        {
+#if defined(__CUDA_ARCH__)
+            report_error(err, DEVERR_UNRECORDED_ACCESS);
+#endif
+            slot = 0;
+        }
         Vec<S, d> r;
 #pragma unroll
         for (int i = 0; i < d; ++i)
@@ -126,13 +131,32 @@ struct SubsetElement
         }
         return r;
     }
-    __device__ S variable(int v) const
+    TAD_HD S variable(int v) const
     {
         static_assert(d == 1, "element.variable(vh) needs variable dimension 1; use element.variables(vh)");
         return variables(v)[0];
     }
-#endif
 };
+
+/* Index triple of line l (0..11) of the affine plane of order 3, on the 9
+   indices 3u + c (points (u, c), u, c in 0..2): the lines of direction 0 are
+   {3u, 3u+1, 3u+2}; those of slope a = dir - 1 through (0, c) are
+   {(u, c + a u mod 3)}.  Any two points lie on exactly one line, so the 12
+   lines' 3 x 3 principal blocks hold every off-diagonal entry of a 9 x 9
+   matrix once, and the 3 lines of direction 0 hold each diagonal entry once
+   (k_elem_hess_lanes; tests/cpp/lane_split_test.cpp checks both). */
+TAD_HD void plane_line(int l, int (&t)[3])
+{
+    const int dir = l / 3, c = l % 3;
+    if (dir == 0) { t[0] = 3 * c; t[1] = 3 * c + 1; t[2] = 3 * c + 2; }
+    else
+    {
+        const int a = dir - 1;   // slope
+        t[0] = c;
+        t[1] = 3 + (c + a) % 3;
+        t[2] = 6 + (c + 2 * a) % 3;
+    }
+}
 
 template <int d, int N, typename T>
 struct PassiveElement

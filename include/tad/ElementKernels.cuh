@@ -427,20 +427,6 @@ constexpr int HL_ELEMS = 8;    // elements per block of k_elem_hess_lanes (12 la
 constexpr int GL_MIN_BLOCKS = TAD_GL_MINB;
 constexpr int HL_MIN_BLOCKS = TAD_HL_MINB;
 
-/* reduced index triple of line l (0..11) of the affine plane of order 3 */
-__device__ __forceinline__ void plane_line(int l, int (&t)[3])
-{
-    const int dir = l / 3, c = l % 3;
-    if (dir == 0) { t[0] = 3 * c; t[1] = 3 * c + 1; t[2] = 3 * c + 2; }
-    else
-    {
-        const int a = dir - 1;   // slope
-        t[0] = c;
-        t[1] = 3 + (c + a) % 3;
-        t[2] = 6 + (c + 2 * a) % 3;
-    }
-}
-
 template <int d, int N, typename Energy>
 __global__ void __launch_bounds__(3 * GL_ELEMS, GL_MIN_BLOCKS) k_elem_grad_lanes(ElemLaunch L, Energy energy)
 {
