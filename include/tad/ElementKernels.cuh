@@ -604,7 +604,10 @@ template <int d, int N, typename T, typename Energy>
 inline void launch_elements_hessian(const ElemLaunch& L, const Energy& energy, cudaStream_t s)
 {
     if (L.n_elem <= 0) return;
-    constexpr bool deflated = DeflatedProjection<N>::value;
+    // energies that declare translation invariance take the deflated form
+    // without a test, so they never list an element for the general kernel:
+    // neither the list nor that kernel is needed for them
+    constexpr bool deflated = DeflatedProjection<N>::value && !ReducedDerivatives<Energy, N>::value;
     if (deflated && L.project && L.proj_list) cudaMemsetAsync(L.proj_list, 0, sizeof(uint32_t), s);
     if constexpr (LaneHessian<d, N, T, Energy>::value)
     {

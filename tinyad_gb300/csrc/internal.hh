@@ -136,6 +136,7 @@ struct Problem
     int64_t amg_solves = 0;          // solves that used it (statistics)
     bool amg_sticky = false;         // the last solve needed the V-cycle: the next one switches after its first iteration
     bool in_newton = false;          // solves of the Newton loop (the only ones that use amg_sticky)
+    int amg_last_chunks = 0;         // captured V-cycle chunks the last V-cycle solve of the Newton loop needed
     bool amg_values_ready = false;   // values computed for the current H
 
     int kind = 0;                    // 0: empty, 1: scalar terms, 2: vector terms (sum of squares)

@@ -653,6 +653,7 @@ static tad_status ensure_amg_graph(Problem& P, T* xs, T* r, T* z, T* p, T* Ap, i
 template <int d, typename T>
 static tad_status pcg_core_amg(Problem& P, T* xs, int* iters_out, T* r, T* z, T* p, T* Ap, int prec)
 {
+    const int64_t it_switch = P.hs->iters;   // block-Jacobi iterations before the switch
     tad_status st = amg_prepare(P, prec);
     if (st != TAD_OK) return st;
     ++P.amg_solves;
@@ -663,7 +664,14 @@ static tad_status pcg_core_amg(Problem& P, T* xs, int* iters_out, T* r, T* z, T*
     TAD_CUDA_TRY(cudaGetLastError());
     st = ensure_amg_graph<d, T>(P, xs, r, z, p, Ap, prec);
     if (st != TAD_OK) return st;
-    int replays = 1;
+    // Replays between host checks: 1, 2, 4, 4, ... chunks -- or, in the
+    // Newton loop after a V-cycle solve, first as many chunks as that solve
+    // needed, then one at a time.  The iterations a replay runs past
+    // convergence return at once but still cost their launches (a V-cycle
+    // iteration is a dozen kernels); consecutive hard Newton steps need
+    // similar counts.
+    const bool predicted = P.in_newton && P.amg_sticky && P.amg_last_chunks > 0;
+    int replays = predicted ? std::min(8, P.amg_last_chunks) : 1;
     double rr_last = 0.0;
     int slow = 0;
     for (;;)
@@ -686,8 +694,11 @@ static tad_status pcg_core_amg(Problem& P, T* xs, int* iters_out, T* r, T* z, T*
                 return TAD_ERR_PCG_NOCONV;
             }
         }
-        replays = std::min(4, 2 * replays);
+        replays = predicted ? 1 : std::min(4, 2 * replays);
     }
+    // the chunks this solve's iterations filled: the next hard solve's first replay
+    const int64_t vc_iters = std::max<int64_t>(0, P.hs->iters - it_switch);
+    P.amg_last_chunks = P.in_newton ? (int)std::min<int64_t>(8, (vc_iters + AMG_CHUNK - 1) / AMG_CHUNK) : 0;
     if (iters_out) *iters_out = P.hs->iters;
     if (P.hs->breakdown || !(P.hs->rr <= P.hs->tol2)) return TAD_ERR_PCG_NOCONV;
     return TAD_OK;
