@@ -852,7 +852,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_amg_post(int64_t n, const int32
    ...; a fixed xor-shuffle tree sums them): a coarse row of a tetrahedral
    mesh has 30-40 3 x 3 blocks, whose dependent loads one thread per row
    walked in sequence (95 us per call on the 48^3 cube, 12 sweeps). */
-template <int d> struct CoarseLanes { static constexpr int value = d == 3 ? 8 : 4; };
+template <int d> struct CoarseLanes { static constexpr int value = d == 3 ? 16 : 4; };
 
 template <int d, typename T>
 __global__ void __launch_bounds__(AMG_COARSE_THREADS) k_amg_coarse(int64_t n, const int32_t* __restrict__ bptr,
