@@ -417,15 +417,14 @@ template <int d, int N, typename T, typename Energy> struct LaneHessian
 
 constexpr int GL_ELEMS = 32;   // elements per block of k_elem_grad_lanes (3 lanes each)
 constexpr int HL_ELEMS = 8;    // elements per block of k_elem_hess_lanes (12 lanes each)
-/* minimum resident blocks per SM of the two kernels */
-#ifndef TAD_GL_MINB
-#define TAD_GL_MINB 5
-#endif
-#ifndef TAD_HL_MINB
-#define TAD_HL_MINB 5
-#endif
-constexpr int GL_MIN_BLOCKS = TAD_GL_MINB;
-constexpr int HL_MIN_BLOCKS = TAD_HL_MINB;
+/* Minimum resident 96-thread blocks per SM of the two kernels: 5, i.e. at
+   most 128 registers a thread.  The gradient lanes then keep 984 B of
+   spill and the Hessian lanes 112 B; measured on the 48^3 cube (projected
+   evaluation with both kernels): 3.52 ms at 5 / 5, 3.72 ms with 168
+   registers for the gradient lanes (316 B of spill), and unbounded (255
+   registers) they ran slower still -- occupancy pays more than the spill. */
+constexpr int GL_MIN_BLOCKS = 5;
+constexpr int HL_MIN_BLOCKS = 5;
 
 template <int d, int N, typename Energy>
 __global__ void __launch_bounds__(3 * GL_ELEMS, GL_MIN_BLOCKS) k_elem_grad_lanes(ElemLaunch L, Energy energy)
