@@ -362,10 +362,13 @@ def measure_batch(args, rank: int, n_meshes: int, sequential: bool = True) -> di
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         if name == "mixed":
             clk.mark()
+            torch.cuda.profiler.start()   # an ncu launch list with --profile-from-start off covers these iterations
         e0.record(stream)
         b.newton_solve_device(x.data_ptr(), args.steps)
         e1.record(stream)
         torch.cuda.synchronize()
+        if name == "mixed":
+            torch.cuda.profiler.stop()
         clk.unmark()
         ms = e0.elapsed_time(e1)
         fh = b.newton_solve_device(x.data_ptr(), 1, history=True)
