@@ -22,6 +22,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import platform
 import subprocess
 import sys
 import threading
@@ -244,6 +245,24 @@ def cpu_sample(full_w):
     return make_workload("tet24" if full_w.name.startswith("tet") else CPU_SAMPLE)
 
 
+def host_cpu() -> dict:
+    """The host the CPU legs ran on: hardware threads and the CPU model (lscpu's
+    "Model name", else /proc/cpuinfo's "model name", else the machine type)."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        model = next((l.split(":", 1)[1].strip() for l in out.splitlines() if l.startswith("Model name")), None)
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if not model:
+        try:
+            with open("/proc/cpuinfo") as f:
+                model = next((l.split(":", 1)[1].strip() for l in f if l.lower().startswith("model name")), None)
+        except OSError:
+            pass
+    return {"nproc": os.cpu_count(), "model": model or platform.machine()}
+
+
 def cpu_baseline(full_w, threads: int | None = None) -> dict:
     """One oracle Projected-Newton iteration (OpenMP element eval, serial
     scatter + triplet sort, sparse LDL^T, Armijo) on cpu_sample(full_w),
@@ -262,7 +281,7 @@ def cpu_baseline(full_w, threads: int | None = None) -> dict:
                        f"element eval + projection, serial triplet assembly, sparse LDL^T, Armijo) on {CPU} "
                        f"({w.n_elements} elements) = {dt:.2f} s, scaled by elements to {full_w.n_elements} "
                        f"(linear scaling; the LDL^T grows faster, so this favours the CPU)"),
-            "stage_s": {"eval_assemble": times[0], "ldlt": times[1], "line_search": times[2]}}
+            "stage_s": {"eval_assemble": times[0], "ldlt": times[1], "line_search": times[2]}, "host": host_cpu()}
 
 
 REF_BUDGET_S = 150.0   # timed Newton iterations of the reference arm stop once the next would pass this
@@ -328,7 +347,8 @@ def run_reference(args):
             "config": {"workload": workload_desc(w)},
             "seconds_per_iteration": per_iter,
             "stage_s": {"eval_assemble": stages[0], "factor_solve": stages[1], "line_search": stages[2]},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": p.n_threads, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": p.n_threads, "kind": "port", "sample": sample,
+                             "host": host_cpu()},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

@@ -26,6 +26,7 @@ def test_reference_arm_line():
     assert d["config"]["workload"].startswith("disk64")
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and "disk64" in cb["sample"]
+    assert cb["host"]["nproc"] >= cb["cores"] and cb["host"]["model"]
     e2e = d["e2e"]
     assert e2e["value"] == d["value"] and e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
 
