@@ -284,7 +284,7 @@ def cpu_baseline(full_w, threads: int | None = None) -> dict:
             "stage_s": {"eval_assemble": times[0], "ldlt": times[1], "line_search": times[2]}, "host": host_cpu()}
 
 
-REF_BUDGET_S = 150.0   # timed Newton iterations of the reference arm stop once the next would pass this
+REF_TIME_LIMIT_S = 150.0   # timed Newton iterations of the reference arm stop once the next would pass this
 
 
 def run_reference(args):
@@ -295,7 +295,7 @@ def run_reference(args):
     Hessian's sparsity, the fill-reducing ordering and the symbolic LDL^T) runs
     untimed first, as the reference caches it across iterations
     (LinearSolver.hh:12-19).  Full Newton iterations are then timed one at a
-    time, as many as fit REF_BUDGET_S (at least one, at most --steps), after
+    time, as many as fit REF_TIME_LIMIT_S (at least one, at most --steps), after
     the requested warm-up iterations when they are cheap: on the 1.64M-face
     disk one iteration takes about a minute, so only one warm-up iteration
     runs there, and "steps" / "warmup" give the counts actually run."""
@@ -311,14 +311,14 @@ def run_reference(args):
     t_prep = time.perf_counter() - t0
     x = w.x0.copy()
     # warm-up iterations while they are cheap: all W when W times the first
-    # one's cost fits half the budget, else only that first one
+    # one's cost fits half the time limit, else only that first one
     warm = 0
     if args.warmup > 0:
         t0 = time.perf_counter()
         x, _, _ = p.newton(x, 1)
         t_first = time.perf_counter() - t0
         warm = 1
-        if args.warmup * t_first <= 0.5 * REF_BUDGET_S:
+        if args.warmup * t_first <= 0.5 * REF_TIME_LIMIT_S:
             for _ in range(args.warmup - 1):
                 x, _, _ = p.newton(x, 1)
             warm = args.warmup
@@ -331,7 +331,7 @@ def run_reference(args):
         per_iter.append(dt)
         stages += times[:3]
         total += dt
-        if total + dt > REF_BUDGET_S:
+        if total + dt > REF_TIME_LIMIT_S:
             break
     n = len(per_iter)
     v = n / total
@@ -339,7 +339,7 @@ def run_reference(args):
               f"after {warm} untimed warm-up iteration(s)) of the oracle, the CPU restatement of the reference path "
               f"(OpenMP element evaluation + projection, serial triplet assembly, sparse LDL^T with a "
               f"nested-dissection ordering, Armijo), on the benchmark workload itself ({w.name}, {w.n_elements} "
-              f"elements); pattern analysis {t_prep:.1f} s untimed; iterations stop at a {REF_BUDGET_S:.0f} s budget")
+              f"elements); pattern analysis {t_prep:.1f} s untimed; iterations stop at a {REF_TIME_LIMIT_S:.0f} s limit")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": n, "steps_requested": args.steps, "warmup": warm, "warmup_requested": args.warmup,
             "ms_per_step": total / n * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

@@ -2,7 +2,7 @@
  * ORACLE -- test infrastructure only.  Not part of the product.
  *
  * CPU restatement of TinyAD's sparse per-element derivative path, used by
- * tests/ as the parity checker and by bench.py as the CPU baseline.  It is
+ * tests/ as the parity reference and by bench.py as the CPU baseline.  It is
  * written from the reference's behaviour, file by file:
  *
  *   Element access, first-access local order    include/TinyAD/Detail/Element.hh:159-260

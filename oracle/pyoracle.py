@@ -2,7 +2,7 @@
 
 ctypes front end of the CPU restatement in oracle/oracle.cpp.  Only tests/,
 __graft_entry__.smoke() and bench.py's CPU-baseline leg import this module,
-and only as the checker / the timed CPU baseline.
+and only as the parity reference / the timed CPU baseline.
 """
 from __future__ import annotations
 
